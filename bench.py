@@ -1,0 +1,326 @@
+"""Benchmark: ground-classified Mpts/s on one GB300 (whole pipeline per step).
+
+A step is one pass of the hot path over one synthetic cloud: octree build
+(decode, keys, sort, de-duplication, leaves, store order, node hierarchy),
+tile scan + postscan, and per-point classification.  The default workload is
+50M points over 700 x 700 m (about 100 pts/m^2), 1 mm quantisation, seeded.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value:  points / second with the cloud already resident in HBM (device
+        pointer in, device class bytes out), CUDA events on the library's
+        stream, max over ranks.
+e2e:    the same through wb_classify_cloud with pinned host buffers: the
+        int32 XYZ copy in and the class-byte copy out are inside the timing.
+--impl reference: the reference's CPU algorithm (the oracle restatement,
+        oracle/) on this machine's cores, on a bounded sample of the workload.
+Multi-GPU runs are independent replicas (one cloud per rank, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ground-classified Mpts/s on 1 GB300, served vs plain, at >=99.99% label match"
+UNIT = "Mpts/s"
+CLASSIFY_BYTES_PER_POINT = 13     # 12 B int32 XYZ read + 1 B class written
+BUILD_BYTES_PER_POINT = 28        # 12 B read, 12 B leaf-ordered XYZ + 4 B index written
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def crop(cloud, n_target, seed=0):
+    """A square window of the cloud holding about n_target points (same density and terrain)."""
+    from wolkenbase_gb300 import synth
+    d = cloud.decoded()
+    lo = d.min(axis=0)
+    hi = d.max(axis=0)
+    frac = min(1.0, n_target / cloud.n)
+    side = math.sqrt(frac) * min(hi[0] - lo[0], hi[1] - lo[1])
+    cx = (lo[0] + hi[0]) / 2
+    cy = (lo[1] + hi[1]) / 2
+    m = (np.abs(d[:, 0] - cx) <= side / 2) & (np.abs(d[:, 1] - cy) <= side / 2)
+    sub = synth.Cloud(cloud.xyz[m], cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+    ds = d[m]
+    sub.minc = tuple(float(v) / cloud.unit for v in ds.min(axis=0))
+    sub.maxc = tuple(float(v) / cloud.unit for v in ds.max(axis=0))
+    return sub, side
+
+
+def cpu_sample(cloud, n_sample, threads, reps=1):
+    from oracle import oracle as O
+    O.build()
+    sub, side = crop(cloud, n_sample)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.run(sub, threads=threads)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return sub.n / best / 1e6, sub.n, side, best
+
+
+def workload(args, rank):
+    from wolkenbase_gb300 import synth
+    side = 700.0 * math.sqrt(args.points / 50_000_000)
+    cloud = synth.terrain_cloud(args.points, side, side, args.seed + rank)
+    cfg = {"workload": f"plain_scale: {args.points} pts over {side:.0f} x {side:.0f} m, 1 mm int32 LAS XYZ, "
+                       "4-sinusoid terrain + 2 cm noise, 10% buildings 3-15 m, 10% vegetation 0.5-10 m",
+           "points": args.points, "area_m": [round(side, 1), round(side, 1)], "seed": args.seed,
+           "params": {"tile_size": 1.0, "max_slope": 1.0, "thickness": 0.0, "min_hyp_size": 0.1},
+           "l2": "inputs larger than L2 (int32 XYZ + leaf-ordered store >> 126 MB)"}
+    return cloud, cfg
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    cloud, cfg = workload(args, 0)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, n_s, side, dt = cpu_sample(cloud, args.ref_sample, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    sample = (f"square crop of the workload, {n_s} points ({side:.1f} m side, same density and terrain), "
+              "octree build + scan + postscan + classify")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_s / value / 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": cfg,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--points", type=int, default=50_000_000)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=150_000, help="points in the CPU-baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=40_000, help="points per step of the reference arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import wolkenbase_gb300 as wb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cloud, cfg = workload(args, rank)
+    n = cloud.n
+    params = wb.Params()
+    stream = torch.cuda.Stream()
+    clf = wb.Classifier(local)
+    clf.set_stream(stream.cuda_stream)
+
+    dev_xyz = torch.from_numpy(np.ascontiguousarray(cloud.xyz)).to(f"cuda:{local}")
+    dev_cls = torch.zeros(n, dtype=torch.uint8, device=f"cuda:{local}")
+    cs_dev = wb.cloud_struct(dev_xyz.data_ptr(), n, 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc,
+                             cloud.maxc, device_resident=True)
+    import ctypes as C
+
+    def step_dev():
+        rc = clf.L.wb_classify_cloud(clf.ctx, C.byref(cs_dev), C.byref(params.c()), C.c_void_p(dev_cls.data_ptr()))
+        clf._check(rc)
+
+    for _ in range(args.warmup):
+        step_dev()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # device-resident timed region
+    clf.profile(True)
+    stage_acc = {}
+    launches0 = clf.launch_count()
+    barrier()
+    with ClockSampler(local) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_dev()
+            for name, ms in clf.stage_times():
+                stage_acc[name] = stage_acc.get(name, 0.0) + ms
+        ev1.record(stream)
+        barrier()
+    launches = clf.launch_count() - launches0
+    clf.profile(False)
+    ms_total = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = world * n / (ms_step / 1e3) / 1e6
+    cls_dev = dev_cls.cpu().numpy()
+
+    # end-to-end through the public API with pinned host buffers
+    pin_xyz = torch.from_numpy(np.ascontiguousarray(cloud.xyz)).pin_memory()
+    pin_cls = torch.zeros(n, dtype=torch.uint8).pin_memory()
+    cs_host = wb.cloud_struct(pin_xyz.data_ptr(), n, 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc,
+                              cloud.maxc, device_resident=False)
+
+    def step_host():
+        rc = clf.L.wb_classify_cloud(clf.ctx, C.byref(cs_host), C.byref(params.c()), C.c_void_p(pin_cls.data_ptr()))
+        clf._check(rc)
+
+    step_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n / e2e_s / 1e6
+    same = bool(np.array_equal(pin_cls.numpy(), cls_dev))
+
+    info = clf.info()
+    stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
+    dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download")), key=lambda k: stage_ms[k])
+    peak, peak_kind = peaks()
+    nd = info["n_distinct"]
+    alg_bytes = {"classify": CLASSIFY_BYTES_PER_POINT * nd}.get(dom, None)
+    roof = None
+    if alg_bytes:
+        achieved = alg_bytes / (stage_ms[dom] / 1e3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            tr = json.load(open(tp)).get(dom)
+            if tr:
+                traffic = float(tr["bytes_per_point"]) * nd
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes": alg_bytes, "avg_ms": stage_ms[dom]}
+    build_ms = sum(v for k, v in stage_ms.items() if k in ("decode_key", "sort", "dedup", "leaves", "leaf_order",
+                                                         "point_map", "nodes"))
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n_s, side, dt = cpu_sample(cloud, args.cpu_sample, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"square crop of the workload, {n_s} points ({side:.1f} m side), full pipeline, "
+                         f"{dt:.1f} s on {threads} threads"}
+    clk = clocks.summary()
+    labels = np.bincount(cls_dev, minlength=3)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n, "d2h_bytes_per_step": n,
+                   "same_labels_as_device_run": same},
+           "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+           "stages_ms": {k: round(v, 3) for k, v in stage_ms.items()},
+           "build": {"ms": build_ms, "achieved_GBps": BUILD_BYTES_PER_POINT * n / (build_ms / 1e3) / 1e9
+                     if build_ms else None, "frac": (BUILD_BYTES_PER_POINT * n / (build_ms / 1e3) / 1e9) / peak
+                     if build_ms else None, "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT},
+           "octree": {"leaves": info["n_leaves"], "distinct": nd, "max_depth": info["max_depth"]},
+           "labels": {"ground": int(labels[2]), "not_ground": int(labels[1]), "untouched": int(labels[0])}}
+    if rank == 0:
+        print(json.dumps(out))
+    clf.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/* wolkenbase_gb300 -- GPU (sm_103a) replacement for wolkenbase's classification
+ * hot path behind a plain C ABI.
+ *
+ * The reference runs this path in-process through C++ globals:
+ *   Octree octRoot / OctStore octStore   (octree.h:55-212, octree.cpp:37-38)
+ *   Flowsnake snake, harray<Tile> tiles  (threads.cpp:69, tile.cpp:27)
+ *   scanCylinder / postscanCylinder      (scan.h:27-28)
+ *   classifyCylinder                     (classify.h:24)
+ * driven phase by phase by WolkenThread (threads.cpp:446-695).  Here one
+ * context owns the device-resident octree, point store and tile table for one
+ * cloud; each call below replaces one of those phases for the whole cloud.
+ *
+ * Conventions: every function returns 0 on success or a negative WB_E* code;
+ * wb_last_error() describes the last failure.  No exception crosses the ABI.
+ * The caller owns every host array; the context owns all device memory.  A
+ * context is not thread-safe: use one per host thread.  Host arrays may be
+ * pageable or pinned; pinned buffers make the copies asynchronous.
+ */
+#ifndef WOLKENBASE_GB300_H
+#define WOLKENBASE_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WB_OK 0
+#define WB_EINVAL -1      /* bad argument                                    */
+#define WB_ENOMEM -2      /* device allocation failed or HBM budget exceeded */
+#define WB_ECUDA -3       /* a CUDA call failed                              */
+#define WB_EDEPTH -4      /* a leaf would lie deeper than 21 levels          */
+#define WB_ESTATE -5      /* call out of order (e.g. classify before build)  */
+#define WB_ETIMEDOUT -6   /* a bounded device-side wait gave up              */
+#define WB_ENOTFOUND -7   /* no such job / entry                             */
+
+typedef struct wb_ctx wb_ctx;
+
+/* Classification settings; defaults as MainWindow::readSettings
+ * (mainwindow.cpp:407-410) and scan.cpp:29. */
+typedef struct
+{
+  double tile_size;     /* WolkenCanvas::tileSize, 1 m        */
+  double max_slope;     /* maxSlope, 1                        */
+  double thickness;     /* thickness, 0 m                     */
+  double min_hyp_size;  /* minHyperboloidSize, 0.1 m          */
+} wb_params;
+
+/* One LAS point block as LasHeader::readPoint sees it (las.cpp:735-820).
+ * records[i*stride + 0..11] hold the little-endian int32 X, Y, Z of point i
+ * (true for every LAS point format); stride is the point record length
+ * (12 for packed XYZ, 28 for format 1).  Coordinates decode as
+ * (offset + scale*X) * unit, exactly las.cpp:808.  minc/maxc are the header's
+ * min/max corner in file units (LasHeader::minCorner/maxCorner, las.cpp:704-712),
+ * which size the octree root and the tile grid (wolkencanvas.cpp:497-520). */
+typedef struct
+{
+  const void *records;
+  uint64_t n;
+  uint32_t stride;
+  uint32_t device_resident;   /* 1: records is a device pointer      */
+  double scale[3], offset[3], unit;
+  double minc[3], maxc[3];
+} wb_cloud;
+
+typedef struct
+{
+  uint64_t n_points;        /* input records                                    */
+  uint64_t n_distinct;      /* after exact-xyz de-duplication (octree.cpp:620-644) */
+  uint64_t n_leaves;        /* leaf blocks (OctStore::getNumBlocks, octree.h:168) */
+  uint32_t max_depth;       /* deepest leaf level below the root                */
+  uint32_t pad;
+  double root_center[3], root_side;    /* Octree::sizeFit (octree.cpp:268-310)  */
+  double tile_center[3], tile_side;    /* cube handed to Flowsnake::setSize     */
+  double spacing;                       /* Flowsnake::getSpacing                 */
+  uint64_t n_tiles;                     /* Gosper island size (hiLim-loLim+1)    */
+  int32_t tile_lo, tile_hi;             /* flowsnake counter range               */
+} wb_octree_stats;
+
+/* Per-tile results of scan + postscan (Tile, tile.h:27-35), flowsnake order. */
+typedef struct
+{
+  int32_t ex, ey;            /* Eisenstein tile address                    */
+  int32_t n_points, n_ground;
+  int32_t tree_flags, pad;
+  double density, h_scan, hyperboloid_size, height;
+} wb_tile;
+
+/* Replaces octStore.open + startThreads (wolkenbase.cpp:75-76, threads.cpp:91).
+ * device: CUDA ordinal.  hbm_budget: bytes this context may allocate (0 = no
+ * limit).  Returns NULL on failure (see wb_last_error(NULL)). */
+wb_ctx *wb_open(int device, size_t hbm_budget);
+void wb_close(wb_ctx *ctx);
+const char *wb_last_error(const wb_ctx *ctx);
+/* Work is issued on this stream (a cudaStream_t); NULL = the context's own. */
+int wb_set_stream(wb_ctx *ctx, void *cuda_stream);
+int wb_synchronize(wb_ctx *ctx);
+
+/* Octree::sizeFit + OctStore::put for every record + OctStore::split
+ * (octree.cpp:268-347, 620-662, 849-876, 1295-1338).  Leaf cubes and the
+ * point->leaf map equal the reference's; leaves are numbered in depth-first
+ * sub[0..7] order (the order Octree::findBlocks visits them).  Asynchronous
+ * on the context's stream. */
+int wb_octree_build(wb_ctx *ctx, const wb_cloud *cloud);
+int wb_octree_info(wb_ctx *ctx, wb_octree_stats *out);
+
+/* Leaf table: center xyz + side (4 doubles per leaf), first store slot and
+ * point count per leaf (Octree::cube + OctBuffer::countPoints). */
+int wb_octree_leaves(wb_ctx *ctx, double *center_side, uint32_t *first, uint32_t *count);
+
+/* Octree::findBlock for every input record: leaf index (same numbering). */
+int wb_octree_point_leaf(wb_ctx *ctx, uint32_t *leaf_of_point);
+
+/* The point store: input index of each distinct point in store order (leaf
+ * by leaf; inside a leaf by input index, the survivor of duplicates being
+ * the last one read, as OctBuffer::put keeps it). */
+int wb_octree_store_order(wb_ctx *ctx, uint32_t *input_index);
+
+/* Octree::findBlock for arbitrary positions (m xyz triples, doubles):
+ * leaf index, or -1 where findBlock would return -1. */
+int wb_octree_find_block(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *leaf);
+
+/* scanCylinder over every tile then postscanCylinder over every tile
+ * (scan.cpp:31-179), in flowsnake order. */
+int wb_scan_tiles(wb_ctx *ctx, const wb_params *params);
+int wb_tiles(wb_ctx *ctx, wb_tile *out, uint64_t capacity, uint64_t *count);
+
+/* classifyCylinder over every tile (classify.cpp:96-173).  cls is per input
+ * record: on entry the caller's current class byte (the LAS classification,
+ * 0 for a fresh cloud); on return every point that lies in a tile cylinder
+ * holds 1 (not ground) or 2 (ground), written by the last tile in flowsnake
+ * order that contains it; other bytes are left unchanged.  cls may be a host
+ * or (cls_on_device=1) a device pointer. */
+int wb_classify(wb_ctx *ctx, const wb_params *params, uint8_t *cls, int cls_on_device);
+
+/* Build + scan + postscan + classify in one call. */
+int wb_classify_cloud(wb_ctx *ctx, const wb_cloud *cloud, const wb_params *params, uint8_t *cls);
+
+/* Timing of the last pipeline run, per stage, from CUDA events on the
+ * context's stream (milliseconds).  names/ms arrays of capacity entries;
+ * returns the number of stages via *count. */
+int wb_stage_times(wb_ctx *ctx, const char **names, float *ms, uint32_t capacity, uint32_t *count);
+
+/* Enables or disables the per-stage events (off by default). */
+int wb_profile(wb_ctx *ctx, int enable);
+
+/* Kernels this context has launched since wb_open (no reference counterpart:
+ * accounting for timed regions). */
+int wb_launch_count(wb_ctx *ctx, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -48,6 +48,34 @@ double nowSec()
 inline double sq(double x) { return x * x; }
 inline double cube3(double x) { return x * x * x; }
 
+/* The C library hypot that the reference calls (point.cpp:189-192,
+ * shape.cpp:127-135, 214-218) is, in the x86-64 glibc the oracle is pinned
+ * against, the corrected square root of Borges, "An Improved Algorithm for
+ * hypot(a,b)" (2019), non-fused form.  Restating it here keeps the oracle's
+ * results identical on hosts whose libm uses the fused form instead. */
+double hypotR(double a, double b)
+{
+  double ax = fabs(a), ay = fabs(b);
+  if (ay > ax)
+    std::swap(ax, ay);
+  if (ay == 0)
+    return ax;
+  double h = sqrt(ax * ax + ay * ay), t1, t2;
+  if (h <= 2.0 * ay)
+  {
+    double d = h - ay;
+    t1 = ax * (2.0 * d - ax);
+    t2 = (d - 2.0 * (ax - ay)) * d;
+  }
+  else
+  {
+    double d = h - ax;
+    t1 = 2.0 * d * (ax - 2.0 * ay);
+    t2 = (4.0 * d - ay) * ay + d * d;
+  }
+  return h - (t1 + t2) / (2.0 * h);
+}
+
 /* ---------------- integer angles (angle.cpp:117-155, 305-320) ---------------- */
 
 double gTan[511], gSin[512], gCos[512];
@@ -335,7 +363,7 @@ struct HyperboloidR : Shape
   }
   bool in(const V3 &p) const override
   {
-    double xyd = hypot(ctr.x - p.x, ctr.y - p.y);
+    double xyd = hypotR(ctr.x - p.x, ctr.y - p.y);
     double zd = ctr.z - p.z;
     if (slope > 0)
       return zd > 0 && sq(zd) - sq(xyd * slope) >= por2;
@@ -356,7 +384,7 @@ struct CylinderR : Shape
 {
   double cx, cy, r;
   CylinderR(double x, double y, double rad) : cx(x), cy(y), r(rad) {}
-  bool in(const V3 &p) const override { return hypot(cx - p.x, cy - p.y) <= r; }
+  bool in(const V3 &p) const override { return hypotR(cx - p.x, cy - p.y) <= r; }
   V3 closest(const CubeR &c) const override
   {
     return V3{clampToward(cx, c.c.x, c.side), clampToward(cy, c.c.y, c.side), c.c.z};
@@ -756,7 +784,7 @@ struct Pipeline
     double sl[3];
     lsqPlane(px.data(), py.data(), pz.data(), (unsigned)n, sl);
     double sx = sl[0], sy = sl[1];
-    double len = hypot(sx, sy);
+    double len = hypotR(sx, sy);
     if (len > 1)
     {
       sx /= len;
@@ -790,7 +818,7 @@ struct Pipeline
         if (sector < 0)
           sector += 6;
         sector = (sector % 6) + 1;
-        if (hypot(px[i], py[i]) < cyl.r / kSqrt7)
+        if (hypotR(px[i], py[i]) < cyl.r / kSqrt7)
           sector = 0;
         histo[sector]++;
       }
@@ -891,7 +919,7 @@ struct Pipeline
       for (size_t j = 0; j < down.size() && !above; j++)
       {
         const V3 &q = st.loc[down[j]];
-        if (hyp.in(q) && hypot(p.x - q.x, p.y - q.y) != 0)
+        if (hyp.in(q) && hypotR(p.x - q.x, p.y - q.y) != 0)
           dirs.insert(atan2iR(q.y - p.y, q.x - p.x));
         if (surround(dirs))
           above = true;
@@ -901,7 +929,7 @@ struct Pipeline
       for (size_t j = 0; j < down.size() && !above; j++)
       {
         const V3 &q = st.loc[down[j]];
-        if (hypot(p.x - q.x, p.y - q.y) != 0)
+        if (hypotR(p.x - q.x, p.y - q.y) != 0)
           dirs.insert(atan2iR(q.y - p.y, q.x - p.x));
         if (surround(dirs))
           above = true;

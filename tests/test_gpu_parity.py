@@ -1,0 +1,137 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+Octree: leaf cubes and the point->leaf map must equal the reference's exactly.
+Scan: every per-tile field must equal the oracle's run in the same point order
+(each block's points in input order) exactly.  Classes: identical to the
+oracle in that order; against the reference's serial run the bar is 99.99%
+(LABEL_TOL below), since the serial driver's per-block storage order feeds
+the scan's "second lowest point".
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_cloud, golden_params, load_golden
+
+pytestmark = pytest.mark.gpu
+LABEL_TOL = 1e-4   # fraction of labels allowed to differ from the reference's serial run
+
+
+def _params(g):
+    import wolkenbase_gb300 as wb
+    return wb.Params(**golden_params(g))
+
+
+def _gpu_run(classifier, cloud, params, phases=3):
+    classifier.build(cloud)
+    out = {"info": classifier.info()}
+    cs, first, count = classifier.leaves()
+    out.update(cs=cs, first=first, count=count, pleaf=classifier.point_leaf(), order=classifier.store_order())
+    if phases >= 2:
+        classifier.scan(params)
+        out["tiles"] = classifier.tiles()
+    if phases >= 3:
+        out["cls"] = classifier.classify(params)
+    return out
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_octree_matches_reference(classifier, case):
+    g = load_golden(case)
+    cloud = golden_cloud(g)
+    r = _gpu_run(classifier, cloud, _params(g), phases=1)
+    stored = g["block"] >= 0
+    assert r["info"]["n_leaves"] == int(g["n_blocks"])
+    assert r["info"]["n_distinct"] == int(stored.sum())
+    assert np.array_equal(np.array(list(r["info"]["root_center"]) + [r["info"]["root_side"]]), g["root"])
+    cubes = r["cs"][r["pleaf"]]
+    assert np.array_equal(cubes[stored], g["leaf_cube"][stored])
+    # the point store holds exactly the surviving records, in input order inside each leaf
+    assert np.array_equal(np.sort(r["order"]), np.nonzero(stored)[0].astype(np.uint32))
+    for l in range(len(r["first"])):
+        seg = r["order"][r["first"][l]:r["first"][l] + r["count"][l]]
+        assert np.all(np.diff(seg.astype(np.int64)) > 0)
+    assert r["count"].max() <= 537
+    # Octree::findBlock on the decoded points agrees with the map
+    fb = classifier.find_block(cloud.decoded())
+    assert np.array_equal(fb, r["pleaf"].astype(np.int64))
+
+
+@pytest.mark.parametrize("case", [c for c in GOLDEN_CASES if c != "split"])
+def test_scan_and_classify_match(classifier, oracle_mod, case):
+    g = load_golden(case)
+    cloud = golden_cloud(g)
+    r = _gpu_run(classifier, cloud, _params(g))
+    o = oracle_mod.run(cloud, canonical_order=True, threads=8, **golden_params(g))
+    t, ot = r["tiles"], o["tiles"]
+    assert np.array_equal(t["ex"], ot["ex"]) and np.array_equal(t["ey"], ot["ey"])
+    for f, of in (("n_points", "n_points"), ("tree_flags", "tree_flags"), ("density", "density"),
+                  ("h_scan", "h_scan"), ("hyperboloid_size", "h_final"), ("height", "height")):
+        assert np.array_equal(t[f], ot[of]), f
+    # n_points does not depend on point order: equal to the reference's too
+    assert np.array_equal(t["n_points"], g["tiles"]["n_points"])
+    assert np.array_equal(r["cls"], o["cls"])
+    diff = int(np.sum(r["cls"] != g["cls"]))
+    assert diff <= LABEL_TOL * cloud.n, f"{diff} labels differ from the reference's serial run"
+
+
+@pytest.mark.parametrize("seed,n", [(101, 60000), (202, 30000)])
+def test_random_tiles_match_oracle(classifier, oracle_mod, seed, n):
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    cloud = synth.density_tile(n, seed)
+    r = _gpu_run(classifier, cloud, wb.Params())
+    o = oracle_mod.run(cloud, canonical_order=True, threads=16)
+    assert np.array_equal(r["tiles"]["hyperboloid_size"], o["tiles"]["h_final"])
+    assert np.array_equal(r["cls"], o["cls"])
+    assert np.array_equal(r["cs"][r["pleaf"]], o["leaves"][o["leaf"]])
+
+
+def test_large_cloud_properties(classifier):
+    """Size-independent checks at 4M points: determinism, leaf invariants,
+    input-order independence of the octree."""
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    cloud = synth.density_tile(4_000_000, 9)
+    a = _gpu_run(classifier, cloud, wb.Params())
+    b = _gpu_run(classifier, cloud, wb.Params())
+    assert np.array_equal(a["cls"], b["cls"])
+    assert np.array_equal(a["tiles"]["hyperboloid_size"], b["tiles"]["hyperboloid_size"])
+    assert a["count"].max() <= 537 and a["count"].min() >= 1
+    assert a["count"].sum() == a["info"]["n_distinct"]
+    # every point lies in its leaf cube (closed cube, as Cube::in)
+    d = cloud.decoded()
+    c = a["cs"][a["pleaf"]]
+    assert np.all(np.abs(d - c[:, :3]) <= c[:, 3:4] / 2)
+    # leaf cubes do not depend on the input order
+    perm = np.random.default_rng(1).permutation(cloud.n)
+    c2 = synth.Cloud(cloud.xyz[perm], cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+    classifier.build(c2)
+    cs2, _, _ = classifier.leaves()
+    pl2 = classifier.point_leaf()
+    cubes2 = np.empty_like(c)
+    cubes2[perm] = cs2[pl2]
+    assert np.array_equal(c, cubes2)
+    labels = np.bincount(a["cls"], minlength=3)
+    assert labels[0] < cloud.n * 0.01 and labels[1] > 0 and labels[2] > 0
+
+
+def test_classify_cloud_one_call(classifier, oracle_mod):
+    """wb_classify_cloud (host in, host out) equals the staged calls."""
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    cloud = synth.density_tile(20000, 33)
+    staged = _gpu_run(classifier, cloud, wb.Params())["cls"]
+    one = classifier.classify_cloud(cloud, wb.Params())
+    assert np.array_equal(staged, one)
+
+
+def test_classify_keeps_unclassified_bytes(classifier):
+    """Points outside every tile cylinder keep the caller's class byte."""
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    cloud = synth.density_tile(5000, 44)
+    classifier.build(cloud)
+    classifier.scan(wb.Params())
+    cls = np.full(cloud.n, 7, np.uint8)
+    out = classifier.classify(wb.Params(), cls)
+    assert set(np.unique(out)) <= {1, 2, 7}

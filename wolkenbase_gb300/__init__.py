@@ -1,0 +1,194 @@
+"""wolkenbase_gb300: wolkenbase's ground-classification hot path on one GB300.
+
+The compute lives in libwolkenbase_gb300.so (hand-written sm_103a CUDA behind
+the C ABI of include/wolkenbase_gb300.h).  This module is the Python host
+mirror of the reference's interface for that path:
+
+  reference (phma/wolkenbase)                     here
+  ---------------------------------------------   ------------------------------
+  octRoot.sizeFit + octStore.put (octree.cpp)     Classifier.build(cloud)
+  Octree::findBlock / findCube (octree.cpp:199)   Classifier.find_block(xyz)
+  OctStore::getNumBlocks / getAll                 Classifier.leaves(), store_order()
+  scanCylinder + postscanCylinder (scan.cpp)      Classifier.scan(params)
+  classifyCylinder (classify.cpp:96)              Classifier.classify(params, cls)
+  Tile (tile.h:27-35)                             Classifier.tiles()
+
+Errors raise WolkenbaseError carrying the C status code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+from ._lib import wb_cloud, wb_octree_stats, wb_params, wb_tile
+
+__all__ = ["Params", "Classifier", "WolkenbaseError", "cloud_struct"]
+
+
+class WolkenbaseError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_lib.ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+@dataclasses.dataclass
+class Params:
+    """Classification settings with the reference's defaults (mainwindow.cpp:407-410)."""
+    tile_size: float = 1.0
+    max_slope: float = 1.0
+    thickness: float = 0.0
+    min_hyp_size: float = 0.1
+
+    def c(self):
+        return wb_params(self.tile_size, self.max_slope, self.thickness, self.min_hyp_size)
+
+
+TILE_DTYPE = np.dtype([("ex", "<i4"), ("ey", "<i4"), ("n_points", "<i4"), ("n_ground", "<i4"),
+                       ("tree_flags", "<i4"), ("pad", "<i4"), ("density", "<f8"), ("h_scan", "<f8"),
+                       ("hyperboloid_size", "<f8"), ("height", "<f8")])
+
+
+def cloud_struct(records, n, stride, scale, offset, unit, minc, maxc, device_resident=False):
+    """Builds a wb_cloud for a host array (numpy) or a device pointer (int)."""
+    cs = wb_cloud()
+    if isinstance(records, np.ndarray):
+        cs.records = records.ctypes.data
+    else:
+        cs.records = int(records)
+    cs.n = n
+    cs.stride = stride
+    cs.device_resident = 1 if device_resident else 0
+    cs.scale[:] = scale
+    cs.offset[:] = offset
+    cs.unit = unit
+    cs.minc[:] = minc
+    cs.maxc[:] = maxc
+    return cs
+
+
+class Classifier:
+    """One device context: octree, point store and tile table of one cloud."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self.L = _lib.load()
+        self.ctx = self.L.wb_open(device, hbm_budget)
+        if not self.ctx:
+            raise WolkenbaseError(_lib.WB_ECUDA, self.L.wb_last_error(None).decode())
+        self._keep = None
+
+    def close(self):
+        if self.ctx:
+            self.L.wb_close(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WolkenbaseError(rc, self.L.wb_last_error(self.ctx).decode())
+
+    # -- octree / point store --
+    def build(self, cloud):
+        """Octree::sizeFit + OctStore::put of every point of a synth.Cloud-like object."""
+        xyz = np.ascontiguousarray(cloud.xyz, dtype=np.int32)
+        self._keep = xyz
+        cs = cloud_struct(xyz, xyz.shape[0], 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+        self._check(self.L.wb_octree_build(self.ctx, C.byref(cs)))
+        self.synchronize()
+
+    def build_records(self, cs):
+        self._check(self.L.wb_octree_build(self.ctx, C.byref(cs)))
+
+    def synchronize(self):
+        self._check(self.L.wb_synchronize(self.ctx))
+
+    def set_stream(self, stream_handle):
+        self._check(self.L.wb_set_stream(self.ctx, C.c_void_p(stream_handle)))
+
+    def info(self):
+        s = wb_octree_stats()
+        self._check(self.L.wb_octree_info(self.ctx, C.byref(s)))
+        return {f: (tuple(getattr(s, f)) if f in ("root_center", "tile_center") else getattr(s, f))
+                for f, _ in s._fields_ if f != "pad"}
+
+    def leaves(self):
+        """(center_side (L,4) float64, first (L,) uint32, count (L,) uint32), depth-first order."""
+        L = self.info()["n_leaves"]
+        cs = np.zeros((L, 4))
+        first = np.zeros(L, np.uint32)
+        count = np.zeros(L, np.uint32)
+        self._check(self.L.wb_octree_leaves(self.ctx, cs.ctypes.data, first.ctypes.data, count.ctypes.data))
+        return cs, first, count
+
+    def point_leaf(self):
+        n = self.info()["n_points"]
+        out = np.zeros(n, np.uint32)
+        self._check(self.L.wb_octree_point_leaf(self.ctx, out.ctypes.data))
+        return out
+
+    def store_order(self):
+        nd = self.info()["n_distinct"]
+        out = np.zeros(nd, np.uint32)
+        self._check(self.L.wb_octree_store_order(self.ctx, out.ctypes.data))
+        return out
+
+    def find_block(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(xyz.shape[0], np.int64)
+        self._check(self.L.wb_octree_find_block(self.ctx, xyz.ctypes.data, xyz.shape[0], out.ctypes.data))
+        return out
+
+    # -- tiles --
+    def scan(self, params=None):
+        p = (params or Params()).c()
+        self._check(self.L.wb_scan_tiles(self.ctx, C.byref(p)))
+        self.synchronize()
+
+    def tiles(self):
+        cnt = C.c_uint64(0)
+        self._check(self.L.wb_tiles(self.ctx, None, 0, C.byref(cnt)))
+        out = np.zeros(cnt.value, TILE_DTYPE)
+        self._check(self.L.wb_tiles(self.ctx, out.ctypes.data, cnt.value, C.byref(cnt)))
+        return out
+
+    def classify(self, params=None, cls=None):
+        n = self.info()["n_points"]
+        if cls is None:
+            cls = np.zeros(n, np.uint8)
+        cls = np.ascontiguousarray(cls, dtype=np.uint8)
+        p = (params or Params()).c()
+        self._check(self.L.wb_classify(self.ctx, C.byref(p), cls.ctypes.data, 0))
+        return cls
+
+    def classify_cloud(self, cloud, params=None, cls=None):
+        """Build + scan + postscan + classify in one C call (host in, host out)."""
+        xyz = np.ascontiguousarray(cloud.xyz, dtype=np.int32)
+        cs = cloud_struct(xyz, xyz.shape[0], 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+        if cls is None:
+            cls = np.zeros(xyz.shape[0], np.uint8)
+        p = (params or Params()).c()
+        self._check(self.L.wb_classify_cloud(self.ctx, C.byref(cs), C.byref(p), cls.ctypes.data))
+        return cls
+
+    # -- profiling --
+    def profile(self, enable=True):
+        self._check(self.L.wb_profile(self.ctx, 1 if enable else 0))
+
+    def launch_count(self):
+        v = C.c_uint64(0)
+        self._check(self.L.wb_launch_count(self.ctx, C.byref(v)))
+        return v.value
+
+    def stage_times(self):
+        cnt = C.c_uint32(0)
+        names = (C.c_char_p * 64)()
+        ms = (C.c_float * 64)()
+        self._check(self.L.wb_stage_times(self.ctx, names, ms, 64, C.byref(cnt)))
+        return [(names[i].decode(), ms[i]) for i in range(cnt.value)]

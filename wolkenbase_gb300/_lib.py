@@ -1,0 +1,81 @@
+"""ctypes declarations for libwolkenbase_gb300.so (include/wolkenbase_gb300.h).
+
+The library is built in-tree by wolkenbase_gb300/_build.py.  There is no CPU
+fallback: if the shared library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwolkenbase_gb300.so")
+
+WB_OK, WB_EINVAL, WB_ENOMEM, WB_ECUDA, WB_EDEPTH, WB_ESTATE, WB_ETIMEDOUT, WB_ENOTFOUND = 0, -1, -2, -3, -4, -5, -6, -7
+ERROR_NAMES = {WB_EINVAL: "WB_EINVAL", WB_ENOMEM: "WB_ENOMEM", WB_ECUDA: "WB_ECUDA", WB_EDEPTH: "WB_EDEPTH",
+               WB_ESTATE: "WB_ESTATE", WB_ETIMEDOUT: "WB_ETIMEDOUT", WB_ENOTFOUND: "WB_ENOTFOUND"}
+
+
+class wb_params(C.Structure):
+    _fields_ = [("tile_size", C.c_double), ("max_slope", C.c_double), ("thickness", C.c_double),
+                ("min_hyp_size", C.c_double)]
+
+
+class wb_cloud(C.Structure):
+    _fields_ = [("records", C.c_void_p), ("n", C.c_uint64), ("stride", C.c_uint32),
+                ("device_resident", C.c_uint32), ("scale", C.c_double * 3), ("offset", C.c_double * 3),
+                ("unit", C.c_double), ("minc", C.c_double * 3), ("maxc", C.c_double * 3)]
+
+
+class wb_octree_stats(C.Structure):
+    _fields_ = [("n_points", C.c_uint64), ("n_distinct", C.c_uint64), ("n_leaves", C.c_uint64),
+                ("max_depth", C.c_uint32), ("pad", C.c_uint32), ("root_center", C.c_double * 3),
+                ("root_side", C.c_double), ("tile_center", C.c_double * 3), ("tile_side", C.c_double),
+                ("spacing", C.c_double), ("n_tiles", C.c_uint64), ("tile_lo", C.c_int32), ("tile_hi", C.c_int32)]
+
+
+class wb_tile(C.Structure):
+    _fields_ = [("ex", C.c_int32), ("ey", C.c_int32), ("n_points", C.c_int32), ("n_ground", C.c_int32),
+                ("tree_flags", C.c_int32), ("pad", C.c_int32), ("density", C.c_double), ("h_scan", C.c_double),
+                ("hyperboloid_size", C.c_double), ("height", C.c_double)]
+
+
+# name -> (restype, argtypes); every symbol include/wolkenbase_gb300.h declares
+SIGNATURES = {
+    "wb_open": (C.c_void_p, [C.c_int, C.c_size_t]),
+    "wb_close": (None, [C.c_void_p]),
+    "wb_last_error": (C.c_char_p, [C.c_void_p]),
+    "wb_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wb_synchronize": (C.c_int, [C.c_void_p]),
+    "wb_octree_build": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud)]),
+    "wb_octree_info": (C.c_int, [C.c_void_p, C.POINTER(wb_octree_stats)]),
+    "wb_octree_leaves": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "wb_octree_point_leaf": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wb_octree_store_order": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wb_octree_find_block": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_scan_tiles": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
+    "wb_tiles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "wb_classify": (C.c_int, [C.c_void_p, C.POINTER(wb_params), C.c_void_p, C.c_int]),
+    "wb_classify_cloud": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud), C.POINTER(wb_params), C.c_void_p]),
+    "wb_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "wb_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "wb_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+}
+
+_lib = None
+
+
+def load():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run wolkenbase_gb300/_build.py (nvcc, sm_103a) first; "
+                              "there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib

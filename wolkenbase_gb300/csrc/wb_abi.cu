@@ -1,0 +1,497 @@
+/* C-ABI entry points of libwolkenbase_gb300 and the context they share.
+ * Each entry point's counterpart in the reference is named in
+ * include/wolkenbase_gb300.h. */
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+#include "wb_internal.h"
+#include "wb_device.cuh"
+
+static thread_local std::string gOpenError;
+
+int wb_fail(wb_ctx *c, int code, const std::string &msg)
+{
+  if (c)
+    c->err = msg;
+  else
+    gOpenError = msg;
+  return code;
+}
+
+int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes)
+{
+  if (bytes <= b.cap)
+    return 0;
+  size_t want = bytes + bytes / 8 + 256;
+  if (c->budget && c->used - b.cap + want > c->budget)
+    return wb_fail(c, WB_ENOMEM, "device memory budget exceeded (" + std::to_string(c->used - b.cap + want) +
+                                     " > " + std::to_string(c->budget) + " bytes)");
+  if (b.p)
+  {
+    // ordered free: earlier work on the stream may still read the old buffer
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.p);
+    c->used -= b.cap;
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess)
+  {
+    b.p = nullptr;
+    cudaGetLastError();
+    return wb_fail(c, WB_ENOMEM, std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
+  }
+  b.cap = want;
+  c->used += want;
+  return 0;
+}
+
+void wb_mark(wb_ctx *c, const char *name)
+{
+  if (!c->profile)
+    return;
+  cudaEvent_t ev;
+  if (cudaEventCreate(&ev) != cudaSuccess)
+    return;
+  cudaEventRecord(ev, c->stream);
+  c->evNames.push_back(name);
+  c->events.push_back(ev);
+}
+
+static void releaseBuffers(wb_ctx *c)
+{
+  DevBuf *all[] = {&c->rec, &c->key0, &c->key1, &c->idx0, &c->idx1, &c->tmp32, &c->tmp32b, &c->tmp8, &c->scanTmp,
+                   &c->small, &c->lev, &c->cpl, &c->pre, &c->suf, &c->leafId, &c->leafFirst, &c->leafCount,
+                   &c->leafLevel, &c->leafKey, &c->leafBox, &c->sidx, &c->sx, &c->sy, &c->sz, &c->pointLeaf,
+                   &c->storeOf, &c->survivorOf, &c->nodeChild, &c->nodeBox, &c->nodeStart, &c->nodeIdLevel,
+                   &c->tileEx, &c->tileEy, &c->tileLookup, &c->tileStart, &c->tilePts, &c->owner, &c->tileRes,
+                   &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->angleT,
+                   &c->flowCache};
+  for (DevBuf *b : all)
+    if (b->p)
+    {
+      cudaFree(b->p);
+      b->p = nullptr;
+      b->cap = 0;
+    }
+  c->used = 0;
+}
+
+static void beginRun(wb_ctx *c)
+{
+  for (cudaEvent_t e : c->events)
+    cudaEventDestroy(e);
+  c->events.clear();
+  c->evNames.clear();
+  wb_mark(c, "start");
+}
+
+static void endRun(wb_ctx *c)
+{
+  if (!c->profile || c->events.size() < 2)
+    return;
+  cudaEventSynchronize(c->events.back());
+  c->lastMs.clear();
+  c->lastNames.clear();
+  for (size_t i = 1; i < c->events.size(); i++)
+  {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->events[i - 1], c->events[i]);
+    c->lastMs.push_back(ms);
+    c->lastNames.push_back(c->evNames[i]);
+  }
+}
+
+extern "C" {
+
+wb_ctx *wb_open(int device, size_t hbm_budget)
+{
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+  {
+    cudaGetLastError();
+    wb_fail(nullptr, WB_ECUDA, "wb_open: no CUDA device");
+    return nullptr;
+  }
+  if (device < 0 || device >= count)
+  {
+    wb_fail(nullptr, WB_EINVAL, "wb_open: bad device ordinal");
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess)
+  {
+    wb_fail(nullptr, WB_ECUDA, "wb_open: cudaSetDevice failed");
+    return nullptr;
+  }
+  wb_ctx *c = new (std::nothrow) wb_ctx;
+  if (!c)
+    return nullptr;
+  c->device = device;
+  c->budget = hbm_budget;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    wb_fail(nullptr, WB_ECUDA, "wb_open: cudaStreamCreate failed");
+    delete c;
+    return nullptr;
+  }
+  c->own_stream = true;
+  c->params = wb_params{1.0, 1.0, 0.0, 0.1};
+  return c;
+}
+
+void wb_close(wb_ctx *c)
+{
+  if (!c)
+    return;
+  cudaSetDevice(c->device);
+  if (c->stream)
+    cudaStreamSynchronize(c->stream);
+  for (cudaEvent_t e : c->events)
+    cudaEventDestroy(e);
+  releaseBuffers(c);
+  if (c->own_stream && c->stream)
+    cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *wb_last_error(const wb_ctx *c)
+{
+  return c ? c->err.c_str() : gOpenError.c_str();
+}
+
+int wb_set_stream(wb_ctx *c, void *s)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (c->stream)
+    cudaStreamSynchronize(c->stream);
+  if (c->own_stream && c->stream)
+    cudaStreamDestroy(c->stream);
+  if (s)
+  {
+    c->stream = (cudaStream_t)s;
+    c->own_stream = false;
+  }
+  else
+  {
+    cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->own_stream = true;
+  }
+  return 0;
+}
+
+int wb_synchronize(wb_ctx *c)
+{
+  if (!c)
+    return WB_EINVAL;
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int wb_profile(wb_ctx *c, int enable)
+{
+  if (!c)
+    return WB_EINVAL;
+  c->profile = enable != 0;
+  return 0;
+}
+
+int wb_launch_count(wb_ctx *c, uint64_t *count)
+{
+  if (!c || !count)
+    return WB_EINVAL;
+  *count = c->launches;
+  return 0;
+}
+
+int wb_stage_times(wb_ctx *c, const char **names, float *ms, uint32_t capacity, uint32_t *count)
+{
+  if (!c)
+    return WB_EINVAL;
+  uint32_t k = (uint32_t)c->lastMs.size();
+  for (uint32_t i = 0; i < k && i < capacity; i++)
+  {
+    if (names)
+      names[i] = c->lastNames[i];
+    if (ms)
+      ms[i] = c->lastMs[i];
+  }
+  if (count)
+    *count = k;
+  return 0;
+}
+
+int wb_octree_build(wb_ctx *c, const wb_cloud *cloud)
+{
+  if (!c || !cloud)
+    return WB_EINVAL;
+  cudaSetDevice(c->device);
+  beginRun(c);
+  int rc = wb_build_impl(c, cloud);
+  endRun(c);
+  return rc;
+}
+
+int wb_octree_info(wb_ctx *c, wb_octree_stats *o)
+{
+  if (!c || !o)
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_info: no octree built");
+  memset(o, 0, sizeof *o);
+  o->n_points = c->n;
+  o->n_distinct = c->nd;
+  o->n_leaves = c->n_leaves;
+  o->max_depth = c->max_depth;
+  for (int k = 0; k < 3; k++)
+  {
+    o->root_center[k] = c->g.root_c[k];
+    o->tile_center[k] = c->g.tile_c[k];
+  }
+  o->root_side = c->g.root_side;
+  o->tile_side = c->g.tile_side;
+  wb_params p = c->params;
+  int idx, lo, hi;
+  double sp;
+  wb_snake_size(c->g.tile_side, p.tile_size > 0 ? p.tile_size : 1.0, &idx, &sp, &lo, &hi);
+  o->spacing = sp;
+  o->n_tiles = (uint64_t)((int64_t)hi - lo + 1);
+  o->tile_lo = lo;
+  o->tile_hi = hi;
+  return 0;
+}
+
+int wb_octree_leaves(wb_ctx *c, double *cs, uint32_t *first, uint32_t *count)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_leaves: no octree built");
+  uint64_t L = c->n_leaves;
+  if (L == 0)
+    return 0;
+  std::vector<uint64_t> key(L);
+  std::vector<uint8_t> lev(L);
+  WB_CUDA(c, cudaMemcpyAsync(key.data(), c->leafKey.p, L * 8, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(lev.data(), c->leafLevel.p, L, cudaMemcpyDeviceToHost, c->stream));
+  if (first)
+    WB_CUDA(c, cudaMemcpyAsync(first, c->leafFirst.p, L * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (count)
+    WB_CUDA(c, cudaMemcpyAsync(count, c->leafCount.p, L * 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (cs)
+    for (uint64_t l = 0; l < L; l++)
+    {
+      // Octree::cube: centre = parent centre +- side/4 per level, computed exactly
+      int lv = lev[l];
+      uint32_t ix = 0, iy = 0, iz = 0;
+      for (int d = 1; d <= lv; d++)
+      {
+        int oct = (int)((key[l] >> (63 - 3 * d)) & 7);
+        ix = (ix << 1) | (oct & 1);
+        iy = (iy << 1) | ((oct >> 1) & 1);
+        iz = (iz << 1) | ((oct >> 2) & 1);
+      }
+      double side = ldexp(c->g.root_side, -lv);
+      cs[4 * l + 0] = c->g.root_lo[0] + ((double)ix + 0.5) * side;
+      cs[4 * l + 1] = c->g.root_lo[1] + ((double)iy + 0.5) * side;
+      cs[4 * l + 2] = c->g.root_lo[2] + ((double)iz + 0.5) * side;
+      cs[4 * l + 3] = side;
+    }
+  return 0;
+}
+
+int wb_octree_point_leaf(wb_ctx *c, uint32_t *out)
+{
+  if (!c || (!out && c->n))
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_point_leaf: no octree built");
+  if (c->n)
+  {
+    WB_CUDA(c, cudaMemcpyAsync(out, c->pointLeaf.p, c->n * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return 0;
+}
+
+int wb_octree_store_order(wb_ctx *c, uint32_t *out)
+{
+  if (!c || (!out && c->nd))
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_store_order: no octree built");
+  if (c->nd)
+  {
+    WB_CUDA(c, cudaMemcpyAsync(out, c->sidx.p, c->nd * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return 0;
+}
+
+int wb_octree_find_block(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
+{
+  if (!c || (m && (!xyz || !leaf)))
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_find_block: no octree built");
+  return wb_find_block_impl(c, xyz, m, leaf);
+}
+
+int wb_scan_tiles(wb_ctx *c, const wb_params *p)
+{
+  if (!c || !p)
+    return WB_EINVAL;
+  cudaSetDevice(c->device);
+  beginRun(c);
+  int rc = wb_scan_impl(c, p);
+  endRun(c);
+  return rc;
+}
+
+int wb_tiles(wb_ctx *c, wb_tile *out, uint64_t capacity, uint64_t *count)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (c->stage < 2)
+    return wb_fail(c, WB_ESTATE, "wb_tiles: scan the tiles first");
+  uint64_t T = c->n_tiles;
+  if (count)
+    *count = T;
+  if (!out)
+    return 0;
+  if (capacity < T)
+    return wb_fail(c, WB_EINVAL, "wb_tiles: capacity below the tile count");
+  std::vector<TileRes> r(T);
+  WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint64_t k = 0; k < T; k++)
+  {
+    wb_tile &t = out[k];
+    t.ex = c->flowHostEx[k];
+    t.ey = c->flowHostEy[k];
+    t.n_points = r[k].nPoints;
+    t.n_ground = r[k].nGround;
+    t.tree_flags = r[k].treeFlags;
+    t.pad = 0;
+    t.density = r[k].density;
+    t.h_scan = r[k].hScan;
+    t.hyperboloid_size = r[k].h;
+    t.height = r[k].height;
+  }
+  return 0;
+}
+
+int wb_classify(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
+{
+  if (!c || !p)
+    return WB_EINVAL;
+  cudaSetDevice(c->device);
+  beginRun(c);
+  int rc = wb_classify_impl(c, p, cls, onDevice);
+  if (rc == 0 && !onDevice)
+  {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+      rc = wb_fail(c, WB_ECUDA, std::string("wb_classify: ") + cudaGetErrorString(e));
+  }
+  endRun(c);
+  return rc;
+}
+
+int wb_classify_cloud(wb_ctx *c, const wb_cloud *cloud, const wb_params *p, uint8_t *cls)
+{
+  if (!c || !cloud || !p)
+    return WB_EINVAL;
+  cudaSetDevice(c->device);
+  beginRun(c);
+  int rc = wb_build_impl(c, cloud);
+  if (rc == 0)
+    rc = wb_scan_impl(c, p);
+  if (rc == 0)
+    rc = wb_classify_impl(c, p, cls, cloud->device_resident ? 1 : 0);
+  if (rc == 0)
+  {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+      rc = wb_fail(c, WB_ECUDA, std::string("wb_classify_cloud: ") + cudaGetErrorString(e));
+  }
+  endRun(c);
+  return rc;
+}
+
+}  // extern "C"
+
+/* ---- Octree::findBlock for arbitrary positions ---- */
+namespace
+{
+__global__ void findBlockKernel(const double *__restrict__ xyz, uint64_t m, WbRoot r, const uint64_t *__restrict__ leafKey,
+                                const uint8_t *__restrict__ leafLev, uint64_t L, int64_t *__restrict__ out)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t ix = wb_cell_index(xyz[3 * i], r.lo[0], r.cell);
+    uint32_t iy = wb_cell_index(xyz[3 * i + 1], r.lo[1], r.cell);
+    uint32_t iz = wb_cell_index(xyz[3 * i + 2], r.lo[2], r.cell);
+    uint64_t key = wb_morton(ix, iy, iz);
+    // last leaf whose key prefix is <= key
+    uint64_t lo = 0, hi = L;
+    while (lo < hi)
+    {
+      uint64_t mid = (lo + hi) / 2;
+      if (leafKey[mid] <= key)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    int64_t res = -1;
+    if (lo > 0)
+    {
+      uint64_t l = lo - 1;
+      int lv = leafLev[l];
+      if ((key >> (63 - 3 * lv)) == (leafKey[l] >> (63 - 3 * lv)))
+        res = (int64_t)l;
+    }
+    out[i] = res;
+  }
+}
+}  // namespace
+
+int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
+{
+  if (m == 0)
+    return 0;
+  int rc;
+  DevBuf in, out;
+  if ((rc = wb_ensure(c, in, m * 24)) || (rc = wb_ensure(c, out, m * 8)))
+  {
+    if (in.p)
+    {
+      cudaFree(in.p);
+      c->used -= in.cap;
+    }
+    return rc;
+  }
+  WbRoot r;
+  for (int k = 0; k < 3; k++)
+    r.lo[k] = c->g.root_lo[k];
+  r.side = c->g.root_side;
+  r.cell = c->g.cell;
+  cudaMemcpyAsync(in.p, xyz, m * 24, cudaMemcpyHostToDevice, c->stream);
+  { findBlockKernel<<<(unsigned)std::min<uint64_t>((m + 255) / 256, 4096), 256, 0, c->stream>>>(
+      (const double *)in.p, m, r, (const uint64_t *)c->leafKey.p, (const uint8_t *)c->leafLevel.p, c->n_leaves,
+      (int64_t *)out.p); ++c->launches; }
+  cudaMemcpyAsync(leaf, out.p, m * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaFree(in.p);
+  cudaFree(out.p);
+  c->used -= in.cap + out.cap;
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_octree_find_block: ") + cudaGetErrorString(e));
+  return 0;
+}

@@ -1,0 +1,104 @@
+/* Internal declarations of libwolkenbase_gb300: the context, device buffers,
+ * host-side geometry set-up and the kernel launchers of each stage. */
+#ifndef WB_INTERNAL_H
+#define WB_INTERNAL_H
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/wolkenbase_gb300.h"
+
+/* Grow-only device buffer; capacity is charged against the context budget. */
+struct DevBuf
+{
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct WbGeom
+{
+  double off[3], scale[3], unit;
+  double root_c[3], root_side;
+  double root_lo[3], cell;          /* root lo corner and level-21 cell edge */
+  double tile_c[3], tile_side;      /* cube given to Flowsnake::setSize      */
+  double spacing;
+  int snake_idx, tile_lo, tile_hi;
+  bool exact_ints;                  /* decode is strictly increasing in X, Y, Z */
+};
+
+struct wb_ctx
+{
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t budget = 0, used = 0;
+  std::string err;
+  int sm_count = 0;
+  uint64_t launches = 0;            /* kernels launched by this context */
+
+  /* state */
+  int stage = 0;                    /* 0 empty, 1 built, 2 scanned, 3 classified */
+  uint64_t n = 0, nd = 0, n_leaves = 0, n_nodes = 0, n_tiles = 0, n_pairs = 0;
+  uint32_t max_depth = 0;
+  WbGeom g{};
+  wb_params params{};
+
+  /* named device buffers */
+  DevBuf rec, key0, key1, idx0, idx1, tmp32, tmp32b, tmp8, scanTmp, small;
+  DevBuf lev, cpl, pre, suf, leafId;
+  DevBuf leafFirst, leafCount, leafLevel, leafKey, leafBox;
+  DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;
+  DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
+  DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
+  DevBuf label, clsDev, ambiguous, angleT;
+  DevBuf flowCache;
+  std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
+  int flowIdxCached = -1;
+  int lookupX0 = 0, lookupY0 = 0, lookupW = 0, lookupH = 0;
+
+  /* profiling */
+  bool profile = false;
+  std::vector<const char *> evNames;
+  std::vector<cudaEvent_t> events;
+  std::vector<float> lastMs;
+  std::vector<const char *> lastNames;
+};
+
+/* Per-tile results of scan/postscan/classify (Tile, tile.h:27-35). */
+struct TileRes
+{
+  int32_t nPoints, nGround, treeFlags, pad;
+  double density, hScan, h, height;
+};
+
+/* error helpers */
+int wb_fail(wb_ctx *c, int code, const std::string &msg);
+#define WB_CUDA(c, call)                                                        \
+  do                                                                            \
+  {                                                                             \
+    cudaError_t e__ = (call);                                                   \
+    if (e__ != cudaSuccess)                                                     \
+      return wb_fail((c), WB_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+  } while (0)
+
+int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes);
+void wb_mark(wb_ctx *c, const char *name);   /* profiling event after a stage */
+
+/* host geometry (wb_geom.cpp) */
+void wb_size_fit(const double mn[3], const double mx[3], double center[3], double *side);
+void wb_tile_cube(const double mn[3], const double mx[3], double center[3], double *side);
+void wb_snake_size(const double tile_side, double desired, int *idx, double *spacing, int *lo, int *hi);
+void wb_flowsnake_order(int idx, std::vector<int32_t> &ex, std::vector<int32_t> &ey);
+
+/* primitives (wb_prims.cu) */
+int wb_exclusive_scan_u32(wb_ctx *c, const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total_dev);
+int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *keysAlt, uint32_t *valsAlt,
+                        uint64_t n, int beginBit, int endBit);
+
+/* stages */
+int wb_build_impl(wb_ctx *c, const wb_cloud *cloud);
+int wb_scan_impl(wb_ctx *c, const wb_params *p);
+int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice);
+int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf);
+
+#endif

@@ -1,0 +1,698 @@
+/* Tile stage on the GPU: cylinder gathers, scanCylinder and postscanCylinder.
+ *
+ * Tile cylinders (Flowsnake::cyl, flowsnake.cpp:263-271) are gathered by one
+ * warp per tile walking the node hierarchy depth-first in child order 0..7,
+ * which visits leaves in the order Octree::findBlocks lists blocks; inside a
+ * leaf, points are taken in store order.  That is the order
+ * OctStore::pointsIn returns (octree.cpp:1214-1242) when each block holds its
+ * points in input order, so the per-tile sums below are formed in the same
+ * sequence as the reference's and the plane fit, the untilt and the
+ * "second lowest" point come out identical.
+ *
+ * Pass 1 counts each tile's points, pass 2 writes them (a CSR: tileStart,
+ * tilePts) and records for every point the last tile in flowsnake order that
+ * contains it (owner), which is the tile whose classification survives.
+ */
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include "wb_internal.h"
+#include "wb_device.cuh"
+
+namespace
+{
+constexpr int kStack = 192;
+constexpr int kTileWarps = 4;
+
+struct TileArgs
+{
+  const int32_t *ex, *ey;
+  uint64_t T;
+  double cx, cy, spacing, rad;
+  double off[3], scale[3], unit;
+  const int32_t *child, *nodeBox, *leafBox;
+  uint64_t N, L;
+  const uint32_t *leafFirst, *leafCount;
+  const int32_t *sx, *sy, *sz;
+};
+
+__device__ __forceinline__ void tileCenter(const TileArgs &a, uint64_t k, double &x, double &y)
+{
+  int e1 = a.ex[k], e2 = a.ey[k];
+  double re = ((double)e1 - (double)e2 / 2.) * a.spacing;
+  double im = ((double)e2 * 0.86602540378443864676372317) * a.spacing;
+  x = re + a.cx;
+  y = im + a.cy;
+}
+
+__device__ __forceinline__ double dec(const TileArgs &a, int ax, int32_t q)
+{
+  return wb_decode(q, a.off[ax], a.scale[ax], a.unit);
+}
+
+/* Can a box (integer X/Y bounds) hold a point within rad of (x,y)?  Slack of
+ * 1e-9 relative keeps the pruning conservative; points are tested exactly. */
+__device__ __forceinline__ bool boxMeetsCyl(const TileArgs &a, const int32_t *box, uint64_t stride, uint64_t id,
+                                            double x, double y)
+{
+  double x0 = dec(a, 0, box[0 * stride + id]), x1 = dec(a, 0, box[3 * stride + id]);
+  double y0 = dec(a, 1, box[1 * stride + id]), y1 = dec(a, 1, box[4 * stride + id]);
+  double dx = x < x0 ? x0 - x : (x > x1 ? x - x1 : 0.0);
+  double dy = y < y0 ? y0 - y : (y > y1 ? y - y1 : 0.0);
+  double r = a.rad * (1 + 1e-9) + 1e-9;
+  return dx * dx + dy * dy <= r * r;
+}
+
+/* Walks the tile's cylinder; mode 0 counts, mode 1 writes store positions
+ * and owner.  One warp per tile. */
+template <int MODE>
+__global__ void __launch_bounds__(32 * kTileWarps) cylGather(TileArgs a, uint32_t *__restrict__ tileN,
+                                                             const uint32_t *__restrict__ tileStart,
+                                                             uint32_t *__restrict__ tilePts,
+                                                             int32_t *__restrict__ owner)
+{
+  __shared__ int32_t stack[kTileWarps][kStack];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
+  if (k >= a.T)
+    return;
+  double cx, cy;
+  tileCenter(a, k, cx, cy);
+  const unsigned lt = (1u << lane) - 1;
+  uint32_t found = 0;
+  uint32_t base = MODE ? tileStart[k] : 0;
+  int sp = 0;
+  if (lane == 0)
+    stack[w][0] = 0;
+  sp = 1;
+  __syncwarp();
+  if (a.N == 0)
+    sp = 0;
+  while (sp > 0)
+  {
+    int32_t code = stack[w][sp - 1];
+    sp--;
+    __syncwarp();
+    if (code >= 0)
+    {
+      // internal node: test its 8 children, push the ones that meet (reverse order)
+      int32_t ch = -1;
+      bool meet = false;
+      if (lane < 8)
+      {
+        ch = a.child[(uint64_t)code * 8 + lane];
+        if (ch >= 0)
+          meet = boxMeetsCyl(a, a.nodeBox, a.N, (uint64_t)ch, cx, cy);
+        else if (ch <= -2)
+          meet = boxMeetsCyl(a, a.leafBox, a.L, (uint64_t)(-2 - ch), cx, cy);
+      }
+      unsigned m = __ballot_sync(0xffffffffu, meet);
+      int cnt = __popc(m);
+      if (meet)
+      {
+        int above = __popc(m >> (lane + 1));   // children after me go deeper in the stack
+        stack[w][sp + above] = ch;
+      }
+      sp += cnt;
+      __syncwarp();
+    }
+    else
+    {
+      uint64_t l = (uint64_t)(-2 - code);
+      uint32_t f = a.leafFirst[l], cntL = a.leafCount[l];
+      for (uint32_t t0 = 0; t0 < cntL; t0 += 32)
+      {
+        uint32_t t = t0 + lane;
+        bool in = false;
+        if (t < cntL)
+        {
+          uint32_t j = f + t;
+          double px = dec(a, 0, a.sx[j]), py = dec(a, 1, a.sy[j]);
+          in = wb_hypot(cx - px, cy - py) <= a.rad;
+        }
+        unsigned m = __ballot_sync(0xffffffffu, in);
+        if (MODE && in)
+        {
+          uint32_t j = f + t;
+          tilePts[base + found + __popc(m & lt)] = j;
+          atomicMax(&owner[j], (int32_t)k);
+        }
+        found += __popc(m);
+      }
+    }
+  }
+  if (!MODE && lane == 0)
+    tileN[k] = found;
+}
+
+/* ---- scanCylinder ---- */
+struct ScanArgs
+{
+  TileArgs t;
+  const uint32_t *tileStart, *tilePts;
+  double minH;
+};
+
+constexpr int kQ = 8;   // summed quantities: xx, yx, yy, x, y, xz, yz, z
+
+__device__ __forceinline__ void counterMergeGroup(double *part, uint64_t i, double g)
+{
+  uint64_t carry = i ^ (i + 8);
+  if (carry == 8)
+    part[3] = g;
+  else
+  {
+    part[3] += g;
+    int lvl = 4;
+    for (; carry >> (lvl + 1); lvl++)
+      part[lvl] += part[lvl - 1];
+    part[lvl] = part[lvl - 1];
+  }
+}
+
+__device__ __forceinline__ void counterMergeOne(double *part, uint64_t i, double v)
+{
+  uint64_t carry = i ^ (i + 1);
+  if (carry == 1)
+    part[0] = v;
+  else
+  {
+    part[0] += v;
+    int lvl = 1;
+    for (; carry >> (lvl + 1); lvl++)
+      part[lvl] += part[lvl - 1];
+    part[lvl] = part[lvl - 1];
+  }
+}
+
+__device__ double pairwiseFinish(const double *part, uint64_t n)
+{
+  double s = 0;
+  for (int i = 0; i < 32; i++)
+    if ((n >> i) & 1)
+      s += part[i];
+  return s;
+}
+
+/* 3x3 Gauss-Jordan with the reference's ratio pivoting (matrix.cpp:262-422). */
+__device__ double pw3(double a, double b, double c)
+{
+  // pairwisesum of three values: ((a+b) + c) by the counter rule
+  double part[4];
+  part[0] = a;
+  part[0] += b;
+  part[1] = part[0];
+  part[0] = c;
+  double s = 0;
+  s += part[0];
+  s += part[1];
+  return s;
+}
+
+__device__ double pwN(const double *v, int n)
+{
+  if (n == 1)
+    return v[0];
+  if (n == 2)
+    return v[0] + v[1];
+  return pw3(v[0], v[1], v[2]);
+}
+
+__device__ void swapRow(double m[3][3], double b[3], int r0, int r1)
+{
+  for (int k = 0; k < 3; k++)
+  {
+    double t = m[r0][k];
+    m[r0][k] = m[r1][k];
+    m[r1][k] = t;
+  }
+  double t = b[r0];
+  b[r0] = b[r1];
+  b[r1] = t;
+}
+
+__device__ void findPivot3(double m[3][3], double b[3], int row, int column)
+{
+  int pivotrow = -1;
+  double maxratio = 0;
+  for (; pivotrow < row && column < 3; column++)
+    for (int i = row; i < 3; i++)
+    {
+      double sq[3] = {0, 0, 0};
+      for (int j = column + 1; j < 3; j++)
+        sq[j - column - 1] = m[i][j] * m[i][j];
+      double ratio = (m[i][column] * m[i][column]) / pwN(sq, 3 - column);
+      if (ratio > maxratio)
+      {
+        pivotrow = i;
+        maxratio = ratio;
+      }
+    }
+  if (pivotrow > row)
+    swapRow(m, b, pivotrow, row);
+}
+
+__device__ void rowOp3(double m[3][3], double b[3], int row0, int row1, int piv)
+{
+  double slope = 0, minslope = INFINITY, det;
+  int flags = 0, pivot;
+  if (piv >= 0 && m[row0][piv] == 0 && m[row1][piv] == 0)
+    piv = -1;
+  pivot = piv;
+  if (piv >= 0 && m[row0][piv] == 0)
+    flags = 9;
+  for (int i = 0; piv < 0 && i < 3; i++)
+    if (m[row0][i] != 0 || m[row1][i] != 0)
+    {
+      if (fabs(m[row0][i]) > fabs(m[row1][i]) || row0 >= row1)
+      {
+        slope = fabs(m[row1][i] / m[row0][i]);
+        flags &= ~8;
+      }
+      else
+      {
+        slope = fabs(m[row0][i] / m[row1][i]);
+        flags |= 8;
+      }
+      if (slope < minslope)
+      {
+        minslope = slope;
+        flags = (flags >> 3) * 9;
+        pivot = i;
+      }
+    }
+  flags &= 1;
+  if (flags)
+    swapRow(m, b, row0, row1);
+  det = pivot < 0 ? 0 : m[row0][pivot];
+  if (det != 0 && det != 1)
+  {
+    for (int i = 0; i < 3; i++)
+      m[row0][i] /= det;
+    b[row0] /= det;
+  }
+  if (pivot >= 0)
+    slope = m[row1][pivot];
+  if (slope != 0 && row0 != row1)
+  {
+    for (int i = 0; i < 3; i++)
+      m[row1][i] -= m[row0][i] * slope;
+    b[row1] -= b[row0] * slope;
+  }
+}
+
+__global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRes *__restrict__ res)
+{
+  __shared__ double part[kTileWarps][kQ][32];
+  __shared__ double tail[kTileWarps][kQ][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const TileArgs &a = s.t;
+  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
+  if (k >= a.T)
+    return;
+  uint32_t b0 = s.tileStart[k], M = s.tileStart[k + 1] - b0;
+  TileRes r{};
+  if (M == 0)
+  {
+    if (lane == 0)
+      res[k] = r;
+    return;
+  }
+  double cx, cy;
+  tileCenter(a, k, cx, cy);
+  uint64_t G = M / 8;   // complete groups of eight
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    double q[kQ];
+    if (i < M)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      q[0] = x * x;
+      q[1] = y * x;
+      q[2] = y * y;
+      q[3] = 1.0 * x;
+      q[4] = 1.0 * y;
+      q[5] = x * z;
+      q[6] = y * z;
+      q[7] = 1.0 * z;
+    }
+    else
+      for (int u = 0; u < kQ; u++)
+        q[u] = 0;
+    uint64_t grp = i / 8;
+    // fixed tree inside each group of eight: ((a0+a1)+(a2+a3))+((a4+a5)+(a6+a7))
+    double gs[kQ];
+    for (int u = 0; u < kQ; u++)
+    {
+      double v = q[u];
+      v = v + __shfl_xor_sync(0xffffffffu, v, 1);
+      v = v + __shfl_xor_sync(0xffffffffu, v, 2);
+      v = v + __shfl_xor_sync(0xffffffffu, v, 4);
+      gs[u] = v;
+    }
+    // lane u (< kQ) merges quantity u for the up-to-4 complete groups of the chunk
+    for (int gq = 0; gq < 4; gq++)
+    {
+      uint64_t gi = (uint64_t)c0 / 8 + gq;
+      double gv[kQ];
+      for (int u = 0; u < kQ; u++)
+        gv[u] = __shfl_sync(0xffffffffu, gs[u], gq * 8);
+      if (gi < G && lane < kQ)
+      {
+        double g = gv[0];
+        for (int u = 1; u < kQ; u++)
+          if (lane == u)
+            g = gv[u];
+        counterMergeGroup(part[w][lane], gi * 8, g);
+      }
+    }
+    // stash the trailing incomplete group's values
+    if (i < M && grp == G)
+      for (int u = 0; u < kQ; u++)
+        tail[w][u][i - G * 8] = q[u];
+    __syncwarp();
+  }
+  if (lane < kQ)
+  {
+    for (uint64_t i = G * 8; i < M; i++)
+      counterMergeOne(part[w][lane], i, tail[w][lane][i - G * 8]);
+  }
+  __syncwarp();
+  double sx = 0, sy = 0;
+  if (lane == 0)
+  {
+    double tot[kQ];
+    for (int u = 0; u < kQ; u++)
+      tot[u] = pairwiseFinish(part[w][u], M);
+    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)M}};
+    double bv[3] = {tot[5], tot[6], tot[7]};
+    for (int i = 0; i < 3; i++)
+    {
+      findPivot3(m, bv, i, i);
+      for (int j = 0; j < 3; j++)
+        rowOp3(m, bv, i, j, i);
+    }
+    for (int i = 2; i >= 0; i--)
+      for (int j = 0; j < i; j++)
+        rowOp3(m, bv, i, j, i);
+    double v0 = bv[0], v1 = bv[1];
+    if (m[0][0] == 0)
+      v0 = NAN;
+    if (m[1][1] == 0)
+      v1 = NAN;
+    sx = v0;
+    sy = v1;
+    double len = wb_hypot(sx, sy);
+    if (len > 1)
+    {
+      sx /= len;
+      sy /= len;
+    }
+    if (isnan(sx) || isnan(sy))
+      sx = sy = 0;
+  }
+  sx = __shfl_sync(0xffffffffu, sx, 0);
+  sy = __shfl_sync(0xffffffffu, sy, 0);
+  // untilt: bottom (first minimum), bottom2 (running minimum before it), top
+  double bottom = INFINITY, top = -INFINITY;
+  uint32_t argmin = 0xffffffffu;
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    double uz = INFINITY, ut = -INFINITY;
+    if (i < M)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double zz = sy * y + sx * x;
+      uz = z - zz;
+      ut = uz;
+    }
+    // chunk minimum with first index
+    double mv = uz;
+    uint32_t mi = (i < M && uz < INFINITY) ? i : 0xffffffffu;
+    for (int o = 16; o; o >>= 1)
+    {
+      double ov = __shfl_xor_sync(0xffffffffu, mv, o);
+      uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
+      if (ov < mv || (ov == mv && oi < mi))
+      {
+        mv = ov;
+        mi = oi;
+      }
+    }
+    if (mv < bottom)
+    {
+      bottom = mv;
+      argmin = mi;
+    }
+    double tv = ut;
+    for (int o = 16; o; o >>= 1)
+      tv = fmax(tv, __shfl_xor_sync(0xffffffffu, tv, o));
+    top = fmax(top, tv);
+  }
+  double bottom2 = INFINITY;
+  uint32_t nBottom = 0;
+  int histo[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    double v = INFINITY;
+    if (i < M && i < argmin)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      v = z - (sy * y + sx * x);
+    }
+    for (int o = 16; o; o >>= 1)
+      v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    bottom2 = fmin(bottom2, v);
+  }
+  if (isinf(bottom2))
+    bottom2 = bottom;
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    int sector = -1;
+    if (i < M)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double uz = z - (sy * y + sx * x);
+      if (uz < bottom2 + 2 * a.rad)
+      {
+        sector = (int)rint(atan2(y, x) * 3 / M_PI);
+        if (sector < 0)
+          sector += 6;
+        sector = (sector % 6) + 1;
+        if (wb_hypot(x, y) < a.rad / 2.6457513110645905905016)
+          sector = 0;
+      }
+    }
+    for (int sct = 0; sct < 7; sct++)
+      histo[sct] += __popc(__ballot_sync(0xffffffffu, sector == sct));
+    nBottom += __popc(__ballot_sync(0xffffffffu, sector >= 0));
+  }
+  if (lane == 0)
+  {
+    double density = 0;
+    int treeFlags = 0;
+    for (int i = 0; i < 7; i++)
+      density += (double)histo[i] * (double)histo[i];
+    if (M > nBottom && density < 7)
+      treeFlags = 1;
+    density = sqrt(density) * 2.6457513110645905905016 / (a.rad * a.rad) / M_PI;
+    if (M > nBottom && density < 0.5)
+      treeFlags = 1;
+    if (top - bottom > 1.5)
+      treeFlags = 1;
+    r.nPoints = (int32_t)M;
+    r.nGround = 0;
+    r.treeFlags = treeFlags;
+    r.density = density;
+    r.hScan = r.h = sqrt(1 / density + s.minH * s.minH);
+    r.height = top - bottom;
+    res[k] = r;
+  }
+}
+
+/* postscanCylinder (scan.cpp:142-179): tree tiles grow their hyperboloid by
+ * the number of tree tiles met walking the six lattice rays. */
+__global__ void postscanKernel(uint64_t T, const int32_t *__restrict__ ex, const int32_t *__restrict__ ey,
+                               const int32_t *__restrict__ lookup, int x0, int y0, int W, int H, double spacing,
+                               TileRes *__restrict__ res, double *__restrict__ hOut)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    TileRes me = res[k];
+    double h = me.h;
+    if (me.nPoints)
+    {
+      const int rx[6] = {1, 1, 0, -1, -1, 0}, ry[6] = {0, 1, 1, 0, -1, -1};
+      int i = 1, count = 0, nontree, ringcount;
+      do
+      {
+        nontree = ringcount = 0;
+        for (int j = 0; j < 6 && (me.treeFlags & 1); j++)
+        {
+          int ax = ex[k] + rx[j] * i - x0, ay = ey[k] + ry[j] * i - y0;
+          if (ax < 0 || ay < 0 || ax >= W || ay >= H)
+            continue;
+          int32_t kk = lookup[(uint64_t)ay * W + ax];
+          if (kk < 0)
+            continue;
+          TileRes o = res[kk];
+          if (o.nPoints)
+          {
+            ringcount++;
+            if (o.treeFlags & 1)
+              count++;
+            else
+              nontree++;
+          }
+        }
+        ++i;
+      } while (ringcount && !nontree);
+      double e = count * spacing / 6;
+      h = sqrt(h * h + e * e);
+    }
+    hOut[k] = h;
+  }
+}
+
+__global__ void applyH(uint64_t T, const double *__restrict__ hIn, TileRes *__restrict__ res)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
+    res[k].h = hIn[k];
+}
+
+__global__ void fillOwner(int32_t *p, uint64_t n)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = -1;
+}
+}  // namespace
+
+static int uploadTiles(wb_ctx *c)
+{
+  WbGeom &g = c->g;
+  if (c->flowIdxCached != g.snake_idx)
+  {
+    wb_flowsnake_order(g.snake_idx, c->flowHostEx, c->flowHostEy);
+    uint64_t T = c->flowHostEx.size();
+    int x0 = INT32_MAX, y0 = INT32_MAX, x1 = INT32_MIN, y1 = INT32_MIN;
+    for (uint64_t k = 0; k < T; k++)
+    {
+      x0 = std::min(x0, c->flowHostEx[k]);
+      x1 = std::max(x1, c->flowHostEx[k]);
+      y0 = std::min(y0, c->flowHostEy[k]);
+      y1 = std::max(y1, c->flowHostEy[k]);
+    }
+    c->lookupX0 = x0;
+    c->lookupY0 = y0;
+    c->lookupW = x1 - x0 + 1;
+    c->lookupH = y1 - y0 + 1;
+    std::vector<int32_t> look((uint64_t)c->lookupW * c->lookupH, -1);
+    for (uint64_t k = 0; k < T; k++)
+      look[(uint64_t)(c->flowHostEy[k] - y0) * c->lookupW + (c->flowHostEx[k] - x0)] = (int32_t)k;
+    int rc;
+    if ((rc = wb_ensure(c, c->tileEx, T * 4 + 64)) || (rc = wb_ensure(c, c->tileEy, T * 4 + 64)) ||
+        (rc = wb_ensure(c, c->tileLookup, look.size() * 4 + 64)))
+      return rc;
+    WB_CUDA(c, cudaMemcpyAsync(c->tileEx.p, c->flowHostEx.data(), T * 4, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->tileEy.p, c->flowHostEy.data(), T * 4, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->tileLookup.p, look.data(), look.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->flowIdxCached = g.snake_idx;
+  }
+  c->n_tiles = c->flowHostEx.size();
+  return 0;
+}
+
+static TileArgs tileArgs(wb_ctx *c)
+{
+  TileArgs a;
+  WbGeom &g = c->g;
+  a.ex = (const int32_t *)c->tileEx.p;
+  a.ey = (const int32_t *)c->tileEy.p;
+  a.T = c->n_tiles;
+  a.cx = g.tile_c[0];
+  a.cy = g.tile_c[1];
+  a.spacing = g.spacing;
+  a.rad = g.spacing * 41 / 71;
+  for (int k = 0; k < 3; k++)
+  {
+    a.off[k] = g.off[k];
+    a.scale[k] = g.scale[k];
+  }
+  a.unit = g.unit;
+  a.child = (const int32_t *)c->nodeChild.p;
+  a.nodeBox = (const int32_t *)c->nodeBox.p;
+  a.leafBox = (const int32_t *)c->leafBox.p;
+  a.N = c->n_nodes;
+  a.L = c->n_leaves;
+  a.leafFirst = (const uint32_t *)c->leafFirst.p;
+  a.leafCount = (const uint32_t *)c->leafCount.p;
+  a.sx = (const int32_t *)c->sx.p;
+  a.sy = (const int32_t *)c->sy.p;
+  a.sz = (const int32_t *)c->sz.p;
+  return a;
+}
+
+int wb_scan_impl(wb_ctx *c, const wb_params *p)
+{
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_scan_tiles: build the octree first");
+  if (!(p->tile_size > 0))
+    return wb_fail(c, WB_EINVAL, "wb_scan_tiles: tile_size must be > 0");
+  c->params = *p;
+  WbGeom &g = c->g;
+  wb_snake_size(g.tile_side, p->tile_size, &g.snake_idx, &g.spacing, &g.tile_lo, &g.tile_hi);
+  int rc = uploadTiles(c);
+  if (rc)
+    return rc;
+  uint64_t T = c->n_tiles, nd = c->nd;
+  if ((rc = wb_ensure(c, c->tileN, T * 4 + 64)) || (rc = wb_ensure(c, c->tileStart, (T + 1) * 4 + 64)) ||
+      (rc = wb_ensure(c, c->owner, nd * 4 + 64)) || (rc = wb_ensure(c, c->tileRes, T * sizeof(TileRes) + 64)) ||
+      (rc = wb_ensure(c, c->tileH, T * 8 + 64)) || (rc = wb_ensure(c, c->small, 4096)))
+    return rc;
+  TileArgs a = tileArgs(c);
+  uint32_t *tileN = (uint32_t *)c->tileN.p, *tileStart = (uint32_t *)c->tileStart.p;
+  int32_t *owner = (int32_t *)c->owner.p;
+  unsigned blocks = (unsigned)((T + kTileWarps - 1) / kTileWarps);
+  { cylGather<0><<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, tileN, nullptr, nullptr, nullptr); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
+  if ((rc = wb_exclusive_scan_u32(c, tileN, tileStart, T, dTot)))
+    return rc;
+  WB_CUDA(c, cudaMemcpyAsync(tileStart + T, dTot, 4, cudaMemcpyDeviceToDevice, c->stream));
+  uint32_t M = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&M, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->n_pairs = M;
+  if ((rc = wb_ensure(c, c->tilePts, (uint64_t)M * 4 + 64)))
+    return rc;
+  { fillOwner<<<(unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(owner, nd); ++c->launches; }
+  { cylGather<1><<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, nullptr, tileStart, (uint32_t *)c->tilePts.p, owner); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  wb_mark(c, "tile_gather");
+  ScanArgs s;
+  s.t = a;
+  s.tileStart = tileStart;
+  s.tilePts = (const uint32_t *)c->tilePts.p;
+  s.minH = p->min_hyp_size;
+  TileRes *res = (TileRes *)c->tileRes.p;
+  { scanKernel<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  wb_mark(c, "scan");
+  unsigned pb = (unsigned)std::min<uint64_t>((T + 255) / 256, (uint64_t)c->sm_count * 16);
+  { postscanKernel<<<pb, 256, 0, c->stream>>>(T, a.ex, a.ey, (const int32_t *)c->tileLookup.p, c->lookupX0, c->lookupY0,
+                                            c->lookupW, c->lookupH, g.spacing, res, (double *)c->tileH.p); ++c->launches; }
+  { applyH<<<pb, 256, 0, c->stream>>>(T, (const double *)c->tileH.p, res); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  wb_mark(c, "postscan");
+  c->stage = 2;
+  return 0;
+}
