@@ -148,6 +148,15 @@ int wb_profile(wb_ctx *ctx, int enable);
  * accounting for timed regions). */
 int wb_launch_count(wb_ctx *ctx, uint64_t *count);
 
+/* Self-checks of the device arithmetic (no reference counterpart: they let a
+ * caller verify the GPU's integer directions and distances against its own
+ * host): atan2i (angle.cpp:117-155) of m (y,x) pairs; hypot as the
+ * reference's libm computes it; Hyperboloid::in (shape.cpp:127-135) of m
+ * points for vertex v, curvature radius r and slope s.  Synchronous. */
+int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out);
+int wb_check_hypot(const double *ab, uint64_t m, double *out);
+int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz, uint64_t m, uint8_t *out);
+
 #ifdef __cplusplus
 }
 #endif

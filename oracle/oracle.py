@@ -66,6 +66,7 @@ def lib():
         L.wbo_quadrant_trig.argtypes = [C.c_void_p]
         L.wbo_pairwisesum.argtypes = [C.c_void_p, C.c_uint]
         L.wbo_pairwisesum.restype = C.c_double
+        L.wbo_hypot_many.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
         L.wbo_lsq_plane.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
         L.wbo_hyperboloid_in.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p]
         L.wbo_cylinder_in.argtypes = [C.c_void_p, C.c_double, C.c_void_p]
@@ -73,6 +74,13 @@ def lib():
         L.wbo_flowsnake.argtypes = [C.c_int, C.c_void_p]
         L.wbo_flowsnake_limits.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
         _lib = L
+        # The reference's atan2i tables come from x86-64 80-bit long double;
+        # hosts with another long double (aarch64: 128-bit) would round a few
+        # entries differently, so the oracle uses the pinned values.
+        golden = os.path.join(os.path.dirname(HERE), "tests", "golden", "primitives.npz")
+        if os.path.exists(golden):
+            g = np.load(golden)
+            set_tables(g["tan"], g["sin"], g["cos"])
     return _lib
 
 
@@ -131,6 +139,13 @@ def atan2i(y, x):
     yx = np.ascontiguousarray(np.stack([np.asarray(y, np.float64), np.asarray(x, np.float64)], axis=1))
     out = np.zeros(yx.shape[0], np.int32)
     L.wbo_atan2i_many(yx.ctypes.data, yx.shape[0], out.ctypes.data)
+    return out
+
+
+def hypot(a, b):
+    ab = np.ascontiguousarray(np.stack([np.asarray(a, np.float64), np.asarray(b, np.float64)], axis=1))
+    out = np.zeros(ab.shape[0])
+    lib().wbo_hypot_many(ab.ctypes.data, ab.shape[0], out.ctypes.data)
     return out
 
 

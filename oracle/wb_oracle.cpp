@@ -1177,6 +1177,12 @@ void wbo_quadrant_trig(double *cs)
 
 double wbo_pairwisesum(const double *a, unsigned n) { return pairwise(a, n); }
 
+void wbo_hypot_many(const double *ab, uint64_t n, double *out)
+{
+  for (uint64_t i = 0; i < n; i++)
+    out[i] = hypotR(ab[2 * i], ab[2 * i + 1]);
+}
+
 void wbo_lsq_plane(const double *xyz, uint64_t rows, double *out3)
 {
   std::vector<double> x(rows), y(rows), z(rows);

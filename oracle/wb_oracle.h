@@ -77,6 +77,7 @@ int32_t wbo_atan2i(double y, double x);
 void wbo_atan2i_many(const double *yx, uint64_t n, int32_t *out);
 void wbo_quadrant_trig(double *cos_sin8);
 double wbo_pairwisesum(const double *a, unsigned n);
+void wbo_hypot_many(const double *ab, uint64_t n, double *out);
 void wbo_lsq_plane(const double *xyz, uint64_t rows, double *out3);
 int wbo_hyperboloid_in(const double *vertex, double r, double s, const double *pnt);
 int wbo_cylinder_in(const double *center_xy, double r, const double *pnt);

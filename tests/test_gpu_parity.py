@@ -69,9 +69,25 @@ def test_scan_and_classify_match(classifier, oracle_mod, case):
         assert np.array_equal(t[f], ot[of]), f
     # n_points does not depend on point order: equal to the reference's too
     assert np.array_equal(t["n_points"], g["tiles"]["n_points"])
-    assert np.array_equal(r["cls"], o["cls"])
-    diff = int(np.sum(r["cls"] != g["cls"]))
+    # A record overwritten by a later duplicate (OctBuffer::put) has no class of
+    # its own in the reference; the GPU reports its survivor's class for it.
+    stored = g["block"] >= 0
+    bad = np.nonzero((r["cls"] != o["cls"]) & stored)[0]
+    assert bad.size == 0, f"{bad.size} labels differ from the oracle, e.g. {bad[:10].tolist()}"
+    diff = int(np.sum((r["cls"] != g["cls"]) & stored))
     assert diff <= LABEL_TOL * cloud.n, f"{diff} labels differ from the reference's serial run"
+    _check_duplicates_share_class(cloud, r["cls"])
+
+
+def _check_duplicates_share_class(cloud, cls):
+    d = np.ascontiguousarray(cloud.xyz).view(np.dtype((np.void, 12))).ravel()
+    _, inv = np.unique(d, return_inverse=True)
+    first = np.full(inv.max() + 1, -1, np.int64)
+    for i, k in enumerate(inv):
+        if first[k] < 0:
+            first[k] = i
+        else:
+            assert cls[i] == cls[first[k]]
 
 
 @pytest.mark.parametrize("seed,n", [(101, 60000), (202, 30000)])
@@ -82,7 +98,8 @@ def test_random_tiles_match_oracle(classifier, oracle_mod, seed, n):
     r = _gpu_run(classifier, cloud, wb.Params())
     o = oracle_mod.run(cloud, canonical_order=True, threads=16)
     assert np.array_equal(r["tiles"]["hyperboloid_size"], o["tiles"]["h_final"])
-    assert np.array_equal(r["cls"], o["cls"])
+    bad = np.nonzero(r["cls"] != o["cls"])[0]
+    assert bad.size == 0, f"{bad.size} labels differ from the oracle, e.g. {bad[:10].tolist()}"
     assert np.array_equal(r["cs"][r["pleaf"]], o["leaves"][o["leaf"]])
 
 

@@ -60,6 +60,9 @@ SIGNATURES = {
     "wb_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]),
     "wb_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "wb_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "wb_check_atan2i": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_check_hypot": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_check_hyperboloid": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p]),
 }
 
 _lib = None

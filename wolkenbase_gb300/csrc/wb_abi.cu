@@ -495,3 +495,97 @@ int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
     return wb_fail(c, WB_ECUDA, std::string("wb_octree_find_block: ") + cudaGetErrorString(e));
   return 0;
 }
+
+/* ---- device arithmetic self-checks ---- */
+#include "angle_tables.h"
+namespace
+{
+__global__ void atanCheckKernel(const double *yx, uint64_t m, const double *tab, int32_t *out)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = wb_atan2i(yx[2 * i], yx[2 * i + 1], tab, tab + 511, tab + 1023, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
+}
+__global__ void hypotCheckKernel(const double *ab, uint64_t m, double *out)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = wb_hypot(ab[2 * i], ab[2 * i + 1]);
+}
+__global__ void hypCheckKernel(double vx, double vy, double vz, double r, double s, const double *xyz, uint64_t m,
+                               uint8_t *out)
+{
+  double por = r * (s * s);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = wb_hyp_in(vx + 0, vy + 0, vz + por, por * por, s, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+}
+
+template <class F>
+int withDevice(size_t inBytes, const void *in, size_t outBytes, void *out, F launch)
+{
+  void *din = nullptr, *dout = nullptr;
+  if (cudaMalloc(&din, inBytes + 16) != cudaSuccess)
+    return WB_ENOMEM;
+  if (cudaMalloc(&dout, outBytes + 16) != cudaSuccess)
+  {
+    cudaFree(din);
+    return WB_ENOMEM;
+  }
+  int rc = 0;
+  if (cudaMemcpy(din, in, inBytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = WB_ECUDA;
+  if (!rc)
+  {
+    launch(din, dout);
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, outBytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = WB_ECUDA;
+  }
+  cudaFree(din);
+  cudaFree(dout);
+  return rc;
+}
+}  // namespace
+
+extern "C" {
+int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out)
+{
+  if (!m)
+    return 0;
+  if (!yx || !out)
+    return WB_EINVAL;
+  double *tab = nullptr;
+  if (cudaMalloc(&tab, 1535 * 8) != cudaSuccess)
+    return WB_ENOMEM;
+  cudaMemcpy(tab, kWbTan, 511 * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(tab + 511, kWbSin, 512 * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(tab + 1023, kWbCos, 512 * 8, cudaMemcpyHostToDevice);
+  int rc = withDevice(m * 16, yx, m * 4, out, [&](void *din, void *dout) {
+    atanCheckKernel<<<(unsigned)((m + 255) / 256 < 4096 ? (m + 255) / 256 : 4096), 256>>>((const double *)din, m, tab,
+                                                                                         (int32_t *)dout);
+  });
+  cudaFree(tab);
+  return rc;
+}
+
+int wb_check_hypot(const double *ab, uint64_t m, double *out)
+{
+  if (!m)
+    return 0;
+  if (!ab || !out)
+    return WB_EINVAL;
+  return withDevice(m * 16, ab, m * 8, out, [&](void *din, void *dout) {
+    hypotCheckKernel<<<(unsigned)((m + 255) / 256 < 4096 ? (m + 255) / 256 : 4096), 256>>>((const double *)din, m,
+                                                                                          (double *)dout);
+  });
+}
+
+int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz, uint64_t m, uint8_t *out)
+{
+  if (!m)
+    return 0;
+  if (!v || !xyz || !out)
+    return WB_EINVAL;
+  return withDevice(m * 24, xyz, m, out, [&](void *din, void *dout) {
+    hypCheckKernel<<<(unsigned)((m + 255) / 256 < 4096 ? (m + 255) / 256 : 4096), 256>>>(
+        v[0], v[1], v[2], r, s, (const double *)din, m, (uint8_t *)dout);
+  });
+}
+}  // extern "C"

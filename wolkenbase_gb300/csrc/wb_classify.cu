@@ -40,6 +40,9 @@ struct ClsArgs
   const int32_t *child, *nodeBox, *leafBox;
   uint64_t N, L;
   const uint32_t *leafFirst, *leafCount;
+  const uint64_t *leafKey;
+  const uint8_t *leafLev;
+  double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
   const int32_t *owner;
   const TileRes *tiles;
@@ -130,6 +133,29 @@ __global__ void __launch_bounds__(32 * kWarps) classifyKernel(ClsArgs a)
     }
     uint64_t l = (uint64_t)(-2 - code);
     uint32_t f = a.leafFirst[l], cnt = a.leafCount[l];
+    // OctStore::pointsIn (octree.cpp:1214-1242): a block counts only if its
+    // cube meets the shape (Octree::findBlocks); if all eight corners are
+    // inside, all its points are taken without testing them one by one.
+    // The two differ from testing every point only for points outside the
+    // root cube (Octree::sizeFit can leave a sliver of the cloud below it).
+    bool cubeTest = false;
+    {
+      double lx, ly, lz, ls;
+      wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
+      if (lane == 0)
+        cubeTest = wb_hyp_in(cx, cy, cz, por2, a.slope, wb_clamp_toward(cx, lx, ls), wb_clamp_toward(cy, ly, ls),
+                             lz - ls / 2);
+      else if (lane <= 8)
+      {
+        int n = lane - 1;
+        cubeTest = wb_hyp_in(cx, cy, cz, por2, a.slope, (n & 1) ? lx + ls / 2 : lx - ls / 2,
+                             (n & 2) ? ly + ls / 2 : ly - ls / 2, (n & 4) ? lz + ls / 2 : lz - ls / 2);
+      }
+    }
+    unsigned cb = __ballot_sync(0xffffffffu, cubeTest);
+    if (!(cb & 1))
+      continue;
+    const bool allIn = (cb & 0x1feu) == 0x1feu;
     for (uint32_t t0 = 0; t0 < cnt; t0 += 32)
     {
       uint32_t t = t0 + lane;
@@ -137,7 +163,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyKernel(ClsArgs a)
       {
         uint32_t q = f + t;
         double qx = decA(a, 0, a.sx[q]), qy = decA(a, 1, a.sy[q]), qz = decA(a, 2, a.sz[q]);
-        if (wb_hyp_in(cx, cy, cz, por2, a.slope, qx, qy, qz))
+        if (allIn || wb_hyp_in(cx, cy, cz, por2, a.slope, qx, qy, qz))
         {
           double dx = qx - px, dy = qy - py;
           if (wb_hypot(px - qx, py - qy) != 0)
@@ -252,6 +278,11 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   a.L = c->n_leaves;
   a.leafFirst = (const uint32_t *)c->leafFirst.p;
   a.leafCount = (const uint32_t *)c->leafCount.p;
+  a.leafKey = (const uint64_t *)c->leafKey.p;
+  a.leafLev = (const uint8_t *)c->leafLevel.p;
+  for (int k = 0; k < 3; k++)
+    a.rootLo[k] = c->g.root_lo[k];
+  a.rootSide = c->g.root_side;
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;

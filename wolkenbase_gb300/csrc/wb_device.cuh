@@ -203,6 +203,35 @@ __device__ __forceinline__ int wb_atan2i(double y, double x, const double *__res
   return ret + (int)nr;
 }
 
+/* Cube of a leaf from its key and level, as Octree::cube builds it by
+ * halving (octree.cpp:349-358); every value is an exact dyadic double. */
+__device__ __forceinline__ void wb_leaf_cube(uint64_t key, int lev, const double *lo, double rootSide, double &cx,
+                                             double &cy, double &cz, double &side)
+{
+  uint32_t ix = 0, iy = 0, iz = 0;
+  for (int d = 1; d <= lev; d++)
+  {
+    int oct = (int)((key >> (63 - 3 * d)) & 7);
+    ix = (ix << 1) | (oct & 1);
+    iy = (iy << 1) | ((oct >> 1) & 1);
+    iz = (iz << 1) | ((oct >> 2) & 1);
+  }
+  side = ldexp(rootSide, -lev);
+  cx = lo[0] + ((double)ix + 0.5) * side;
+  cy = lo[1] + ((double)iy + 0.5) * side;
+  cz = lo[2] + ((double)iz + 0.5) * side;
+}
+
+/* Shape::closestPoint of a cube for a shape whose axis passes through
+ * (ax, ay): the coordinate of the nearest face, or ax itself when it lies
+ * strictly inside the slab (shape.cpp:137-159, 220-238). */
+__device__ __forceinline__ double wb_clamp_toward(double a, double c, double side)
+{
+  if (fabs(a - c) < side / 2)
+    return a;
+  return a > c ? c + side / 2 : c - side / 2;
+}
+
 /* Hyperboloid::in (shape.cpp:127-135) for slope > 0, exact double form. */
 __device__ __forceinline__ bool wb_hyp_in(double cx, double cy, double cz, double por2, double slope,
                                          double qx, double qy, double qz)

@@ -33,6 +33,9 @@ struct TileArgs
   const int32_t *child, *nodeBox, *leafBox;
   uint64_t N, L;
   const uint32_t *leafFirst, *leafCount;
+  const uint64_t *leafKey;
+  const uint8_t *leafLev;
+  double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
 };
 
@@ -120,6 +123,22 @@ __global__ void __launch_bounds__(32 * kTileWarps) cylGather(TileArgs a, uint32_
     {
       uint64_t l = (uint64_t)(-2 - code);
       uint32_t f = a.leafFirst[l], cntL = a.leafCount[l];
+      // OctStore::pointsIn semantics: the block's cube must meet the
+      // cylinder; when its four vertical edges are inside, every point counts.
+      double lx, ly, lz, ls;
+      wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
+      bool ct = false;
+      if (lane == 0)
+        ct = wb_hypot(cx - wb_clamp_toward(cx, lx, ls), cy - wb_clamp_toward(cy, ly, ls)) <= a.rad;
+      else if (lane <= 4)
+      {
+        int n = lane - 1;
+        ct = wb_hypot(cx - ((n & 1) ? lx + ls / 2 : lx - ls / 2), cy - ((n & 2) ? ly + ls / 2 : ly - ls / 2)) <= a.rad;
+      }
+      unsigned cb = __ballot_sync(0xffffffffu, ct);
+      if (!(cb & 1))
+        continue;
+      const bool allIn = (cb & 0x1eu) == 0x1eu;
       for (uint32_t t0 = 0; t0 < cntL; t0 += 32)
       {
         uint32_t t = t0 + lane;
@@ -128,7 +147,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) cylGather(TileArgs a, uint32_
         {
           uint32_t j = f + t;
           double px = dec(a, 0, a.sx[j]), py = dec(a, 1, a.sy[j]);
-          in = wb_hypot(cx - px, cy - py) <= a.rad;
+          in = allIn || wb_hypot(cx - px, cy - py) <= a.rad;
         }
         unsigned m = __ballot_sync(0xffffffffu, in);
         if (MODE && in)
@@ -635,6 +654,11 @@ static TileArgs tileArgs(wb_ctx *c)
   a.L = c->n_leaves;
   a.leafFirst = (const uint32_t *)c->leafFirst.p;
   a.leafCount = (const uint32_t *)c->leafCount.p;
+  a.leafKey = (const uint64_t *)c->leafKey.p;
+  a.leafLev = (const uint8_t *)c->leafLevel.p;
+  for (int k = 0; k < 3; k++)
+    a.rootLo[k] = g.root_lo[k];
+  a.rootSide = g.root_side;
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;
