@@ -276,7 +276,7 @@ def main():
 
     info = clf.info()
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
-    dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download")), key=lambda k: stage_ms[k])
+    dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download", "classify_exact")), key=lambda k: stage_ms[k])
     peak, peak_kind = peaks()
     nd = info["n_distinct"]
     alg_bytes = {"classify": CLASSIFY_BYTES_PER_POINT * nd}.get(dom, None)
@@ -293,7 +293,7 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes": alg_bytes, "avg_ms": stage_ms[dom]}
     build_ms = sum(v for k, v in stage_ms.items() if k in ("decode_key", "sort", "dedup", "leaves", "leaf_order",
-                                                         "point_map", "nodes"))
+                                                         "point_map", "nodes", "grid"))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -5,19 +5,29 @@
  * Hyperboloid(p - (0,0,thickness), tile.hyperboloidSize, maxSlope), stopping
  * as soon as no circular gap between successive directions reaches 144
  * degrees (surround, classify.cpp:67-94).  Adding directions can only shrink
- * gaps and the pruning it does never opens one, so the label is a function of
- * the whole neighbour set: 1 (not ground) if it surrounds p, else 2.
+ * gaps, and the pruning surround() does never opens one, so the label is a
+ * function of the neighbour set alone: 1 (not ground) if it surrounds p, else 2.
+ * The neighbour set is what OctStore::pointsIn returns for the hyperboloid.
  *
- * Here one warp classifies one point: it walks the node hierarchy depth-first,
- * pruning boxes the hyperboloid cannot reach, tests the points of each leaf
- * it reaches (32 lanes at a time), and keeps, for 64 direction bins of 2^25
- * units, the smallest and largest direction seen.  Gaps inside a bin are
- * shorter than 144 degrees, so the largest circular gap of the whole set is
- * the largest gap between the last direction of one occupied bin and the first
- * of the next one: the test is exact.  The warp stops when that gap drops
- * below 144 degrees.  A point is classified with the hyperboloid size of its
- * owner tile, the last tile in flowsnake order whose cylinder contains it,
- * because that tile's classification is the one the reference keeps.
+ * One warp classifies one point.  It walks rings of grid columns outward from
+ * the point, so directions from every side arrive early, and stops as soon as
+ * the directions seen surround the point.  Per column it first checks whether
+ * the column's lowest point could be inside the hyperboloid at the column's
+ * nearest distance.  Each candidate is tested in FP32 in a frame centred on p
+ * (integer record differences times the scale); the few whose FP32 value lies
+ * within 1e-5 of the boundary, and points outside the octree root cube (which
+ * the reference treats through their leaf's cube), are tested exactly in
+ * FP64 as the reference computes it.  Directions are FP32 atan2 values in the
+ * reference's integer angle unit; 64 bins keep each bin's extremes, and the
+ * largest circular gap follows from them.  With the direction error bounded
+ * by kMargin units, a gap estimate below 144 degrees - 2*kMargin proves
+ * "surrounded" and one above 144 degrees + 2*kMargin proves the opposite;
+ * anything between is re-run by the exact kernel with the reference's own
+ * integer atan2i (angle.cpp:117-155) and exact bins.
+ *
+ * A point is classified with the hyperboloid size of its owner tile, the last
+ * tile in flowsnake order whose cylinder contains it, because that tile's
+ * classification is the one the reference keeps.
  */
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -29,25 +39,41 @@
 namespace
 {
 constexpr int kWarps = 4;
-constexpr int kStack = 192;
 constexpr int kBins = 64;
+constexpr uint32_t kStray = 0x80000000u;
+/* bound on |FP32 direction - atan2i| in angle units (2^31 per turn); the
+ * FP32 error is below 400 units, so this is a tenfold safety factor. */
+constexpr uint32_t kMargin = 4096;
 
 struct ClsArgs
 {
   uint64_t nd;
   double off[3], scale[3], unit;
   double slope, thickness;
-  const int32_t *child, *nodeBox, *leafBox;
-  uint64_t N, L;
-  const uint32_t *leafFirst, *leafCount;
   const uint64_t *leafKey;
   const uint8_t *leafLev;
+  const uint32_t *leafId;
   double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
   const int32_t *owner;
   const TileRes *tiles;
   const double *tanT, *sinT, *cosT;
   uint8_t *label;
+  /* grid */
+  double gx0, gy0, cell;
+  int nx, ny;
+  uint64_t ncell;
+  const uint32_t *cellStart;
+  const int32_t *cellBox;
+  const int32_t *gx, *gy, *gz;
+  const uint32_t *gpos;
+  double zmin;
+  int exactInts;
+  /* ambiguous points for the exact pass */
+  uint32_t *ambList;
+  uint32_t *ambCount;
+  const uint32_t *work;   /* exact pass: store positions to classify */
+  uint32_t nwork;
 };
 
 __device__ __forceinline__ double decA(const ClsArgs &a, int ax, int32_t q)
@@ -55,32 +81,123 @@ __device__ __forceinline__ double decA(const ClsArgs &a, int ax, int32_t q)
   return wb_decode(q, a.off[ax], a.scale[ax], a.unit);
 }
 
-/* Could any point of the box lie inside the hyperboloid?  The most favourable
- * point of a box is its lowest corner height at the xy position nearest the
- * axis; a small relative slack keeps this conservative. */
-__device__ __forceinline__ bool boxMeetsHyp(const ClsArgs &a, const int32_t *box, uint64_t stride, uint64_t id,
-                                            double cx, double cy, double cz, double por2)
+struct Hyp
 {
-  double x0 = decA(a, 0, box[0 * stride + id]), x1 = decA(a, 0, box[3 * stride + id]);
-  double y0 = decA(a, 1, box[1 * stride + id]), y1 = decA(a, 1, box[4 * stride + id]);
-  double z0 = decA(a, 2, box[2 * stride + id]);
-  double dx = cx < x0 ? x0 - cx : (cx > x1 ? cx - x1 : 0.0);
-  double dy = cy < y0 ? y0 - cy : (cy > y1 ? cy - y1 : 0.0);
-  double zd = cz - z0;
-  if (!(zd > 0))
+  double cx, cy, cz, por2;      /* exact Hyperboloid members (centre, polar radius^2) */
+  double px, py;                /* the point, decoded                                  */
+  int32_t qx, qy, qz;           /* the point, record integers                          */
+  float sx, sy, sz;             /* metres per record unit                              */
+  float czp, s2, por2f;         /* cz - pz, slope^2, por^2 in FP32                     */
+};
+
+/* OctStore::pointsIn membership of one candidate, exactly: Hyperboloid::in on
+ * the decoded doubles; for a point outside the root cube, its leaf cube must
+ * meet the hyperboloid (Octree::findBlocks) and then either all eight corners
+ * are inside (the whole block is taken) or the point itself is. */
+__device__ bool memberExact(const ClsArgs &a, const Hyp &h, uint32_t gp, int32_t qx, int32_t qy, int32_t qz)
+{
+  double x = decA(a, 0, qx), y = decA(a, 1, qy), z = decA(a, 2, qz);
+  bool in = wb_hyp_in(h.cx, h.cy, h.cz, h.por2, a.slope, x, y, z);
+  if (!(gp & kStray))
+    return in;
+  uint32_t l = a.leafId[gp & ~kStray];
+  double lx, ly, lz, ls;
+  wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
+  if (!wb_hyp_in(h.cx, h.cy, h.cz, h.por2, a.slope, wb_clamp_toward(h.cx, lx, ls), wb_clamp_toward(h.cy, ly, ls),
+                 lz - ls / 2))
     return false;
-  double lhs = zd * zd - a.slope * a.slope * (dx * dx + dy * dy);
-  return lhs >= por2 - 1e-9 * (zd * zd + por2) - 1e-12;
+  bool all = true;
+  for (int n = 0; n < 8 && all; n++)
+    all = wb_hyp_in(h.cx, h.cy, h.cz, h.por2, a.slope, (n & 1) ? lx + ls / 2 : lx - ls / 2,
+                    (n & 2) ? ly + ls / 2 : ly - ls / 2, (n & 4) ? lz + ls / 2 : lz - ls / 2);
+  return all || in;
 }
 
-__global__ void __launch_bounds__(32 * kWarps) classifyKernel(ClsArgs a)
+/* Can any point of column c be inside?  FP32 with generous slack. */
+__device__ __forceinline__ bool cellMeets(const ClsArgs &a, const Hyp &h, uint64_t c)
 {
-  __shared__ int32_t stack[kWarps][kStack];
+  const uint64_t N = a.ncell;
+  float xl = (float)((int64_t)a.cellBox[c] - h.qx) * h.sx, xh = (float)((int64_t)a.cellBox[3 * N + c] - h.qx) * h.sx;
+  float yl = (float)((int64_t)a.cellBox[N + c] - h.qy) * h.sy, yh = (float)((int64_t)a.cellBox[4 * N + c] - h.qy) * h.sy;
+  float zd = (float)((int64_t)h.qz - a.cellBox[2 * N + c]) * h.sz + h.czp;
+  float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
+  float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
+  float r2 = h.s2 * (dx * dx + dy * dy);
+  float mag = zd * zd + r2 + h.por2f;
+  if (zd < -1e-4f * (fabsf(zd) + 1e-3f))
+    return false;
+  return zd * zd - r2 - h.por2f >= -(1e-4f * mag + 1e-9f);
+}
+
+/* Column offset of ring cell m (0 <= m < 8k) at Chebyshev distance k. */
+__device__ __forceinline__ void ringCell(int k, int m, int &di, int &dj)
+{
+  if (k == 0)
+  {
+    di = dj = 0;
+    return;
+  }
+  int side = m / (2 * k), o = m % (2 * k);
+  if (side == 0)
+  {
+    di = -k + o;
+    dj = -k;
+  }
+  else if (side == 1)
+  {
+    di = k;
+    dj = -k + o;
+  }
+  else if (side == 2)
+  {
+    di = k - o;
+    dj = k;
+  }
+  else
+  {
+    di = -k;
+    dj = k - o;
+  }
+}
+
+/* Largest circular gap between occupied bins' extremes; lanes hold 2 bins. */
+__device__ __forceinline__ uint32_t largestGap(const uint32_t *bmin, const uint32_t *bmax, int lane, int &nocc)
+{
+  uint32_t mn0 = bmin[lane], mn1 = bmin[lane + 32];
+  uint32_t mx0 = bmax[lane], mx1 = bmax[lane + 32];
+  unsigned lo = __ballot_sync(0xffffffffu, mn0 != 0xffffffffu);
+  unsigned hi = __ballot_sync(0xffffffffu, mn1 != 0xffffffffu);
+  uint64_t occ = ((uint64_t)hi << 32) | lo;
+  nocc = __popcll(occ);
+  uint32_t worst = 0;
+  if (nocc >= 2)
+  {
+    for (int half = 0; half < 2; half++)
+    {
+      int b = lane + 32 * half;
+      if ((occ >> b) & 1)
+      {
+        uint64_t rot = (b == 63) ? 0 : (occ >> (b + 1));
+        int nb = rot ? b + 1 + __ffsll((long long)rot) - 1 : __ffsll((long long)occ) - 1;
+        uint32_t gap = (bmin[nb] - (half ? mx1 : mx0)) & 0x7fffffffu;
+        worst = max(worst, gap);
+      }
+    }
+    for (int o = 16; o; o >>= 1)
+      worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  }
+  return worst;
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
+{
   __shared__ uint32_t bmin[kWarps][kBins], bmax[kWarps][kBins];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t j = (uint64_t)blockIdx.x * kWarps + w;
-  if (j >= a.nd)
+  uint64_t item = (uint64_t)blockIdx.x * kWarps + w;
+  if (item >= (EXACT ? (uint64_t)a.nwork : a.nd))
     return;
+  uint64_t j = EXACT ? a.work[item] : item;
   int32_t k = a.owner[j];
   if (k < 0)
   {
@@ -88,131 +205,149 @@ __global__ void __launch_bounds__(32 * kWarps) classifyKernel(ClsArgs a)
       a.label[j] = 0;
     return;
   }
-  double h = a.tiles[k].h;
-  double px = decA(a, 0, a.sx[j]), py = decA(a, 1, a.sy[j]), pz = decA(a, 2, a.sz[j]);
-  // Hyperboloid(v, h, slope) with v = p - (0,0,thickness)  (shape.cpp:119-125)
-  double por = h * (a.slope * a.slope);
-  double por2 = por * por;
-  double cx = px + 0, cy = py + 0, cz = (pz - a.thickness) + por;
+  Hyp h;
+  h.qx = a.sx[j];
+  h.qy = a.sy[j];
+  h.qz = a.sz[j];
+  double hs = a.tiles[k].h;
+  h.px = decA(a, 0, h.qx);
+  h.py = decA(a, 1, h.qy);
+  double pz = decA(a, 2, h.qz);
+  // Hyperboloid(v, hs, slope), v = p - (0,0,thickness)  (shape.cpp:119-125)
+  double por = hs * (a.slope * a.slope);
+  h.por2 = por * por;
+  h.cx = h.px + 0;
+  h.cy = h.py + 0;
+  h.cz = (pz - a.thickness) + por;
+  h.sx = (float)(a.scale[0] * a.unit);
+  h.sy = (float)(a.scale[1] * a.unit);
+  h.sz = (float)(a.scale[2] * a.unit);
+  h.czp = (float)(h.cz - pz);
+  h.s2 = (float)(a.slope * a.slope);
+  h.por2f = (float)h.por2;
   for (int b = lane; b < kBins; b += 32)
   {
     bmin[w][b] = 0xffffffffu;
     bmax[w][b] = 0;
   }
   __syncwarp();
-  bool surrounded = false;
-  int sp = 1;
-  if (lane == 0)
-    stack[w][0] = 0;
-  __syncwarp();
-  if (a.N == 0)
-    sp = 0;
-  while (sp > 0 && !surrounded)
+  // horizontal reach of the hyperboloid at the lowest point of the cloud
+  double zdMax = h.cz - a.zmin;
+  double reach2 = (zdMax * zdMax - h.por2) / (a.slope * a.slope);
+  double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
+  int ci = (int)floor((h.px - a.gx0) / a.cell), cj = (int)floor((h.py - a.gy0) / a.cell);
+  int kmax = (int)ceil(reach / a.cell) + 1;
+  bool surrounded = false, ambiguous = false;
+  const bool fast = !EXACT && a.exactInts;
+  for (int ring = 0; ring <= kmax && !surrounded; ring++)
   {
-    int32_t code = stack[w][sp - 1];
-    sp--;
-    __syncwarp();
-    if (code >= 0)
-    {
-      int32_t ch = -1;
-      bool meet = false;
-      if (lane < 8)
-      {
-        ch = a.child[(uint64_t)code * 8 + lane];
-        if (ch >= 0)
-          meet = boxMeetsHyp(a, a.nodeBox, a.N, (uint64_t)ch, cx, cy, cz, por2);
-        else if (ch <= -2)
-          meet = boxMeetsHyp(a, a.leafBox, a.L, (uint64_t)(-2 - ch), cx, cy, cz, por2);
-      }
-      unsigned m = __ballot_sync(0xffffffffu, meet);
-      if (meet)
-        stack[w][sp + __popc(m >> (lane + 1))] = ch;
-      sp += __popc(m);
-      __syncwarp();
+    if (ci + ring < 0 || ci - ring >= a.nx || cj + ring < 0 || cj - ring >= a.ny)
       continue;
-    }
-    uint64_t l = (uint64_t)(-2 - code);
-    uint32_t f = a.leafFirst[l], cnt = a.leafCount[l];
-    // OctStore::pointsIn (octree.cpp:1214-1242): a block counts only if its
-    // cube meets the shape (Octree::findBlocks); if all eight corners are
-    // inside, all its points are taken without testing them one by one.
-    // The two differ from testing every point only for points outside the
-    // root cube (Octree::sizeFit can leave a sliver of the cloud below it).
-    bool cubeTest = false;
+    int ncells = ring == 0 ? 1 : 8 * ring;
+    bool gotAny = false;
+    for (int m0 = 0; m0 < ncells; m0 += 32)
     {
-      double lx, ly, lz, ls;
-      wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
-      if (lane == 0)
-        cubeTest = wb_hyp_in(cx, cy, cz, por2, a.slope, wb_clamp_toward(cx, lx, ls), wb_clamp_toward(cy, ly, ls),
-                             lz - ls / 2);
-      else if (lane <= 8)
+      int m = m0 + lane;
+      uint64_t c = 0;
+      bool ok = false;
+      if (m < ncells)
       {
-        int n = lane - 1;
-        cubeTest = wb_hyp_in(cx, cy, cz, por2, a.slope, (n & 1) ? lx + ls / 2 : lx - ls / 2,
-                             (n & 2) ? ly + ls / 2 : ly - ls / 2, (n & 4) ? lz + ls / 2 : lz - ls / 2);
-      }
-    }
-    unsigned cb = __ballot_sync(0xffffffffu, cubeTest);
-    if (!(cb & 1))
-      continue;
-    const bool allIn = (cb & 0x1feu) == 0x1feu;
-    for (uint32_t t0 = 0; t0 < cnt; t0 += 32)
-    {
-      uint32_t t = t0 + lane;
-      if (t < cnt)
-      {
-        uint32_t q = f + t;
-        double qx = decA(a, 0, a.sx[q]), qy = decA(a, 1, a.sy[q]), qz = decA(a, 2, a.sz[q]);
-        if (allIn || wb_hyp_in(cx, cy, cz, por2, a.slope, qx, qy, qz))
+        int di, dj;
+        ringCell(ring, m, di, dj);
+        int i = ci + di, jj = cj + dj;
+        if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
-          double dx = qx - px, dy = qy - py;
-          if (wb_hypot(px - qx, py - qy) != 0)
+          c = (uint64_t)jj * a.nx + i;
+          ok = a.cellStart[c] != a.cellStart[c + 1] && cellMeets(a, h, c);
+        }
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, ok);
+      while (mask)
+      {
+        int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        uint64_t cc = __shfl_sync(0xffffffffu, c, src);
+        uint32_t b = a.cellStart[cc], e = a.cellStart[cc + 1];
+        for (uint32_t t0 = b; t0 < e; t0 += 32)
+        {
+          uint32_t t = t0 + lane;
+          if (t >= e)
+            continue;
+          int32_t qx = a.gx[t], qy = a.gy[t], qz = a.gz[t];
+          uint32_t gp = a.gpos[t];
+          int64_t dxi = (int64_t)qx - h.qx, dyi = (int64_t)qy - h.qy;
+          uint32_t u;
+          if (fast)
           {
-            int d = wb_atan2i(dy, dx, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
-            uint32_t u = (uint32_t)d & 0x7fffffffu;
-            atomicMin(&bmin[w][u >> 25], u);
-            atomicMax(&bmax[w][u >> 25], u);
+            if (dxi == 0 && dyi == 0)
+              continue;   // dist(p,q) == 0: no direction (classify.cpp:142,153)
+            bool in;
+            float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
+            if (gp & kStray)
+              in = memberExact(a, h, gp, qx, qy, qz);
+            else
+            {
+              float dzm = (float)((int64_t)h.qz - qz) * h.sz;
+              float zd = dzm + h.czp;
+              float r2 = h.s2 * (dx * dx + dy * dy);
+              float f = zd * zd - r2 - h.por2f;
+              float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
+              float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
+              if (zd > ztol && f > tol)
+                in = true;
+              else if (zd < -ztol || f < -tol)
+                in = false;
+              else
+                in = memberExact(a, h, gp, qx, qy, qz);
+            }
+            if (!in)
+              continue;
+            float th = atan2f(dy, dx);
+            int d = __float2int_rn(th * 341782637.79f);   // 2^30 / pi
+            u = (uint32_t)d & 0x7fffffffu;
           }
+          else
+          {
+            double x = decA(a, 0, qx), y = decA(a, 1, qy);
+            if (wb_hypot(h.px - x, h.py - y) == 0)
+              continue;
+            if (!memberExact(a, h, gp, qx, qy, qz))
+              continue;
+            int d = wb_atan2i(y - h.py, x - h.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
+            u = (uint32_t)d & 0x7fffffffu;
+          }
+          atomicMin(&bmin[w][u >> 25], u);
+          atomicMax(&bmax[w][u >> 25], u);
+          gotAny = true;
         }
       }
     }
+    if (!__any_sync(0xffffffffu, gotAny))
+      continue;
     __syncwarp();
-    // exact largest circular gap from the bin extremes
-    uint32_t mn0 = bmin[w][lane], mn1 = bmin[w][lane + 32];
-    uint32_t mx0 = bmax[w][lane], mx1 = bmax[w][lane + 32];
-    unsigned occLo = __ballot_sync(0xffffffffu, mn0 != 0xffffffffu);
-    unsigned occHi = __ballot_sync(0xffffffffu, mn1 != 0xffffffffu);
-    uint64_t occ = ((uint64_t)occHi << 32) | occLo;
-    int nocc = __popcll(occ);
-    bool sur = false;
+    int nocc;
+    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
     if (nocc >= 2)
     {
-      uint32_t worst = 0;
-      for (int half = 0; half < 2; half++)
-      {
-        int b = lane + 32 * half;
-        if ((occ >> b) & 1)
-        {
-          // next occupied bin after b, circularly
-          uint64_t rot = (b == 63) ? 0 : (occ >> (b + 1));
-          int nb = rot ? b + 1 + __ffsll((long long)rot) - 1 : __ffsll((long long)occ) - 1;
-          uint32_t gap = (bmin[w][nb] - (half ? mx1 : mx0)) & 0x7fffffffu;
-          worst = max(worst, gap);
-        }
-      }
-      for (int o = 16; o; o >>= 1)
-        worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
-      sur = worst < (uint32_t)WB_DEG144;
+      if (EXACT || !fast)
+        surrounded = gap < (uint32_t)WB_DEG144;
+      else
+        surrounded = gap + 2 * kMargin < (uint32_t)WB_DEG144;
     }
-    else if (nocc == 1)
-    {
-      // one bin: at least two distinct directions and every gap < 144 degrees is impossible
-      sur = false;
-    }
-    surrounded = sur;
+  }
+  if (!surrounded && fast)
+  {
+    int nocc;
+    __syncwarp();
+    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
+    ambiguous = nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
   }
   if (lane == 0)
+  {
     a.label[j] = surrounded ? 1 : 2;
+    if (ambiguous)
+      a.ambList[atomicAdd(a.ambCount, 1u)] = (uint32_t)j;
+  }
 }
 
 __global__ void scatterCls(uint64_t n, const uint32_t *__restrict__ storeOf, const int32_t *__restrict__ owner,
@@ -241,15 +376,34 @@ __global__ void zeroGround(uint64_t T, TileRes *__restrict__ tiles)
 }
 }  // namespace
 
+/* Decoding is strictly increasing in every record integer when the step
+ * scale*unit is at least four ulps of every coordinate the root cube spans;
+ * then equal decoded doubles mean equal integers, and FP32 differences of
+ * integers stand for differences of the doubles. */
+static bool decodeIsExact(const WbGeom &g, const double mn[3], const double mx[3])
+{
+  for (int a = 0; a < 3; a++)
+  {
+    double step = fabs(g.scale[a] * g.unit);
+    double mag = fmax(fabs(mn[a]), fabs(mx[a])) + fabs(g.off[a] * g.unit) + step;
+    if (!(step > 0) || step < 4 * ldexp(mag, -52))
+      return false;
+  }
+  return true;
+}
+
 int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
 {
   if (c->stage < 2)
     return wb_fail(c, WB_ESTATE, "wb_classify: scan the tiles first");
   if (!cls && c->n)
     return wb_fail(c, WB_EINVAL, "wb_classify: cls must not be NULL");
+  if (!(p->max_slope > 0))
+    return wb_fail(c, WB_EINVAL, "wb_classify: max_slope must be > 0");
   int rc;
   uint64_t nd = c->nd, n = c->n;
-  if ((rc = wb_ensure(c, c->label, nd + 64)) || (rc = wb_ensure(c, c->angleT, (511 + 512 + 512) * 8)))
+  if ((rc = wb_ensure(c, c->label, nd + 64)) || (rc = wb_ensure(c, c->angleT, (511 + 512 + 512) * 8)) ||
+      (rc = wb_ensure(c, c->ambiguous, nd * 4 + 64)))
     return rc;
   if (!onDevice && (rc = wb_ensure(c, c->clsDev, n + 64)))
     return rc;
@@ -263,26 +417,23 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   wb_mark(c, "cls_upload");
   ClsArgs a;
   a.nd = nd;
+  const WbGeom &g = c->g;
+  double mn[3], mx[3];
   for (int k = 0; k < 3; k++)
   {
-    a.off[k] = c->g.off[k];
-    a.scale[k] = c->g.scale[k];
+    a.off[k] = g.off[k];
+    a.scale[k] = g.scale[k];
+    a.rootLo[k] = g.root_lo[k];
+    mn[k] = g.root_lo[k];
+    mx[k] = g.root_lo[k] + g.root_side;
   }
-  a.unit = c->g.unit;
+  a.unit = g.unit;
   a.slope = p->max_slope;
   a.thickness = p->thickness;
-  a.child = (const int32_t *)c->nodeChild.p;
-  a.nodeBox = (const int32_t *)c->nodeBox.p;
-  a.leafBox = (const int32_t *)c->leafBox.p;
-  a.N = c->n_nodes;
-  a.L = c->n_leaves;
-  a.leafFirst = (const uint32_t *)c->leafFirst.p;
-  a.leafCount = (const uint32_t *)c->leafCount.p;
   a.leafKey = (const uint64_t *)c->leafKey.p;
   a.leafLev = (const uint8_t *)c->leafLevel.p;
-  for (int k = 0; k < 3; k++)
-    a.rootLo[k] = c->g.root_lo[k];
-  a.rootSide = c->g.root_side;
+  a.leafId = (const uint32_t *)c->leafId.p;
+  a.rootSide = g.root_side;
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;
@@ -292,17 +443,48 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   a.sinT = tab + 511;
   a.cosT = tab + 1023;
   a.label = (uint8_t *)c->label.p;
+  a.gx0 = c->grid.x0;
+  a.gy0 = c->grid.y0;
+  a.cell = c->grid.cell;
+  a.nx = c->grid.nx;
+  a.ny = c->grid.ny;
+  a.ncell = c->grid.ncell;
+  a.cellStart = (const uint32_t *)c->cellStart.p;
+  a.cellBox = (const int32_t *)c->cellBox.p;
+  a.gx = (const int32_t *)c->gx.p;
+  a.gy = (const int32_t *)c->gy.p;
+  a.gz = (const int32_t *)c->gz.p;
+  a.gpos = (const uint32_t *)c->gpos.p;
+  a.zmin = (g.off[2] + g.scale[2] * (double)c->grid.zminInt) * g.unit;
+  a.exactInts = decodeIsExact(g, mn, mx) ? 1 : 0;
+  a.ambList = (uint32_t *)c->ambiguous.p;
+  a.ambCount = (uint32_t *)((char *)c->small.p + 448);
+  a.work = nullptr;
+  a.nwork = 0;
+  WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 4, c->stream));
   if (nd)
   {
-    { classifyKernel<<<(unsigned)((nd + kWarps - 1) / kWarps), 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
+    { classifyRings<false><<<(unsigned)((nd + kWarps - 1) / kWarps), 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
     WB_CUDA(c, cudaGetLastError());
   }
   wb_mark(c, "classify");
-  unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
-  { zeroGround<<<g, 256, 0, c->stream>>>(c->n_tiles, (TileRes *)c->tileRes.p); ++c->launches; }
-  { groundCount<<<g, 256, 0, c->stream>>>(nd, a.owner, a.label, (TileRes *)c->tileRes.p); ++c->launches; }
+  uint32_t namb = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&namb, a.ambCount, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->n_ambiguous = namb;
+  if (namb)
+  {
+    a.work = a.ambList;
+    a.nwork = namb;
+    { classifyRings<true><<<(namb + kWarps - 1) / kWarps, 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
+    WB_CUDA(c, cudaGetLastError());
+  }
+  wb_mark(c, "classify_exact");
+  unsigned gsz = (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
+  { zeroGround<<<gsz, 256, 0, c->stream>>>(c->n_tiles, (TileRes *)c->tileRes.p); ++c->launches; }
+  { groundCount<<<gsz, 256, 0, c->stream>>>(nd, a.owner, a.label, (TileRes *)c->tileRes.p); ++c->launches; }
   if (n)
-    { scatterCls<<<g, 256, 0, c->stream>>>(n, (const uint32_t *)c->storeOf.p, a.owner, a.label, clsDev); ++c->launches; }
+    { scatterCls<<<gsz, 256, 0, c->stream>>>(n, (const uint32_t *)c->storeOf.p, a.owner, a.label, clsDev); ++c->launches; }
   if (!onDevice && n)
     WB_CUDA(c, cudaMemcpyAsync(cls, clsDev, n, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaGetLastError());

@@ -1,0 +1,200 @@
+/* Column grid over the point store, the spatial index of the tile gather and
+ * of classify.
+ *
+ * The reference answers every neighbourhood query by descending the octree
+ * (Octree::findBlocks, octree.cpp:234-251).  Both queries of this path are
+ * vertical: a cylinder (any z) and a downward hyperboloid whose horizontal
+ * reach grows with depth.  A 2-D grid of square columns answers them with
+ * plain ring walks: cells are visited outward from the query axis, so the
+ * directions a classify query collects spread around the point early and the
+ * surround test can stop after a few rings.
+ *
+ * Cells hold store positions sorted stably (so each cell lists its points in
+ * store order), a copy of the points' integer X/Y/Z in grid order for
+ * coalesced reads, and per-cell integer bounds for pruning.  A point that
+ * lies outside the octree root cube is flagged: the reference's queries treat
+ * such points through their leaf's cube, and the kernels do the same for them.
+ */
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include "wb_internal.h"
+#include "wb_device.cuh"
+
+namespace
+{
+struct GridArgs
+{
+  uint64_t nd;
+  double off[3], scale[3], unit;
+  double x0, y0, cell;
+  int nx, ny;
+  double rootLo[3], rootHi[3];
+};
+
+__global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
+                           const int32_t *__restrict__ sz, uint64_t *__restrict__ key, uint32_t *__restrict__ val,
+                           uint8_t *__restrict__ stray, unsigned long long *__restrict__ nStray)
+{
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.nd; j += (uint64_t)gridDim.x * blockDim.x)
+  {
+    double x = wb_decode(sx[j], g.off[0], g.scale[0], g.unit);
+    double y = wb_decode(sy[j], g.off[1], g.scale[1], g.unit);
+    double z = wb_decode(sz[j], g.off[2], g.scale[2], g.unit);
+    int cx = (int)floor((x - g.x0) / g.cell), cy = (int)floor((y - g.y0) / g.cell);
+    cx = min(max(cx, 0), g.nx - 1);
+    cy = min(max(cy, 0), g.ny - 1);
+    key[j] = (uint64_t)cy * g.nx + cx;
+    val[j] = (uint32_t)j;
+    bool s = x < g.rootLo[0] || y < g.rootLo[1] || z < g.rootLo[2] || x >= g.rootHi[0] || y >= g.rootHi[1] ||
+             z >= g.rootHi[2];
+    stray[j] = s;
+    if (s)
+      atomicAdd(nStray, 1ull);
+  }
+}
+
+__global__ void cellStartKernel(uint64_t nd, uint64_t ncell, const uint64_t *__restrict__ key,
+                                uint32_t *__restrict__ start)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint64_t k = key[i];
+    uint64_t prev = i ? key[i - 1] : (uint64_t)-1;
+    if (i == 0)
+      for (uint64_t c = 0; c <= k; c++)
+        start[c] = 0;
+    else if (k != prev)
+      for (uint64_t c = prev + 1; c <= k; c++)
+        start[c] = (uint32_t)i;
+    if (i == nd - 1)
+      for (uint64_t c = k + 1; c <= ncell; c++)
+        start[c] = (uint32_t)nd;
+  }
+}
+
+/* Gathers X/Y/Z into grid order and forms each cell's bounds; one warp per cell. */
+__global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ start, const uint32_t *__restrict__ pos,
+                               const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
+                               const int32_t *__restrict__ sz, const uint8_t *__restrict__ stray,
+                               int32_t *__restrict__ gx, int32_t *__restrict__ gy, int32_t *__restrict__ gz,
+                               uint32_t *__restrict__ gpos, int32_t *__restrict__ box)
+{
+  uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (c >= ncell)
+    return;
+  uint32_t b = start[c], e = start[c + 1];
+  int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+  for (uint32_t i = b + lane; i < e; i += 32)
+  {
+    uint32_t j = pos[i];
+    int32_t q[3] = {sx[j], sy[j], sz[j]};
+    gx[i] = q[0];
+    gy[i] = q[1];
+    gz[i] = q[2];
+    gpos[i] = j | (stray[j] ? 0x80000000u : 0u);
+    for (int a = 0; a < 3; a++)
+    {
+      mn[a] = min(mn[a], q[a]);
+      mx[a] = max(mx[a], q[a]);
+    }
+  }
+  for (int a = 0; a < 3; a++)
+    for (int o = 16; o; o >>= 1)
+    {
+      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  if (lane < 6)
+  {
+    int32_t v = lane < 3 ? mn[lane] : mx[lane - 3];
+    box[(uint64_t)lane * ncell + c] = v;
+  }
+}
+
+__global__ void zminKernel(uint64_t nd, const int32_t *__restrict__ sz, int *__restrict__ out)
+{
+  int m = INT32_MAX;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
+    m = min(m, sz[j]);
+  for (int o = 16; o; o >>= 1)
+    m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0)
+    atomicMin(out, m);
+}
+}  // namespace
+
+int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
+{
+  uint64_t nd = c->nd;
+  WbGeom &g = c->g;
+  double w = fmax(x1 - x0, 1e-9), h = fmax(y1 - y0, 1e-9);
+  // about 32 points per occupied column, at most 2^24 columns
+  double cell = sqrt(w * h * 32.0 / (double)(nd ? nd : 1));
+  double minCell = sqrt(w * h / (double)(1u << 24));
+  if (cell < minCell)
+    cell = minCell;
+  int nx = (int)ceil(w / cell) + 1, ny = (int)ceil(h / cell) + 1;
+  c->grid.x0 = x0;
+  c->grid.y0 = y0;
+  c->grid.cell = cell;
+  c->grid.nx = nx;
+  c->grid.ny = ny;
+  uint64_t ncell = (uint64_t)nx * ny;
+  c->grid.ncell = ncell;
+  int rc;
+  if ((rc = wb_ensure(c, c->gKey0, nd * 8 + 64)) || (rc = wb_ensure(c, c->gKey1, nd * 8 + 64)) ||
+      (rc = wb_ensure(c, c->gVal0, nd * 4 + 64)) || (rc = wb_ensure(c, c->gVal1, nd * 4 + 64)) ||
+      (rc = wb_ensure(c, c->stray, nd + 64)) || (rc = wb_ensure(c, c->cellStart, (ncell + 1) * 4 + 64)) ||
+      (rc = wb_ensure(c, c->cellBox, ncell * 24 + 64)) || (rc = wb_ensure(c, c->gx, nd * 4 + 64)) ||
+      (rc = wb_ensure(c, c->gy, nd * 4 + 64)) || (rc = wb_ensure(c, c->gz, nd * 4 + 64)) ||
+      (rc = wb_ensure(c, c->gpos, nd * 4 + 64)))
+    return rc;
+  GridArgs a;
+  a.nd = nd;
+  for (int k = 0; k < 3; k++)
+  {
+    a.off[k] = g.off[k];
+    a.scale[k] = g.scale[k];
+    a.rootLo[k] = g.root_lo[k];
+    a.rootHi[k] = g.root_lo[k] + g.root_side;
+  }
+  a.unit = g.unit;
+  a.x0 = x0;
+  a.y0 = y0;
+  a.cell = cell;
+  a.nx = nx;
+  a.ny = ny;
+  unsigned long long *dStray = (unsigned long long *)((char *)c->small.p + 256);
+  int *dZmin = (int *)((char *)c->small.p + 320);
+  int big = INT32_MAX;
+  WB_CUDA(c, cudaMemsetAsync(dStray, 0, 8, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(dZmin, &big, 4, cudaMemcpyHostToDevice, c->stream));
+  unsigned blocks = (unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
+  uint64_t *key = (uint64_t *)c->gKey0.p;
+  uint32_t *val = (uint32_t *)c->gVal0.p;
+  { cellKernel<<<blocks, 256, 0, c->stream>>>(a, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
+                                              (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray); ++c->launches; }
+  { zminKernel<<<blocks, 256, 0, c->stream>>>(nd, (const int32_t *)c->sz.p, dZmin); ++c->launches; }
+  int bits = 1;
+  while ((1ull << bits) < ncell)
+    bits++;
+  if ((rc = wb_radix_sort_pairs(c, key, val, (uint64_t *)c->gKey1.p, (uint32_t *)c->gVal1.p, nd, 0, bits)))
+    return rc;
+  uint32_t *start = (uint32_t *)c->cellStart.p;
+  { cellStartKernel<<<blocks, 256, 0, c->stream>>>(nd, ncell, key, start); ++c->launches; }
+  { cellFillKernel<<<(unsigned)((ncell * 32 + 255) / 256), 256, 0, c->stream>>>(
+        ncell, start, val, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p, (const int32_t *)c->sz.p,
+        (const uint8_t *)c->stray.p, (int32_t *)c->gx.p, (int32_t *)c->gy.p, (int32_t *)c->gz.p,
+        (uint32_t *)c->gpos.p, (int32_t *)c->cellBox.p); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  unsigned long long ns = 0;
+  int zmin = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&ns, dStray, 8, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&zmin, dZmin, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->grid.nStray = ns;
+  c->grid.zminInt = zmin;
+  return 0;
+}

@@ -26,6 +26,15 @@ struct WbGeom
   bool exact_ints;                  /* decode is strictly increasing in X, Y, Z */
 };
 
+/* Column grid over the point store (wb_grid.cu). */
+struct GridInfo
+{
+  double x0 = 0, y0 = 0, cell = 1;
+  int nx = 0, ny = 0;
+  uint64_t ncell = 0, nStray = 0;
+  int zminInt = 0;
+};
+
 struct wb_ctx
 {
   int device = 0;
@@ -40,6 +49,7 @@ struct wb_ctx
   int stage = 0;                    /* 0 empty, 1 built, 2 scanned, 3 classified */
   uint64_t n = 0, nd = 0, n_leaves = 0, n_nodes = 0, n_tiles = 0, n_pairs = 0;
   uint32_t max_depth = 0;
+  uint64_t n_ambiguous = 0;         /* points the exact classify pass re-ran */
   WbGeom g{};
   wb_params params{};
 
@@ -51,6 +61,8 @@ struct wb_ctx
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
   DevBuf label, clsDev, ambiguous, angleT;
+  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos;
+  GridInfo grid;
   DevBuf flowCache;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
   int flowIdxCached = -1;
@@ -97,6 +109,7 @@ int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *k
 
 /* stages */
 int wb_build_impl(wb_ctx *c, const wb_cloud *cloud);
+int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1);
 int wb_scan_impl(wb_ctx *c, const wb_params *p);
 int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice);
 int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf);

@@ -21,7 +21,6 @@
 
 namespace
 {
-constexpr int kStack = 192;
 constexpr int kTileWarps = 4;
 
 struct TileArgs
@@ -53,115 +52,203 @@ __device__ __forceinline__ double dec(const TileArgs &a, int ax, int32_t q)
   return wb_decode(q, a.off[ax], a.scale[ax], a.unit);
 }
 
-/* Can a box (integer X/Y bounds) hold a point within rad of (x,y)?  Slack of
- * 1e-9 relative keeps the pruning conservative; points are tested exactly. */
-__device__ __forceinline__ bool boxMeetsCyl(const TileArgs &a, const int32_t *box, uint64_t stride, uint64_t id,
-                                            double x, double y)
+struct GridDev
 {
-  double x0 = dec(a, 0, box[0 * stride + id]), x1 = dec(a, 0, box[3 * stride + id]);
-  double y0 = dec(a, 1, box[1 * stride + id]), y1 = dec(a, 1, box[4 * stride + id]);
-  double dx = x < x0 ? x0 - x : (x > x1 ? x - x1 : 0.0);
-  double dy = y < y0 ? y0 - y : (y > y1 ? y - y1 : 0.0);
+  double x0, y0, cell;
+  int nx, ny;
+  const uint32_t *cellStart;
+  const int32_t *cellBox;
+  uint64_t ncell;
+  const int32_t *gx, *gy;
+  const uint32_t *gpos;
+  const uint32_t *leafId;
+};
+
+/* Cylinder::in for one point, exactly as the reference evaluates it; points
+ * outside the root cube go through their leaf cube as OctStore::pointsIn
+ * does (findBlocks test on the cube, all-corners fast path). */
+__device__ bool cylExact(const TileArgs &a, const GridDev &gd, double cx, double cy, uint32_t gp, int32_t qx, int32_t qy)
+{
+  double px = dec(a, 0, qx), py = dec(a, 1, qy);
+  bool in = wb_hypot(cx - px, cy - py) <= a.rad;
+  if (!(gp & 0x80000000u))
+    return in;
+  uint32_t l = gd.leafId[gp & 0x7fffffffu];
+  double lx, ly, lz, ls;
+  wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
+  if (!(wb_hypot(cx - wb_clamp_toward(cx, lx, ls), cy - wb_clamp_toward(cy, ly, ls)) <= a.rad))
+    return false;
+  bool all = true;
+  for (int n = 0; n < 4; n++)
+    all = all && wb_hypot(cx - ((n & 1) ? lx + ls / 2 : lx - ls / 2), cy - ((n & 2) ? ly + ls / 2 : ly - ls / 2)) <= a.rad;
+  return all || in;
+}
+
+struct TileFrame
+{
+  double cx, cy;        /* cylinder centre (doubles, as Flowsnake::cyl)     */
+  int32_t qx0, qy0;     /* integer part of the centre in record units       */
+  float fx, fy;         /* fractional part                                  */
+  float sx, sy;         /* metres per record unit                           */
+  float r2lo, r2hi;     /* squared radius band that needs the exact test    */
+  int i0, i1, j0, j1;   /* grid cells covering the cylinder                 */
+};
+
+__device__ TileFrame tileFrame(const TileArgs &a, const GridDev &gd, uint64_t k)
+{
+  TileFrame f;
+  tileCenter(a, k, f.cx, f.cy);
+  double ux = (f.cx / a.unit - a.off[0]) / a.scale[0], uy = (f.cy / a.unit - a.off[1]) / a.scale[1];
+  double fx = floor(ux), fy = floor(uy);
+  f.qx0 = (int32_t)fmax(fmin(fx, 2147483647.0), -2147483648.0);
+  f.qy0 = (int32_t)fmax(fmin(fy, 2147483647.0), -2147483648.0);
+  f.fx = (float)(ux - fx);
+  f.fy = (float)(uy - fy);
+  f.sx = (float)(a.scale[0] * a.unit);
+  f.sy = (float)(a.scale[1] * a.unit);
+  float r2 = (float)(a.rad * a.rad);
+  f.r2lo = r2 * (1 - 2e-5f);
+  f.r2hi = r2 * (1 + 2e-5f);
   double r = a.rad * (1 + 1e-9) + 1e-9;
+  f.i0 = max(0, min(gd.nx - 1, (int)floor((f.cx - r - gd.x0) / gd.cell)));
+  f.i1 = max(0, min(gd.nx - 1, (int)floor((f.cx + r - gd.x0) / gd.cell)));
+  f.j0 = max(0, min(gd.ny - 1, (int)floor((f.cy - r - gd.y0) / gd.cell)));
+  f.j1 = max(0, min(gd.ny - 1, (int)floor((f.cy + r - gd.y0) / gd.cell)));
+  return f;
+}
+
+/* Membership of one grid point: FP32 distance in a frame centred on the
+ * cylinder decides everything outside a +-2e-5 band around the radius; the
+ * band and points outside the root cube use the exact double test. */
+__device__ __forceinline__ bool cylMember(const TileArgs &a, const GridDev &gd, const TileFrame &f, uint32_t gp,
+                                          int32_t qx, int32_t qy)
+{
+  if (gp & 0x80000000u)
+    return cylExact(a, gd, f.cx, f.cy, gp, qx, qy);
+  float dx = ((float)((int64_t)qx - f.qx0) - f.fx) * f.sx;
+  float dy = ((float)((int64_t)qy - f.qy0) - f.fy) * f.sy;
+  float d2 = dx * dx + dy * dy;
+  if (d2 < f.r2lo)
+    return true;
+  if (d2 > f.r2hi)
+    return false;
+  return cylExact(a, gd, f.cx, f.cy, gp, qx, qy);
+}
+
+__device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const GridDev &gd, uint64_t c, double cx, double cy)
+{
+  double x0 = dec(a, 0, gd.cellBox[c]), x1 = dec(a, 0, gd.cellBox[3 * gd.ncell + c]);
+  double y0 = dec(a, 1, gd.cellBox[gd.ncell + c]), y1 = dec(a, 1, gd.cellBox[4 * gd.ncell + c]);
+  double dx = cx < x0 ? x0 - cx : (cx > x1 ? cx - x1 : 0.0);
+  double dy = cy < y0 ? y0 - cy : (cy > y1 ? cy - y1 : 0.0);
+  double r = a.rad * (1 + 1e-6) + 1e-6;
   return dx * dx + dy * dy <= r * r;
 }
 
-/* Walks the tile's cylinder; mode 0 counts, mode 1 writes store positions
- * and owner.  One warp per tile. */
-template <int MODE>
-__global__ void __launch_bounds__(32 * kTileWarps) cylGather(TileArgs a, uint32_t *__restrict__ tileN,
-                                                             const uint32_t *__restrict__ tileStart,
-                                                             uint32_t *__restrict__ tilePts,
-                                                             int32_t *__restrict__ owner)
+/* Pass 1: one warp per tile counts the tile's points. */
+__global__ void __launch_bounds__(32 * kTileWarps) gridCount(TileArgs a, GridDev gd, uint32_t *__restrict__ tileN)
 {
-  __shared__ int32_t stack[kTileWarps][kStack];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
   if (k >= a.T)
     return;
-  double cx, cy;
-  tileCenter(a, k, cx, cy);
-  const unsigned lt = (1u << lane) - 1;
+  TileFrame f = tileFrame(a, gd, k);
   uint32_t found = 0;
-  uint32_t base = MODE ? tileStart[k] : 0;
-  int sp = 0;
-  if (lane == 0)
-    stack[w][0] = 0;
-  sp = 1;
-  __syncwarp();
-  if (a.N == 0)
-    sp = 0;
-  while (sp > 0)
-  {
-    int32_t code = stack[w][sp - 1];
-    sp--;
-    __syncwarp();
-    if (code >= 0)
+  for (int j = f.j0; j <= f.j1; j++)
+    for (int i = f.i0; i <= f.i1; i++)
     {
-      // internal node: test its 8 children, push the ones that meet (reverse order)
-      int32_t ch = -1;
-      bool meet = false;
-      if (lane < 8)
-      {
-        ch = a.child[(uint64_t)code * 8 + lane];
-        if (ch >= 0)
-          meet = boxMeetsCyl(a, a.nodeBox, a.N, (uint64_t)ch, cx, cy);
-        else if (ch <= -2)
-          meet = boxMeetsCyl(a, a.leafBox, a.L, (uint64_t)(-2 - ch), cx, cy);
-      }
-      unsigned m = __ballot_sync(0xffffffffu, meet);
-      int cnt = __popc(m);
-      if (meet)
-      {
-        int above = __popc(m >> (lane + 1));   // children after me go deeper in the stack
-        stack[w][sp + above] = ch;
-      }
-      sp += cnt;
-      __syncwarp();
-    }
-    else
-    {
-      uint64_t l = (uint64_t)(-2 - code);
-      uint32_t f = a.leafFirst[l], cntL = a.leafCount[l];
-      // OctStore::pointsIn semantics: the block's cube must meet the
-      // cylinder; when its four vertical edges are inside, every point counts.
-      double lx, ly, lz, ls;
-      wb_leaf_cube(a.leafKey[l], a.leafLev[l], a.rootLo, a.rootSide, lx, ly, lz, ls);
-      bool ct = false;
-      if (lane == 0)
-        ct = wb_hypot(cx - wb_clamp_toward(cx, lx, ls), cy - wb_clamp_toward(cy, ly, ls)) <= a.rad;
-      else if (lane <= 4)
-      {
-        int n = lane - 1;
-        ct = wb_hypot(cx - ((n & 1) ? lx + ls / 2 : lx - ls / 2), cy - ((n & 2) ? ly + ls / 2 : ly - ls / 2)) <= a.rad;
-      }
-      unsigned cb = __ballot_sync(0xffffffffu, ct);
-      if (!(cb & 1))
+      uint64_t c = (uint64_t)j * gd.nx + i;
+      uint32_t b = gd.cellStart[c], e = gd.cellStart[c + 1];
+      if (b == e || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
         continue;
-      const bool allIn = (cb & 0x1eu) == 0x1eu;
-      for (uint32_t t0 = 0; t0 < cntL; t0 += 32)
+      for (uint32_t t0 = b; t0 < e; t0 += 32)
       {
         uint32_t t = t0 + lane;
-        bool in = false;
-        if (t < cntL)
-        {
-          uint32_t j = f + t;
-          double px = dec(a, 0, a.sx[j]), py = dec(a, 1, a.sy[j]);
-          in = allIn || wb_hypot(cx - px, cy - py) <= a.rad;
-        }
-        unsigned m = __ballot_sync(0xffffffffu, in);
-        if (MODE && in)
-        {
-          uint32_t j = f + t;
-          tilePts[base + found + __popc(m & lt)] = j;
-          atomicMax(&owner[j], (int32_t)k);
-        }
-        found += __popc(m);
+        bool in = t < e && cylMember(a, gd, f, gd.gpos[t], gd.gx[t], gd.gy[t]);
+        found += __popc(__ballot_sync(0xffffffffu, in));
       }
     }
-  }
-  if (!MODE && lane == 0)
+  if (lane == 0)
     tileN[k] = found;
+}
+
+constexpr int kFillThreads = 256;
+constexpr int kFillMax = 4096;
+
+/* Pass 2: one block per tile gathers the tile's store positions, sorts them
+ * (= OctStore::pointsIn order) and records the owner tile of each point. */
+__global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd, const uint32_t *__restrict__ tileStart,
+                                                         uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
+                                                         int *__restrict__ overflow)
+{
+  __shared__ uint32_t buf[kFillMax];
+  __shared__ uint32_t cnt;
+  uint64_t k = blockIdx.x;
+  if (k >= a.T)
+    return;
+  uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
+  if (M == 0)
+    return;
+  if (M > kFillMax)
+  {
+    if (threadIdx.x == 0)
+      atomicExch(overflow, 1);
+    return;
+  }
+  if (threadIdx.x == 0)
+    cnt = 0;
+  __syncthreads();
+  TileFrame f = tileFrame(a, gd, k);
+  for (int j = f.j0; j <= f.j1; j++)
+    for (int i = f.i0; i <= f.i1; i++)
+    {
+      uint64_t c = (uint64_t)j * gd.nx + i;
+      uint32_t b = gd.cellStart[c], e = gd.cellStart[c + 1];
+      if (b == e || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
+        continue;
+      for (uint32_t t = b + threadIdx.x; t < e; t += kFillThreads)
+      {
+        uint32_t gp = gd.gpos[t];
+        if (cylMember(a, gd, f, gp, gd.gx[t], gd.gy[t]))
+        {
+          uint32_t slot = atomicAdd(&cnt, 1u);
+          if (slot < kFillMax)
+            buf[slot] = gp & 0x7fffffffu;
+        }
+      }
+    }
+  __syncthreads();
+  int P = 1;
+  while (P < (int)M)
+    P <<= 1;
+  for (int t = threadIdx.x + M; t < P; t += kFillThreads)
+    buf[t] = 0xffffffffu;
+  __syncthreads();
+  for (int kk = 2; kk <= P; kk <<= 1)
+    for (int jj = kk >> 1; jj > 0; jj >>= 1)
+    {
+      for (int t = threadIdx.x; t < P; t += kFillThreads)
+      {
+        int u = t ^ jj;
+        if (u > t)
+        {
+          bool up = (t & kk) == 0;
+          uint32_t x = buf[t], y = buf[u];
+          if ((x > y) == up)
+          {
+            buf[t] = y;
+            buf[u] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (uint32_t t = threadIdx.x; t < M; t += kFillThreads)
+  {
+    uint32_t j = buf[t];
+    tilePts[base + t] = j;
+    atomicMax(&owner[j], (int32_t)k);
+  }
 }
 
 /* ---- scanCylinder ---- */
@@ -683,10 +770,23 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
       (rc = wb_ensure(c, c->tileH, T * 8 + 64)) || (rc = wb_ensure(c, c->small, 4096)))
     return rc;
   TileArgs a = tileArgs(c);
+  GridDev gd;
+  gd.x0 = c->grid.x0;
+  gd.y0 = c->grid.y0;
+  gd.cell = c->grid.cell;
+  gd.nx = c->grid.nx;
+  gd.ny = c->grid.ny;
+  gd.ncell = c->grid.ncell;
+  gd.cellStart = (const uint32_t *)c->cellStart.p;
+  gd.cellBox = (const int32_t *)c->cellBox.p;
+  gd.gx = (const int32_t *)c->gx.p;
+  gd.gy = (const int32_t *)c->gy.p;
+  gd.gpos = (const uint32_t *)c->gpos.p;
+  gd.leafId = (const uint32_t *)c->leafId.p;
   uint32_t *tileN = (uint32_t *)c->tileN.p, *tileStart = (uint32_t *)c->tileStart.p;
   int32_t *owner = (int32_t *)c->owner.p;
   unsigned blocks = (unsigned)((T + kTileWarps - 1) / kTileWarps);
-  { cylGather<0><<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, tileN, nullptr, nullptr, nullptr); ++c->launches; }
+  { gridCount<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileN); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
   if ((rc = wb_exclusive_scan_u32(c, tileN, tileStart, T, dTot)))
@@ -699,8 +799,15 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   if ((rc = wb_ensure(c, c->tilePts, (uint64_t)M * 4 + 64)))
     return rc;
   { fillOwner<<<(unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(owner, nd); ++c->launches; }
-  { cylGather<1><<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, nullptr, tileStart, (uint32_t *)c->tilePts.p, owner); ++c->launches; }
+  int *dOvf = (int *)((char *)c->small.p + 384);
+  WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 4, c->stream));
+  { gridFill<<<(unsigned)T, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner, dOvf); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
+  int ovf = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&ovf, dOvf, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (ovf)
+    return wb_fail(c, WB_EINVAL, "wb_scan_tiles: a tile cylinder holds more than 4096 points; use a smaller tile_size");
   wb_mark(c, "tile_gather");
   ScanArgs s;
   s.t = a;

@@ -93,14 +93,50 @@ def _uniform_outside(rng, n, x0, y0, sx, sy, boxes):
     return np.concatenate(xs), np.concatenate(ys)
 
 
+def _vegetation_xy(rng, n, x0, y0, sx, sy, boxes, cover):
+    """Plan positions of vegetation points: uniform inside copses (discs of
+    radius 4-12 m, shrunk on small tiles) that together cover about ``cover``
+    of the tile, outside building footprints.  cover=None spreads them over
+    the whole tile."""
+    if cover is None:
+        return _uniform_outside(rng, n, x0, y0, sx, sy, boxes)
+    rmax = min(12.0, 0.2 * min(sx, sy))
+    rmin = min(4.0, 0.5 * rmax)
+    discs = []
+    area = 0.0
+    while area < cover * sx * sy:
+        r = rng.uniform(rmin, rmax)
+        discs.append((x0 + rng.random() * sx, y0 + rng.random() * sy, r))
+        area += math.pi * r * r
+    d = np.array(discs)
+    w = d[:, 2] ** 2
+    xs, ys = [], []
+    need = n
+    while need > 0:
+        m = int(need * 1.3) + 64
+        k = rng.choice(len(d), size=m, p=w / w.sum())
+        rr = d[k, 2] * np.sqrt(rng.random(m))
+        th = rng.random(m) * 2 * math.pi
+        x = d[k, 0] + rr * np.cos(th)
+        y = d[k, 1] + rr * np.sin(th)
+        keep = (x >= x0) & (x < x0 + sx) & (y >= y0) & (y < y0 + sy) & ~_in_boxes(x, y, boxes)
+        x, y = x[keep][:need], y[keep][:need]
+        xs.append(x)
+        ys.append(y)
+        need -= x.size
+    return np.concatenate(xs), np.concatenate(ys)
+
+
 def terrain_cloud(n, size_x, size_y, seed, *, scale=(0.001, 0.001, 0.001), offset=(0.0, 0.0, 0.0),
                   nonground=0.2, amp=(0.5, 2.0), wavelen=(20.0, 80.0), noise=0.02,
-                  max_slope=None, steps=0.0, origin=(0.0, 0.0), unit=1.0, shuffle=True) -> Cloud:
+                  max_slope=None, steps=0.0, origin=(0.0, 0.0), unit=1.0, shuffle=True,
+                  veg_cover=0.15) -> Cloud:
     """One tile: ground sinusoids + noise, box buildings (3-15 m) and vegetation (0.5-10 m).
 
     Half of the nonground points lie on building roofs and walls (uniform by
-    area), half are vegetation uniform in plan and 0.5-10 m above ground.
-    Points are shuffled into a random order unless ``shuffle`` is false.
+    area), half are vegetation 0.5-10 m above ground inside copses covering
+    ``veg_cover`` of the tile (None: spread over the whole tile).  Points are
+    shuffled into a random order unless ``shuffle`` is false.
     """
     rng = np.random.default_rng(seed)
     params = _terrain_params(rng, amp, wavelen, max_slope)
@@ -131,7 +167,7 @@ def terrain_cloud(n, size_x, size_y, seed, *, scale=(0.001, 0.001, 0.001), offse
     gx, gy = _uniform_outside(rng, n_gnd, x0, y0, size_x, size_y, boxes)
     gz = g(gx, gy) + rng.normal(0.0, noise, n_gnd)
 
-    vx, vy = _uniform_outside(rng, n_veg, x0, y0, size_x, size_y, boxes)
+    vx, vy = _vegetation_xy(rng, n_veg, x0, y0, size_x, size_y, boxes, veg_cover)
     vz = g(vx, vy) + rng.uniform(0.5, 10.0, n_veg)
 
     bx = np.empty(n_box)
