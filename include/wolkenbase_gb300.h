@@ -120,6 +120,24 @@ int wb_octree_store_order(wb_ctx *ctx, uint32_t *input_index);
  * leaf index, or -1 where findBlock would return -1. */
 int wb_octree_find_block(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *leaf);
 
+/* wb_octree_find_block without any device allocation (no counterpart in the
+ * reference).  Some callers of this library cannot afford cudaMalloc/cudaFree
+ * on the query path: cudaFree waits for the whole device, so a serving loop
+ * that answers point lookups between classification jobs would stall every
+ * job in flight, and a process running close to its HBM budget (many clouds
+ * resident) may have no room left for even a small staging allocation.  This
+ * entry point stages positions and results in a file-scope device array of
+ * WB_FIND_BLOCK_STATIC_MAX entries that every GPU loading the library keeps
+ * until the process exits (about 2 MB per GPU).  Its first call on a device
+ * looks the array's address up (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  m above WB_FIND_BLOCK_STATIC_MAX is rejected
+ * with WB_EINVAL.  All calls share the one array: calls that overlap on the
+ * GPU (two host threads, or two contexts on one device) race and must be
+ * serialised by the caller.  Every result slot is written by each call, so
+ * nothing left over from an earlier call is read.  Synchronous. */
+#define WB_FIND_BLOCK_STATIC_MAX 65536
+int wb_octree_find_block_static(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *leaf);
+
 /* scanCylinder over every tile then postscanCylinder over every tile
  * (scan.cpp:31-179), in flowsnake order. */
 int wb_scan_tiles(wb_ctx *ctx, const wb_params *params);

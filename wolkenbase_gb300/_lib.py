@@ -53,6 +53,7 @@ SIGNATURES = {
     "wb_octree_point_leaf": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wb_octree_store_order": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wb_octree_find_block": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_octree_find_block_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_scan_tiles": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
     "wb_tiles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wb_classify": (C.c_int, [C.c_void_p, C.POINTER(wb_params), C.c_void_p, C.c_int]),

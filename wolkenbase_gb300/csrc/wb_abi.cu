@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -462,6 +463,76 @@ __global__ void findBlockKernel(const double *__restrict__ xyz, uint64_t m, WbRo
   }
 }
 }  // namespace
+
+/* ---- findBlock with static staging: no allocation on the call path ----
+ * The staging lives in file-scope device arrays.  Host code must not pass the
+ * array names to a kernel (on the host they are only stand-ins); the device
+ * addresses are looked up once per device with cudaGetSymbolAddress. */
+static __device__ __align__(256) double gFindStaticIn[3 * WB_FIND_BLOCK_STATIC_MAX];
+static __device__ __align__(256) int64_t gFindStaticOut[WB_FIND_BLOCK_STATIC_MAX];
+
+namespace
+{
+struct StaticSlots
+{
+  double *in = nullptr;
+  int64_t *out = nullptr;
+};
+std::mutex gStaticMutex;
+StaticSlots gStaticByDevice[64];
+}  // namespace
+
+static int staticSlots(wb_ctx *c, StaticSlots &s)
+{
+  if (c->device < 0 || c->device >= 64)
+    return wb_fail(c, WB_EINVAL, "wb_octree_find_block_static: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(gStaticMutex);
+  StaticSlots &d = gStaticByDevice[c->device];
+  if (!d.in)
+  {
+    void *pin = nullptr, *pout = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&pin, gFindStaticIn);
+    if (e != cudaSuccess)
+      return wb_fail(c, WB_ECUDA, std::string("cudaGetSymbolAddress(staging in): ") + cudaGetErrorString(e));
+    e = cudaGetSymbolAddress(&pout, gFindStaticOut);
+    if (e != cudaSuccess)
+      return wb_fail(c, WB_ECUDA, std::string("cudaGetSymbolAddress(staging out): ") + cudaGetErrorString(e));
+    d.in = (double *)pin;
+    d.out = (int64_t *)pout;
+  }
+  s = d;
+  return 0;
+}
+
+extern "C" int wb_octree_find_block_static(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
+{
+  if (!c || (m && (!xyz || !leaf)))
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_octree_find_block_static: no octree built");
+  if (m > WB_FIND_BLOCK_STATIC_MAX)
+    return wb_fail(c, WB_EINVAL, "wb_octree_find_block_static: " + std::to_string(m) + " positions exceed the " +
+                                     std::to_string(WB_FIND_BLOCK_STATIC_MAX) + "-entry static staging array");
+  if (m == 0)
+    return 0;
+  cudaSetDevice(c->device);
+  StaticSlots s;
+  int rc = staticSlots(c, s);
+  if (rc)
+    return rc;
+  WbRoot r;
+  for (int k = 0; k < 3; k++)
+    r.lo[k] = c->g.root_lo[k];
+  r.side = c->g.root_side;
+  r.cell = c->g.cell;
+  WB_CUDA(c, cudaMemcpyAsync(s.in, xyz, m * 24, cudaMemcpyHostToDevice, c->stream));
+  { findBlockKernel<<<(unsigned)std::min<uint64_t>((m + 255) / 256, 4096), 256, 0, c->stream>>>(
+        s.in, m, r, (const uint64_t *)c->leafKey.p, (const uint8_t *)c->leafLevel.p, c->n_leaves, s.out); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  WB_CUDA(c, cudaMemcpyAsync(leaf, s.out, m * 8, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
 
 int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
 {
