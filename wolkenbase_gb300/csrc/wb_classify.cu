@@ -67,8 +67,10 @@ struct ClsArgs
   const int32_t *cellBox;
   const int32_t *gx, *gy, *gz;
   const uint32_t *gpos;
+  int snx, sny;
+  const int32_t *superBox;
   double zmin;
-  int exactInts;
+  int exactInts;   /* decode strictly increasing and 32-bit record differences exact */
   /* ambiguous points for the exact pass */
   uint32_t *ambList;
   uint32_t *ambCount;
@@ -113,13 +115,17 @@ __device__ bool memberExact(const ClsArgs &a, const Hyp &h, uint32_t gp, int32_t
   return all || in;
 }
 
-/* Can any point of column c be inside?  FP32 with generous slack. */
-__device__ __forceinline__ bool cellMeets(const ClsArgs &a, const Hyp &h, uint64_t c)
+/* Can any point of a box (integer bounds, 6 planes of N entries) be inside?
+ * FP32 with generous slack.  Record differences are exact in 32 bits: the
+ * host checks that the cloud's integer extent fits. */
+__device__ __forceinline__ bool boxMeets(const Hyp &h, const int32_t *box, uint64_t N, uint64_t c)
 {
-  const uint64_t N = a.ncell;
-  float xl = (float)((int64_t)a.cellBox[c] - h.qx) * h.sx, xh = (float)((int64_t)a.cellBox[3 * N + c] - h.qx) * h.sx;
-  float yl = (float)((int64_t)a.cellBox[N + c] - h.qy) * h.sy, yh = (float)((int64_t)a.cellBox[4 * N + c] - h.qy) * h.sy;
-  float zd = (float)((int64_t)h.qz - a.cellBox[2 * N + c]) * h.sz + h.czp;
+  int32_t bx0 = box[c];
+  if (bx0 == INT32_MAX)
+    return false;   // empty block
+  float xl = (float)(bx0 - h.qx) * h.sx, xh = (float)(box[3 * N + c] - h.qx) * h.sx;
+  float yl = (float)(box[N + c] - h.qy) * h.sy, yh = (float)(box[4 * N + c] - h.qy) * h.sy;
+  float zd = (float)(h.qz - box[2 * N + c]) * h.sz + h.czp;
   float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
   float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
   float r2 = h.s2 * (dx * dx + dy * dy);
@@ -239,7 +245,71 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
   int kmax = (int)ceil(reach / a.cell) + 1;
   bool surrounded = false, ambiguous = false;
   const bool fast = !EXACT && a.exactInts;
-  for (int ring = 0; ring <= kmax && !surrounded; ring++)
+  // Adds the directions of column c's points that are inside; returns whether any was.
+  auto column = [&](uint64_t cc) -> bool {
+    bool got = false;
+    uint32_t b = a.cellStart[cc], e = a.cellStart[cc + 1];
+    for (uint32_t t = b + lane; t < e; t += 32)
+    {
+      int32_t qx = a.gx[t], qy = a.gy[t], qz = a.gz[t];
+      uint32_t gp = a.gpos[t];
+      uint32_t u;
+      if (fast)
+      {
+        int32_t dxi = qx - h.qx, dyi = qy - h.qy;
+        if (dxi == 0 && dyi == 0)
+          continue;   // dist(p,q) == 0: no direction (classify.cpp:142,153)
+        bool in;
+        float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
+        if (gp & kStray)
+          in = memberExact(a, h, gp, qx, qy, qz);
+        else
+        {
+          float dzm = (float)(h.qz - qz) * h.sz;
+          float zd = dzm + h.czp;
+          float r2 = h.s2 * (dx * dx + dy * dy);
+          float f = zd * zd - r2 - h.por2f;
+          float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
+          float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
+          if (zd > ztol && f > tol)
+            in = true;
+          else if (zd < -ztol || f < -tol)
+            in = false;
+          else
+            in = memberExact(a, h, gp, qx, qy, qz);
+        }
+        if (!in)
+          continue;
+        float th = atan2f(dy, dx);
+        int d = __float2int_rn(th * 341782637.79f);   // 2^30 / pi
+        u = (uint32_t)d & 0x7fffffffu;
+      }
+      else
+      {
+        double x = decA(a, 0, qx), y = decA(a, 1, qy);
+        if (wb_hypot(h.px - x, h.py - y) == 0)
+          continue;
+        if (!memberExact(a, h, gp, qx, qy, qz))
+          continue;
+        int d = wb_atan2i(y - h.py, x - h.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
+        u = (uint32_t)d & 0x7fffffffu;
+      }
+      atomicMin(&bmin[w][u >> 25], u);
+      atomicMax(&bmax[w][u >> 25], u);
+      got = true;
+    }
+    return got;
+  };
+  auto decide = [&]() {
+    __syncwarp();
+    int nocc;
+    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
+    if (nocc >= 2)
+      surrounded = (EXACT || !fast) ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+  };
+  // Near field: rings of single columns around the point's column.
+  const int kNear = 2;
+  for (int ring = 0; ring <= kNear && ring <= kmax && !surrounded; ring++)
   {
     if (ci + ring < 0 || ci - ring >= a.nx || cj + ring < 0 || cj - ring >= a.ny)
       continue;
@@ -258,7 +328,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
         if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
           c = (uint64_t)jj * a.nx + i;
-          ok = a.cellStart[c] != a.cellStart[c + 1] && cellMeets(a, h, c);
+          ok = a.cellStart[c] != a.cellStart[c + 1] && boxMeets(h, a.cellBox, a.ncell, c);
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
@@ -266,74 +336,68 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
       {
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        uint64_t cc = __shfl_sync(0xffffffffu, c, src);
-        uint32_t b = a.cellStart[cc], e = a.cellStart[cc + 1];
-        for (uint32_t t0 = b; t0 < e; t0 += 32)
+        gotAny |= column(__shfl_sync(0xffffffffu, c, src));
+      }
+    }
+    if (__any_sync(0xffffffffu, gotAny))
+      decide();
+  }
+  // Far field: rings of super-cells (WB_SUPER x WB_SUPER columns) pruned as a
+  // block; columns already visited in the near field are skipped.
+  const int S = WB_SUPER;
+  int si = ci >= 0 ? ci / S : -((-ci + S - 1) / S), sj = cj >= 0 ? cj / S : -((-cj + S - 1) / S);
+  int smax = (int)ceil(reach / (S * a.cell)) + 1;
+  const uint64_t NS = (uint64_t)a.snx * a.sny;
+  for (int sr = 0; sr <= smax && !surrounded && kmax > kNear; sr++)
+  {
+    if (si + sr < 0 || si - sr >= a.snx || sj + sr < 0 || sj - sr >= a.sny)
+      continue;
+    int nsc = sr == 0 ? 1 : 8 * sr;
+    bool gotAny = false;
+    for (int m0 = 0; m0 < nsc; m0 += 32)
+    {
+      int m = m0 + lane;
+      int SI = 0, SJ = 0;
+      bool ok = false;
+      if (m < nsc)
+      {
+        int di, dj;
+        ringCell(sr, m, di, dj);
+        SI = si + di;
+        SJ = sj + dj;
+        if (SI >= 0 && SI < a.snx && SJ >= 0 && SJ < a.sny)
+          ok = boxMeets(h, a.superBox, NS, (uint64_t)SJ * a.snx + SI);
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, ok);
+      while (mask)
+      {
+        int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        int bi = __shfl_sync(0xffffffffu, SI, src) * S, bj = __shfl_sync(0xffffffffu, SJ, src) * S;
+        // lanes 0..S*S-1 take the block's columns
+        uint64_t c = 0;
+        bool cok = false;
+        if (lane < S * S)
         {
-          uint32_t t = t0 + lane;
-          if (t >= e)
-            continue;
-          int32_t qx = a.gx[t], qy = a.gy[t], qz = a.gz[t];
-          uint32_t gp = a.gpos[t];
-          int64_t dxi = (int64_t)qx - h.qx, dyi = (int64_t)qy - h.qy;
-          uint32_t u;
-          if (fast)
+          int i = bi + lane % S, jj = bj + lane / S;
+          int cheb = max(abs(i - ci), abs(jj - cj));
+          if (i < a.nx && jj < a.ny && cheb > kNear)
           {
-            if (dxi == 0 && dyi == 0)
-              continue;   // dist(p,q) == 0: no direction (classify.cpp:142,153)
-            bool in;
-            float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
-            if (gp & kStray)
-              in = memberExact(a, h, gp, qx, qy, qz);
-            else
-            {
-              float dzm = (float)((int64_t)h.qz - qz) * h.sz;
-              float zd = dzm + h.czp;
-              float r2 = h.s2 * (dx * dx + dy * dy);
-              float f = zd * zd - r2 - h.por2f;
-              float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
-              float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
-              if (zd > ztol && f > tol)
-                in = true;
-              else if (zd < -ztol || f < -tol)
-                in = false;
-              else
-                in = memberExact(a, h, gp, qx, qy, qz);
-            }
-            if (!in)
-              continue;
-            float th = atan2f(dy, dx);
-            int d = __float2int_rn(th * 341782637.79f);   // 2^30 / pi
-            u = (uint32_t)d & 0x7fffffffu;
+            c = (uint64_t)jj * a.nx + i;
+            cok = a.cellStart[c] != a.cellStart[c + 1] && boxMeets(h, a.cellBox, a.ncell, c);
           }
-          else
-          {
-            double x = decA(a, 0, qx), y = decA(a, 1, qy);
-            if (wb_hypot(h.px - x, h.py - y) == 0)
-              continue;
-            if (!memberExact(a, h, gp, qx, qy, qz))
-              continue;
-            int d = wb_atan2i(y - h.py, x - h.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
-            u = (uint32_t)d & 0x7fffffffu;
-          }
-          atomicMin(&bmin[w][u >> 25], u);
-          atomicMax(&bmax[w][u >> 25], u);
-          gotAny = true;
+        }
+        unsigned cm = __ballot_sync(0xffffffffu, cok);
+        while (cm)
+        {
+          int cs = __ffs(cm) - 1;
+          cm &= cm - 1;
+          gotAny |= column(__shfl_sync(0xffffffffu, c, cs));
         }
       }
     }
-    if (!__any_sync(0xffffffffu, gotAny))
-      continue;
-    __syncwarp();
-    int nocc;
-    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
-    if (nocc >= 2)
-    {
-      if (EXACT || !fast)
-        surrounded = gap < (uint32_t)WB_DEG144;
-      else
-        surrounded = gap + 2 * kMargin < (uint32_t)WB_DEG144;
-    }
+    if (__any_sync(0xffffffffu, gotAny))
+      decide();
   }
   if (!surrounded && fast)
   {
@@ -455,8 +519,14 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   a.gy = (const int32_t *)c->gy.p;
   a.gz = (const int32_t *)c->gz.p;
   a.gpos = (const uint32_t *)c->gpos.p;
+  a.snx = c->grid.snx;
+  a.sny = c->grid.sny;
+  a.superBox = (const int32_t *)c->superBox.p;
   a.zmin = (g.off[2] + g.scale[2] * (double)c->grid.zminInt) * g.unit;
-  a.exactInts = decodeIsExact(g, mn, mx) ? 1 : 0;
+  bool fits32 = true;
+  for (int k = 0; k < 3; k++)
+    fits32 = fits32 && (int64_t)c->grid.imax[k] - (int64_t)c->grid.imin[k] < ((int64_t)1 << 30);
+  a.exactInts = (decodeIsExact(g, mn, mx) && fits32) ? 1 : 0;
   a.ambList = (uint32_t *)c->ambiguous.p;
   a.ambCount = (uint32_t *)((char *)c->small.p + 448);
   a.work = nullptr;

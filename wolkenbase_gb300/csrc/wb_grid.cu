@@ -113,15 +113,65 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
   }
 }
 
-__global__ void zminKernel(uint64_t nd, const int32_t *__restrict__ sz, int *__restrict__ out)
+/* Record-integer extent of the cloud: out[0..2] minima, out[3..5] maxima. */
+__global__ void extentKernel(uint64_t nd, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
+                             const int32_t *__restrict__ sz, int *__restrict__ out)
 {
-  int m = INT32_MAX;
+  int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
-    m = min(m, sz[j]);
-  for (int o = 16; o; o >>= 1)
-    m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+  {
+    int q[3] = {sx[j], sy[j], sz[j]};
+    for (int a = 0; a < 3; a++)
+    {
+      mn[a] = min(mn[a], q[a]);
+      mx[a] = max(mx[a], q[a]);
+    }
+  }
+  for (int a = 0; a < 3; a++)
+    for (int o = 16; o; o >>= 1)
+    {
+      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
   if ((threadIdx.x & 31) == 0)
-    atomicMin(out, m);
+    for (int a = 0; a < 3; a++)
+    {
+      atomicMin(&out[a], mn[a]);
+      atomicMax(&out[3 + a], mx[a]);
+    }
+}
+
+/* Bounds of each block of WB_SUPER x WB_SUPER columns (same layout as the
+ * column bounds: 6 planes of snx*sny int32). */
+__global__ void superKernel(int nx, int ny, int snx, int sny, uint64_t ncell, const uint32_t *__restrict__ start,
+                            const int32_t *__restrict__ box, int32_t *__restrict__ sbox)
+{
+  uint64_t ns = (uint64_t)snx * sny;
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int si = (int)(s % snx), sj = (int)(s / snx);
+    int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    for (int dj = 0; dj < WB_SUPER; dj++)
+      for (int di = 0; di < WB_SUPER; di++)
+      {
+        int i = si * WB_SUPER + di, j = sj * WB_SUPER + dj;
+        if (i >= nx || j >= ny)
+          continue;
+        uint64_t c = (uint64_t)j * nx + i;
+        if (start[c] == start[c + 1])
+          continue;
+        for (int a = 0; a < 3; a++)
+        {
+          mn[a] = min(mn[a], box[(uint64_t)a * ncell + c]);
+          mx[a] = max(mx[a], box[(uint64_t)(3 + a) * ncell + c]);
+        }
+      }
+    for (int a = 0; a < 3; a++)
+    {
+      sbox[(uint64_t)a * ns + s] = mn[a];
+      sbox[(uint64_t)(3 + a) * ns + s] = mx[a];
+    }
+  }
 }
 }  // namespace
 
@@ -167,16 +217,17 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   a.nx = nx;
   a.ny = ny;
   unsigned long long *dStray = (unsigned long long *)((char *)c->small.p + 256);
-  int *dZmin = (int *)((char *)c->small.p + 320);
-  int big = INT32_MAX;
+  int *dExt = (int *)((char *)c->small.p + 512);
+  static const int kExtInit[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};
   WB_CUDA(c, cudaMemsetAsync(dStray, 0, 8, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(dZmin, &big, 4, cudaMemcpyHostToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(dExt, kExtInit, 24, cudaMemcpyHostToDevice, c->stream));
   unsigned blocks = (unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
   uint64_t *key = (uint64_t *)c->gKey0.p;
   uint32_t *val = (uint32_t *)c->gVal0.p;
   { cellKernel<<<blocks, 256, 0, c->stream>>>(a, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
                                               (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray); ++c->launches; }
-  { zminKernel<<<blocks, 256, 0, c->stream>>>(nd, (const int32_t *)c->sz.p, dZmin); ++c->launches; }
+  { extentKernel<<<blocks, 256, 0, c->stream>>>(nd, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
+                                                (const int32_t *)c->sz.p, dExt); ++c->launches; }
   int bits = 1;
   while ((1ull << bits) < ncell)
     bits++;
@@ -188,13 +239,26 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
         ncell, start, val, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p, (const int32_t *)c->sz.p,
         (const uint8_t *)c->stray.p, (int32_t *)c->gx.p, (int32_t *)c->gy.p, (int32_t *)c->gz.p,
         (uint32_t *)c->gpos.p, (int32_t *)c->cellBox.p); ++c->launches; }
+  int snx = (nx + WB_SUPER - 1) / WB_SUPER, sny = (ny + WB_SUPER - 1) / WB_SUPER;
+  c->grid.snx = snx;
+  c->grid.sny = sny;
+  uint64_t nsup = (uint64_t)snx * sny;
+  if ((rc = wb_ensure(c, c->superBox, nsup * 24 + 64)))
+    return rc;
+  { superKernel<<<(unsigned)std::min<uint64_t>((nsup + 255) / 256, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        nx, ny, snx, sny, ncell, start, (const int32_t *)c->cellBox.p, (int32_t *)c->superBox.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   unsigned long long ns = 0;
-  int zmin = 0;
+  int ext[6];
   WB_CUDA(c, cudaMemcpyAsync(&ns, dStray, 8, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(&zmin, dZmin, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(ext, dExt, 24, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   c->grid.nStray = ns;
-  c->grid.zminInt = zmin;
+  c->grid.zminInt = ext[2];
+  for (int k = 0; k < 3; k++)
+  {
+    c->grid.imin[k] = ext[k];
+    c->grid.imax[k] = ext[3 + k];
+  }
   return 0;
 }

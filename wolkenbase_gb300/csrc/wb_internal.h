@@ -33,7 +33,11 @@ struct GridInfo
   int nx = 0, ny = 0;
   uint64_t ncell = 0, nStray = 0;
   int zminInt = 0;
+  int32_t imin[3] = {0, 0, 0}, imax[3] = {0, 0, 0};   /* record-integer extent of the cloud */
+  /* super-cells: blocks of WB_SUPER x WB_SUPER columns with their own bounds */
+  int snx = 0, sny = 0;
 };
+#define WB_SUPER 4
 
 struct wb_ctx
 {
@@ -61,7 +65,7 @@ struct wb_ctx
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
   DevBuf label, clsDev, ambiguous, angleT;
-  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos;
+  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox;
   GridInfo grid;
   DevBuf flowCache;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */

@@ -36,6 +36,7 @@ struct TileArgs
   const uint8_t *leafLev;
   double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
+  int fast;   /* FP32 filter allowed: decode strictly increasing, 32-bit record differences exact */
 };
 
 __device__ __forceinline__ void tileCenter(const TileArgs &a, uint64_t k, double &x, double &y)
@@ -123,10 +124,10 @@ __device__ TileFrame tileFrame(const TileArgs &a, const GridDev &gd, uint64_t k)
 __device__ __forceinline__ bool cylMember(const TileArgs &a, const GridDev &gd, const TileFrame &f, uint32_t gp,
                                           int32_t qx, int32_t qy)
 {
-  if (gp & 0x80000000u)
+  if ((gp & 0x80000000u) || !a.fast)
     return cylExact(a, gd, f.cx, f.cy, gp, qx, qy);
-  float dx = ((float)((int64_t)qx - f.qx0) - f.fx) * f.sx;
-  float dy = ((float)((int64_t)qy - f.qy0) - f.fy) * f.sy;
+  float dx = ((float)(qx - f.qx0) - f.fx) * f.sx;
+  float dy = ((float)(qy - f.qy0) - f.fy) * f.sy;
   float d2 = dx * dx + dy * dy;
   if (d2 < f.r2lo)
     return true;
@@ -746,6 +747,19 @@ static TileArgs tileArgs(wb_ctx *c)
   for (int k = 0; k < 3; k++)
     a.rootLo[k] = g.root_lo[k];
   a.rootSide = g.root_side;
+  a.fast = 0;
+  {
+    // the centre's integer part stays within a tile of the cloud, so 32-bit
+    // differences are exact when the cloud spans less than 2^30 record units
+    bool ok = true;
+    for (int k = 0; k < 2; k++)
+    {
+      double step = fabs(g.scale[k] * g.unit);
+      ok = ok && step > 0 && (int64_t)c->grid.imax[k] - (int64_t)c->grid.imin[k] < ((int64_t)1 << 30) &&
+           (g.tile_side + 4 * g.spacing) / step < (double)(1 << 30);
+    }
+    a.fast = ok ? 1 : 0;
+  }
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;
