@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwolkenbase_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["wb_abi.cu", "wb_prims.cu", "wb_build.cu", "wb_tiles.cu", "wb_classify.cu", "wb_grid.cu", "wb_geom.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -29,7 +30,7 @@ def nvcc():
 
 def _flags(src):
     f = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
-         "-I" + CSRC]
+         "-I" + CSRC, "-I" + INCLUDE]
     if src.endswith(".cu"):
         f = ARCH + f + ["--expt-relaxed-constexpr"]
     return f
@@ -45,7 +46,7 @@ def _stale(out, deps):
 def build(verbose=False, force=False):
     os.makedirs(OBJ, exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(HERE, "..", "include", "wolkenbase_gb300.h"))
+    headers.append(os.path.join(INCLUDE, "wolkenbase_gb300.h"))
     cc = nvcc()
     jobs = []
     objs = []

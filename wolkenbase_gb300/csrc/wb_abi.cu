@@ -72,7 +72,7 @@ static void releaseBuffers(wb_ctx *c)
                    &c->tileEx, &c->tileEy, &c->tileLookup, &c->tileStart, &c->tilePts, &c->owner, &c->tileRes,
                    &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->angleT,
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
-                   &c->cellBox, &c->gx, &c->gy, &c->gz, &c->gpos, &c->superBox};
+                   &c->cellBox, &c->gx, &c->gy, &c->gz, &c->gpos, &c->superBox, &c->cellFlag, &c->ptSetup};
   for (DevBuf *b : all)
     if (b->p)
     {

@@ -17,11 +17,12 @@
  * (integer record differences times the scale); the few whose FP32 value lies
  * within 1e-5 of the boundary, and points outside the octree root cube (which
  * the reference treats through their leaf's cube), are tested exactly in
- * FP64 as the reference computes it.  Directions are FP32 atan2 values in the
- * reference's integer angle unit; 64 bins keep each bin's extremes, and the
- * largest circular gap follows from them.  With the direction error bounded
- * by kMargin units, a gap estimate below 144 degrees - 2*kMargin proves
- * "surrounded" and one above 144 degrees + 2*kMargin proves the opposite;
+ * FP64 as the reference computes it.  Directions are FP32 arctangents
+ * (wb_dir_units_f32, error below 1000 units) in the reference's integer angle
+ * unit; 64 bins keep each bin's extremes, and the largest circular gap
+ * follows from them.  With the direction error bounded by kMargin units, a
+ * gap estimate below 144 degrees - 2*kMargin proves "surrounded" and one
+ * above 144 degrees + 2*kMargin proves the opposite;
  * anything between is re-run by the exact kernel with the reference's own
  * integer atan2i (angle.cpp:117-155) and exact bins.
  *
@@ -36,14 +37,47 @@
 #include "wb_device.cuh"
 #include "angle_tables.h"
 
+/* Work counters of the classify kernel, compiled in only with
+ * -DWB_CLASSIFY_STATS (an instrumented build for tuning): per label,
+ * 0 points, 1 near columns tested, 2 super-cells tested, 3 far columns
+ * tested, 4 candidates read, 5 candidates inside, 6 surround tests,
+ * 7 columns scanned. */
+#ifdef WB_CLASSIFY_STATS
+__device__ unsigned long long gClassifyStats[3][8];
+extern "C" int wb_classify_stats(unsigned long long *out, int reset)
+{
+  if (cudaMemcpyFromSymbol(out, gClassifyStats, sizeof(gClassifyStats)) != cudaSuccess)
+    return -3;
+  if (reset)
+  {
+    unsigned long long z[24] = {0};
+    cudaMemcpyToSymbol(gClassifyStats, z, sizeof(z));
+  }
+  return 0;
+}
+#define WB_STAT(var, v) (var) += (v)
+#else
+#define WB_STAT(var, v) ((void)0)
+#endif
+
 namespace
 {
 constexpr int kWarps = 4;
 constexpr int kBins = 64;
 constexpr uint32_t kStray = 0x80000000u;
 /* bound on |FP32 direction - atan2i| in angle units (2^31 per turn); the
- * FP32 error is below 400 units, so this is a tenfold safety factor. */
+ * FP32 direction (wb_dir_units_f32) stays below 1000 units. */
 constexpr uint32_t kMargin = 4096;
+
+/* Per-point values the warp kernel needs, formed once per point by a
+ * thread-per-point kernel: double arithmetic costs 16 cycles per warp
+ * instruction on this GPU, so it is kept out of the 32-lane warp kernel. */
+struct PtSetup
+{
+  float czp, por2f;   /* cz - pz and por^2 (FP32)                         */
+  int32_t ci, cj;     /* column of the point (may lie outside the grid)   */
+  int32_t kmax, smax; /* rings of columns / super-cells the reach needs   */
+};
 
 struct ClsArgs
 {
@@ -67,10 +101,13 @@ struct ClsArgs
   const int32_t *cellBox;
   const int32_t *gx, *gy, *gz;
   const uint32_t *gpos;
+  const uint8_t *cellFlag;
   int snx, sny;
   const int32_t *superBox;
   double zmin;
   int exactInts;   /* decode strictly increasing and 32-bit record differences exact */
+  float fsx, fsy, fsz, fs2;   /* metres per record unit and slope^2, FP32 */
+  const PtSetup *setup;
   /* ambiguous points for the exact pass */
   uint32_t *ambList;
   uint32_t *ambCount;
@@ -85,18 +122,40 @@ __device__ __forceinline__ double decA(const ClsArgs &a, int ax, int32_t q)
 
 struct Hyp
 {
-  double cx, cy, cz, por2;      /* exact Hyperboloid members (centre, polar radius^2) */
-  double px, py;                /* the point, decoded                                  */
   int32_t qx, qy, qz;           /* the point, record integers                          */
   float sx, sy, sz;             /* metres per record unit                              */
   float czp, s2, por2f;         /* cz - pz, slope^2, por^2 in FP32                     */
+  uint32_t j;                   /* store position of the point                         */
 };
+
+/* The exact Hyperboloid of point j: centre and polar radius squared, as
+ * shape.cpp:119-125 forms them from p - (0,0,thickness). */
+struct HypExact
+{
+  double cx, cy, cz, por2, px, py;
+};
+
+__device__ __noinline__ HypExact exactHyp(const ClsArgs &a, uint32_t j)
+{
+  HypExact e;
+  double hs = a.tiles[a.owner[j]].h;
+  e.px = decA(a, 0, a.sx[j]);
+  e.py = decA(a, 1, a.sy[j]);
+  double pz = decA(a, 2, a.sz[j]);
+  double por = hs * (a.slope * a.slope);
+  e.por2 = por * por;
+  e.cx = e.px + 0;
+  e.cy = e.py + 0;
+  e.cz = (pz - a.thickness) + por;
+  return e;
+}
 
 /* OctStore::pointsIn membership of one candidate, exactly: Hyperboloid::in on
  * the decoded doubles; for a point outside the root cube, its leaf cube must
  * meet the hyperboloid (Octree::findBlocks) and then either all eight corners
  * are inside (the whole block is taken) or the point itself is. */
-__device__ bool memberExact(const ClsArgs &a, const Hyp &h, uint32_t gp, int32_t qx, int32_t qy, int32_t qz)
+__device__ __noinline__ bool memberExact(const ClsArgs &a, const HypExact &h, uint32_t gp, int32_t qx, int32_t qy,
+                                         int32_t qz)
 {
   double x = decA(a, 0, qx), y = decA(a, 1, qy), z = decA(a, 2, qz);
   bool in = wb_hyp_in(h.cx, h.cy, h.cz, h.por2, a.slope, x, y, z);
@@ -195,6 +254,35 @@ __device__ __forceinline__ uint32_t largestGap(const uint32_t *bmin, const uint3
   return worst;
 }
 
+/* Thread per point: the double-precision set-up of each point's query. */
+__global__ void classifySetup(ClsArgs a, PtSetup *__restrict__ out)
+{
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < a.nd; j += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int32_t k = a.owner[j];
+    if (k < 0)
+      continue;
+    double hs = a.tiles[k].h;
+    double px = decA(a, 0, a.sx[j]), py = decA(a, 1, a.sy[j]), pz = decA(a, 2, a.sz[j]);
+    double por = hs * (a.slope * a.slope);
+    double por2 = por * por;
+    double cz = (pz - a.thickness) + por;
+    PtSetup s;
+    s.czp = (float)(cz - pz);
+    s.por2f = (float)por2;
+    // horizontal reach of the hyperboloid at the lowest point of the cloud
+    double zdMax = cz - a.zmin;
+    double reach2 = (zdMax * zdMax - por2) / (a.slope * a.slope);
+    double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
+    double fi = floor((px - a.gx0) / a.cell), fj = floor((py - a.gy0) / a.cell);
+    s.ci = (int32_t)fmax(fmin(fi, 1e9), -1e9);
+    s.cj = (int32_t)fmax(fmin(fj, 1e9), -1e9);
+    s.kmax = (int32_t)fmin(ceil(reach / a.cell) + 1, 1e9);
+    s.smax = (int32_t)fmin(ceil(reach / (WB_SUPER * a.cell)) + 1, 1e9);
+    out[j] = s;
+  }
+}
+
 template <bool EXACT>
 __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
 {
@@ -215,107 +303,179 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
   h.qx = a.sx[j];
   h.qy = a.sy[j];
   h.qz = a.sz[j];
-  double hs = a.tiles[k].h;
-  h.px = decA(a, 0, h.qx);
-  h.py = decA(a, 1, h.qy);
-  double pz = decA(a, 2, h.qz);
-  // Hyperboloid(v, hs, slope), v = p - (0,0,thickness)  (shape.cpp:119-125)
-  double por = hs * (a.slope * a.slope);
-  h.por2 = por * por;
-  h.cx = h.px + 0;
-  h.cy = h.py + 0;
-  h.cz = (pz - a.thickness) + por;
-  h.sx = (float)(a.scale[0] * a.unit);
-  h.sy = (float)(a.scale[1] * a.unit);
-  h.sz = (float)(a.scale[2] * a.unit);
-  h.czp = (float)(h.cz - pz);
-  h.s2 = (float)(a.slope * a.slope);
-  h.por2f = (float)h.por2;
+  h.j = (uint32_t)j;
+  h.sx = a.fsx;
+  h.sy = a.fsy;
+  h.sz = a.fsz;
+  h.s2 = a.fs2;
+  const PtSetup ps = a.setup[j];
+  h.czp = ps.czp;
+  h.por2f = ps.por2f;
   for (int b = lane; b < kBins; b += 32)
   {
     bmin[w][b] = 0xffffffffu;
     bmax[w][b] = 0;
   }
   __syncwarp();
-  // horizontal reach of the hyperboloid at the lowest point of the cloud
-  double zdMax = h.cz - a.zmin;
-  double reach2 = (zdMax * zdMax - h.por2) / (a.slope * a.slope);
-  double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
-  int ci = (int)floor((h.px - a.gx0) / a.cell), cj = (int)floor((h.py - a.gy0) / a.cell);
-  int kmax = (int)ceil(reach / a.cell) + 1;
+  const int ci = ps.ci, cj = ps.cj, kmax = ps.kmax;
+  HypExact hx;
+  if (EXACT)
+    hx = exactHyp(a, (uint32_t)j);
   bool surrounded = false, ambiguous = false;
   const bool fast = !EXACT && a.exactInts;
-  // Adds the directions of column c's points that are inside; returns whether any was.
+  // Directions are kept as exact per-bin extremes in shared memory plus a
+  // 64-bit occupancy mask in registers (uniform across the warp).
+  uint32_t occLo = 0, occHi = 0;
+  unsigned long long stat[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  (void)stat;
+  // Adds the directions of column c's inside points; returns whether any was.
   auto column = [&](uint64_t cc) -> bool {
+    WB_STAT(stat[7], 1);
     bool got = false;
     uint32_t b = a.cellStart[cc], e = a.cellStart[cc + 1];
-    for (uint32_t t = b + lane; t < e; t += 32)
+    // Points of a column are sorted by height.  None above pz + (czp -
+    // sqrt(por^2 + s^2 d^2)) / sz, d the column's nearest distance, can be
+    // inside, so the scan stops at the first chunk past that height (with
+    // slack).  Columns holding points outside the root cube in x or y are
+    // read in full (their blocks' cubes decide for them).
+    int32_t zlim = INT32_MAX;
+    if (fast && !a.cellFlag[cc] && h.sz > 0)
     {
-      int32_t qx = a.gx[t], qy = a.gy[t], qz = a.gz[t];
-      uint32_t gp = a.gpos[t];
-      uint32_t u;
-      if (fast)
+      const uint64_t N = a.ncell;
+      float xl = (float)(a.cellBox[cc] - h.qx) * h.sx, xh = (float)(a.cellBox[3 * N + cc] - h.qx) * h.sx;
+      float yl = (float)(a.cellBox[N + cc] - h.qy) * h.sy, yh = (float)(a.cellBox[4 * N + cc] - h.qy) * h.sy;
+      float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
+      float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
+      float need = sqrtf(h.por2f + h.s2 * (dx * dx + dy * dy));
+      float dz = (h.czp - need + 1e-4f * (fabsf(h.czp) + need) + 1e-6f) / h.sz + 2.f;
+      zlim = dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
+    }
+    for (uint32_t t0 = b; t0 < e; t0 += 32)
+    {
+      uint32_t t = t0 + lane;
+      bool low = false;
+      int32_t qz = 0;
+      if (t < e)
       {
-        int32_t dxi = qx - h.qx, dyi = qy - h.qy;
-        if (dxi == 0 && dyi == 0)
-          continue;   // dist(p,q) == 0: no direction (classify.cpp:142,153)
-        bool in;
-        float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
-        if (gp & kStray)
-          in = memberExact(a, h, gp, qx, qy, qz);
+        qz = a.gz[t];
+        low = zlim == INT32_MAX || qz - h.qz <= zlim;
+      }
+      if (!__any_sync(0xffffffffu, low))
+        break;
+      WB_STAT(stat[4], __popc(__ballot_sync(0xffffffffu, low)));
+      bool in = false;
+      uint32_t u = 0;
+      if (low)
+      {
+        int32_t qx = a.gx[t], qy = a.gy[t];
+        uint32_t gp = a.gpos[t];
+        if (fast)
+        {
+          int32_t dxi = qx - h.qx, dyi = qy - h.qy;
+          // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
+          if (dxi != 0 || dyi != 0)
+          {
+            float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
+            if (gp & kStray)
+              in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
+            else
+            {
+              float dzm = (float)(h.qz - qz) * h.sz;
+              float zd = dzm + h.czp;
+              float r2 = h.s2 * (dx * dx + dy * dy);
+              float f = zd * zd - r2 - h.por2f;
+              float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
+              float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
+              if (zd > ztol && f > tol)
+                in = true;
+              else if (zd < -ztol || f < -tol)
+                in = false;
+              else
+                in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
+            }
+            if (in)
+              u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+          }
+        }
         else
         {
-          float dzm = (float)(h.qz - qz) * h.sz;
-          float zd = dzm + h.czp;
-          float r2 = h.s2 * (dx * dx + dy * dy);
-          float f = zd * zd - r2 - h.por2f;
-          float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
-          float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
-          if (zd > ztol && f > tol)
+          double x = decA(a, 0, qx), y = decA(a, 1, qy);
+          if (wb_hypot(hx.px - x, hx.py - y) != 0 && memberExact(a, hx, gp, qx, qy, qz))
+          {
             in = true;
-          else if (zd < -ztol || f < -tol)
-            in = false;
-          else
-            in = memberExact(a, h, gp, qx, qy, qz);
+            int d = wb_atan2i(y - hx.py, x - hx.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
+            u = (uint32_t)d & 0x7fffffffu;
+          }
         }
-        if (!in)
-          continue;
-        float th = atan2f(dy, dx);
-        int d = __float2int_rn(th * 341782637.79f);   // 2^30 / pi
-        u = (uint32_t)d & 0x7fffffffu;
+      }
+      if (!__any_sync(0xffffffffu, in))
+        continue;
+      // A chunk comes from one column, so its directions usually share one
+      // bin: then one lane merges the warp's extremes; otherwise each lane does.
+      uint32_t bin = u >> 25;
+      uint32_t lo = __reduce_min_sync(0xffffffffu, in ? u : 0xffffffffu);
+      uint32_t hi = __reduce_max_sync(0xffffffffu, in ? u : 0u);
+      if ((lo >> 25) == (hi >> 25))
+      {
+        if (lane == 0)
+        {
+          atomicMin(&bmin[w][lo >> 25], lo);
+          atomicMax(&bmax[w][lo >> 25], hi);
+        }
+        if ((lo >> 25) < 32)
+          occLo |= 1u << (lo >> 25);
+        else
+          occHi |= 1u << ((lo >> 25) - 32);
       }
       else
       {
-        double x = decA(a, 0, qx), y = decA(a, 1, qy);
-        if (wb_hypot(h.px - x, h.py - y) == 0)
-          continue;
-        if (!memberExact(a, h, gp, qx, qy, qz))
-          continue;
-        int d = wb_atan2i(y - h.py, x - h.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
-        u = (uint32_t)d & 0x7fffffffu;
+        if (in)
+        {
+          atomicMin(&bmin[w][bin], u);
+          atomicMax(&bmax[w][bin], u);
+        }
+        occLo |= __reduce_or_sync(0xffffffffu, in && bin < 32 ? 1u << bin : 0u);
+        occHi |= __reduce_or_sync(0xffffffffu, in && bin >= 32 ? 1u << (bin - 32) : 0u);
       }
-      atomicMin(&bmin[w][u >> 25], u);
-      atomicMax(&bmax[w][u >> 25], u);
+      WB_STAT(stat[5], __popc(__ballot_sync(0xffffffffu, in)));
       got = true;
     }
     return got;
   };
+  // Surround test.  A circular run of 27 empty bins (151.9 degrees) already
+  // proves a gap above 144 degrees plus both margins; only otherwise is the
+  // exact largest gap formed from the bin extremes.
   auto decide = [&]() {
+    WB_STAT(stat[6], 1);
+    uint64_t occ = ((uint64_t)occHi << 32) | occLo;
+    if (__popcll(occ) < 2)
+      return;
+    uint64_t r = ~occ;
+    r &= (r << 1) | (r >> 63);
+    r &= (r << 2) | (r >> 62);
+    r &= (r << 4) | (r >> 60);
+    r &= (r << 8) | (r >> 56);
+    r &= (r << 11) | (r >> 53);
+    if (r)
+      return;
     __syncwarp();
     int nocc;
     uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
     if (nocc >= 2)
       surrounded = (EXACT || !fast) ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
   };
-  // Near field: rings of single columns around the point's column.
+  // Near field: rings of single columns around the point's column, each ring
+  // visited in an order that alternates sides (stride 4k-1 over its 8k
+  // columns), with the surround test after every column.
   const int kNear = 2;
   for (int ring = 0; ring <= kNear && ring <= kmax && !surrounded; ring++)
   {
     if (ci + ring < 0 || ci - ring >= a.nx || cj + ring < 0 || cj - ring >= a.ny)
       continue;
     int ncells = ring == 0 ? 1 : 8 * ring;
-    bool gotAny = false;
-    for (int m0 = 0; m0 < ncells; m0 += 32)
+    int stride = ring == 0 ? 1 : 4 * ring - 1;
+    WB_STAT(stat[1], ncells);
+    for (int m0 = 0; m0 < ncells && !surrounded; m0 += 32)
     {
       int m = m0 + lane;
       uint64_t c = 0;
@@ -323,7 +483,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
       if (m < ncells)
       {
         int di, dj;
-        ringCell(ring, m, di, dj);
+        ringCell(ring, (m * stride) % ncells, di, dj);
         int i = ci + di, jj = cj + dj;
         if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
@@ -332,29 +492,28 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
-      while (mask)
+      while (mask && !surrounded)
       {
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        gotAny |= column(__shfl_sync(0xffffffffu, c, src));
+        if (column(__shfl_sync(0xffffffffu, c, src)))
+          decide();
       }
     }
-    if (__any_sync(0xffffffffu, gotAny))
-      decide();
   }
   // Far field: rings of super-cells (WB_SUPER x WB_SUPER columns) pruned as a
   // block; columns already visited in the near field are skipped.
   const int S = WB_SUPER;
   int si = ci >= 0 ? ci / S : -((-ci + S - 1) / S), sj = cj >= 0 ? cj / S : -((-cj + S - 1) / S);
-  int smax = (int)ceil(reach / (S * a.cell)) + 1;
+  const int smax = ps.smax;
   const uint64_t NS = (uint64_t)a.snx * a.sny;
   for (int sr = 0; sr <= smax && !surrounded && kmax > kNear; sr++)
   {
     if (si + sr < 0 || si - sr >= a.snx || sj + sr < 0 || sj - sr >= a.sny)
       continue;
     int nsc = sr == 0 ? 1 : 8 * sr;
-    bool gotAny = false;
-    for (int m0 = 0; m0 < nsc; m0 += 32)
+    WB_STAT(stat[2], nsc);
+    for (int m0 = 0; m0 < nsc && !surrounded; m0 += 32)
     {
       int m = m0 + lane;
       int SI = 0, SJ = 0;
@@ -369,7 +528,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
           ok = boxMeets(h, a.superBox, NS, (uint64_t)SJ * a.snx + SI);
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
-      while (mask)
+      while (mask && !surrounded)
       {
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
@@ -388,16 +547,18 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
           }
         }
         unsigned cm = __ballot_sync(0xffffffffu, cok);
+        WB_STAT(stat[3], S * S);
+        bool gotAny = false;
         while (cm)
         {
           int cs = __ffs(cm) - 1;
           cm &= cm - 1;
           gotAny |= column(__shfl_sync(0xffffffffu, c, cs));
         }
+        if (gotAny)
+          decide();
       }
     }
-    if (__any_sync(0xffffffffu, gotAny))
-      decide();
   }
   if (!surrounded && fast)
   {
@@ -406,6 +567,15 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
     uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
     ambiguous = nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
   }
+#ifdef WB_CLASSIFY_STATS
+  if (lane == 0 && !EXACT)
+  {
+    int L = surrounded ? 1 : 2;
+    atomicAdd(&gClassifyStats[L][0], 1ull);
+    for (int q = 1; q < 8; q++)
+      atomicAdd(&gClassifyStats[L][q], stat[q]);
+  }
+#endif
   if (lane == 0)
   {
     a.label[j] = surrounded ? 1 : 2;
@@ -467,7 +637,7 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   int rc;
   uint64_t nd = c->nd, n = c->n;
   if ((rc = wb_ensure(c, c->label, nd + 64)) || (rc = wb_ensure(c, c->angleT, (511 + 512 + 512) * 8)) ||
-      (rc = wb_ensure(c, c->ambiguous, nd * 4 + 64)))
+      (rc = wb_ensure(c, c->ambiguous, nd * 4 + 64)) || (rc = wb_ensure(c, c->ptSetup, nd * sizeof(PtSetup) + 64)))
     return rc;
   if (!onDevice && (rc = wb_ensure(c, c->clsDev, n + 64)))
     return rc;
@@ -519,6 +689,7 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   a.gy = (const int32_t *)c->gy.p;
   a.gz = (const int32_t *)c->gz.p;
   a.gpos = (const uint32_t *)c->gpos.p;
+  a.cellFlag = (const uint8_t *)c->cellFlag.p;
   a.snx = c->grid.snx;
   a.sny = c->grid.sny;
   a.superBox = (const int32_t *)c->superBox.p;
@@ -527,6 +698,11 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   for (int k = 0; k < 3; k++)
     fits32 = fits32 && (int64_t)c->grid.imax[k] - (int64_t)c->grid.imin[k] < ((int64_t)1 << 30);
   a.exactInts = (decodeIsExact(g, mn, mx) && fits32) ? 1 : 0;
+  a.fsx = (float)(g.scale[0] * g.unit);
+  a.fsy = (float)(g.scale[1] * g.unit);
+  a.fsz = (float)(g.scale[2] * g.unit);
+  a.fs2 = (float)(p->max_slope * p->max_slope);
+  a.setup = (const PtSetup *)c->ptSetup.p;
   a.ambList = (uint32_t *)c->ambiguous.p;
   a.ambCount = (uint32_t *)((char *)c->small.p + 448);
   a.work = nullptr;
@@ -534,6 +710,8 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 4, c->stream));
   if (nd)
   {
+    unsigned sb = (unsigned)std::min<uint64_t>((nd + 255) / 256, (uint64_t)c->sm_count * 16);
+    { classifySetup<<<sb, 256, 0, c->stream>>>(a, (PtSetup *)c->ptSetup.p); ++c->launches; }
     { classifyRings<false><<<(unsigned)((nd + kWarps - 1) / kWarps), 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
     WB_CUDA(c, cudaGetLastError());
   }

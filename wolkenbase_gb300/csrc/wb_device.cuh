@@ -232,6 +232,33 @@ __device__ __forceinline__ double wb_clamp_toward(double a, double c, double sid
   return a > c ? c + side / 2 : c - side / 2;
 }
 
+/* Direction of (dx, dy) in the reference's angle unit (2^31 per turn) in
+ * FP32, for the fast classify filter.  atan on [0,1] is an odd polynomial
+ * of degree 11 fitted here by Chebyshev-weighted least squares (maximum
+ * error 1.75e-6 rad evaluated in FP32); the octant is restored from the
+ * signs and the larger component.  With the fast division and the unit
+ * conversion the error stays below 1000 units; callers allow 4096. */
+__device__ __forceinline__ float wb_dir_units_f32(float dy, float dx)
+{
+  float ax = fabsf(dx), ay = fabsf(dy);
+  float t = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
+  float t2 = t * t;
+  float p = -0x1.800344p-7f;
+  p = __fmaf_rn(p, t2, 0x1.af4986p-5f);
+  p = __fmaf_rn(p, t2, -0x1.dce206p-4f);
+  p = __fmaf_rn(p, t2, 0x1.8c5ee6p-3f);
+  p = __fmaf_rn(p, t2, -0x1.549b14p-2f);
+  p = __fmaf_rn(p, t2, 0x1.fffd04p-1f);
+  float th = p * t;
+  if (ay > ax)
+    th = 1.57079637f - th;
+  if (dx < 0)
+    th = 3.14159274f - th;
+  if (dy < 0)
+    th = -th;
+  return th * 341782637.79f;   // 2^30 / pi
+}
+
 /* Hyperboloid::in (shape.cpp:127-135) for slope > 0, exact double form. */
 __device__ __forceinline__ bool wb_hyp_in(double cx, double cy, double cz, double por2, double slope,
                                          double qx, double qy, double qz)

@@ -9,9 +9,10 @@
  * directions a classify query collects spread around the point early and the
  * surround test can stop after a few rings.
  *
- * Cells hold store positions sorted stably (so each cell lists its points in
- * store order), a copy of the points' integer X/Y/Z in grid order for
- * coalesced reads, and per-cell integer bounds for pruning.  A point that
+ * Cells hold store positions sorted by height (so a query can stop reading a
+ * column once its points are above the hyperboloid), a copy of the points'
+ * integer X/Y/Z in grid order for coalesced reads, and per-cell integer
+ * bounds for pruning.  A point that
  * lies outside the octree root cube is flagged: the reference's queries treat
  * such points through their leaf's cube, and the kernels do the same for them.
  */
@@ -44,11 +45,12 @@ __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int
     int cx = (int)floor((x - g.x0) / g.cell), cy = (int)floor((y - g.y0) / g.cell);
     cx = min(max(cx, 0), g.nx - 1);
     cy = min(max(cy, 0), g.ny - 1);
-    key[j] = (uint64_t)cy * g.nx + cx;
+    // column in the high 32 bits, height (order-preserving int32 -> uint32) below
+    key[j] = (((uint64_t)cy * g.nx + cx) << 32) | (uint32_t)(sz[j] ^ (int32_t)0x80000000);
     val[j] = (uint32_t)j;
-    bool s = x < g.rootLo[0] || y < g.rootLo[1] || z < g.rootLo[2] || x >= g.rootHi[0] || y >= g.rootHi[1] ||
-             z >= g.rootHi[2];
-    stray[j] = s;
+    bool sxy = x < g.rootLo[0] || y < g.rootLo[1] || x >= g.rootHi[0] || y >= g.rootHi[1];
+    bool s = sxy || z < g.rootLo[2] || z >= g.rootHi[2];
+    stray[j] = (uint8_t)((s ? 1 : 0) | (sxy ? 2 : 0));
     if (s)
       atomicAdd(nStray, 1ull);
   }
@@ -59,8 +61,8 @@ __global__ void cellStartKernel(uint64_t nd, uint64_t ncell, const uint64_t *__r
 {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint64_t k = key[i];
-    uint64_t prev = i ? key[i - 1] : (uint64_t)-1;
+    uint64_t k = key[i] >> 32;
+    uint64_t prev = i ? key[i - 1] >> 32 : (uint64_t)-1;
     if (i == 0)
       for (uint64_t c = 0; c <= k; c++)
         start[c] = 0;
@@ -78,7 +80,7 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
                                const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                                const int32_t *__restrict__ sz, const uint8_t *__restrict__ stray,
                                int32_t *__restrict__ gx, int32_t *__restrict__ gy, int32_t *__restrict__ gz,
-                               uint32_t *__restrict__ gpos, int32_t *__restrict__ box)
+                               uint32_t *__restrict__ gpos, int32_t *__restrict__ box, uint8_t *__restrict__ flags)
 {
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -86,6 +88,7 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
     return;
   uint32_t b = start[c], e = start[c + 1];
   int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+  bool xyStray = false;
   for (uint32_t i = b + lane; i < e; i += 32)
   {
     uint32_t j = pos[i];
@@ -93,7 +96,9 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
     gx[i] = q[0];
     gy[i] = q[1];
     gz[i] = q[2];
-    gpos[i] = j | (stray[j] ? 0x80000000u : 0u);
+    uint8_t st = stray[j];
+    gpos[i] = j | ((st & 1) ? 0x80000000u : 0u);
+    xyStray |= (st & 2) != 0;
     for (int a = 0; a < 3; a++)
     {
       mn[a] = min(mn[a], q[a]);
@@ -111,6 +116,10 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
     int32_t v = lane < 3 ? mn[lane] : mx[lane - 3];
     box[(uint64_t)lane * ncell + c] = v;
   }
+  // a column holding a point outside the root cube in x or y is read in full
+  unsigned any = __ballot_sync(0xffffffffu, xyStray);
+  if (lane == 0)
+    flags[c] = any ? 1 : 0;
 }
 
 /* Record-integer extent of the cloud: out[0..2] minima, out[3..5] maxima. */
@@ -199,7 +208,7 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
       (rc = wb_ensure(c, c->stray, nd + 64)) || (rc = wb_ensure(c, c->cellStart, (ncell + 1) * 4 + 64)) ||
       (rc = wb_ensure(c, c->cellBox, ncell * 24 + 64)) || (rc = wb_ensure(c, c->gx, nd * 4 + 64)) ||
       (rc = wb_ensure(c, c->gy, nd * 4 + 64)) || (rc = wb_ensure(c, c->gz, nd * 4 + 64)) ||
-      (rc = wb_ensure(c, c->gpos, nd * 4 + 64)))
+      (rc = wb_ensure(c, c->gpos, nd * 4 + 64)) || (rc = wb_ensure(c, c->cellFlag, ncell + 64)))
     return rc;
   GridArgs a;
   a.nd = nd;
@@ -231,14 +240,14 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   int bits = 1;
   while ((1ull << bits) < ncell)
     bits++;
-  if ((rc = wb_radix_sort_pairs(c, key, val, (uint64_t *)c->gKey1.p, (uint32_t *)c->gVal1.p, nd, 0, bits)))
+  if ((rc = wb_radix_sort_pairs(c, key, val, (uint64_t *)c->gKey1.p, (uint32_t *)c->gVal1.p, nd, 0, 32 + bits)))
     return rc;
   uint32_t *start = (uint32_t *)c->cellStart.p;
   { cellStartKernel<<<blocks, 256, 0, c->stream>>>(nd, ncell, key, start); ++c->launches; }
   { cellFillKernel<<<(unsigned)((ncell * 32 + 255) / 256), 256, 0, c->stream>>>(
         ncell, start, val, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p, (const int32_t *)c->sz.p,
         (const uint8_t *)c->stray.p, (int32_t *)c->gx.p, (int32_t *)c->gy.p, (int32_t *)c->gz.p,
-        (uint32_t *)c->gpos.p, (int32_t *)c->cellBox.p); ++c->launches; }
+        (uint32_t *)c->gpos.p, (int32_t *)c->cellBox.p, (uint8_t *)c->cellFlag.p); ++c->launches; }
   int snx = (nx + WB_SUPER - 1) / WB_SUPER, sny = (ny + WB_SUPER - 1) / WB_SUPER;
   c->grid.snx = snx;
   c->grid.sny = sny;

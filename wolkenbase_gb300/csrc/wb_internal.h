@@ -6,7 +6,7 @@
 #include <cstdint>
 #include <string>
 #include <vector>
-#include "../../include/wolkenbase_gb300.h"
+#include "wolkenbase_gb300.h"
 
 /* Grow-only device buffer; capacity is charged against the context budget. */
 struct DevBuf
@@ -65,7 +65,7 @@ struct wb_ctx
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
   DevBuf label, clsDev, ambiguous, angleT;
-  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox;
+  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox, cellFlag, ptSetup;
   GridInfo grid;
   DevBuf flowCache;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */

@@ -176,25 +176,108 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridCount(TileArgs a, GridDev
 constexpr int kFillThreads = 256;
 constexpr int kFillMax = 4096;
 
-/* Pass 2: one block per tile gathers the tile's store positions, sorts them
- * (= OctStore::pointsIn order) and records the owner tile of each point. */
-__global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd, const uint32_t *__restrict__ tileStart,
-                                                         uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
-                                                         int *__restrict__ overflow)
+constexpr int kWarpFill = 1024;
+
+/* Pass 2: one warp per tile gathers the tile's store positions, sorts them
+ * (= OctStore::pointsIn order: leaf depth-first, then store order) with a
+ * bitonic network in shared memory, and records each point's owner tile.
+ * Tiles above kWarpFill points are listed for the block-wide version. */
+__global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, GridDev gd,
+                                                                const uint32_t *__restrict__ tileStart,
+                                                                uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
+                                                                uint32_t *__restrict__ bigList, uint32_t *__restrict__ bigCount)
 {
-  __shared__ uint32_t buf[kFillMax];
-  __shared__ uint32_t cnt;
-  uint64_t k = blockIdx.x;
+  __shared__ uint32_t buf[kTileWarps][kWarpFill];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
   if (k >= a.T)
     return;
   uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
   if (M == 0)
     return;
+  if (M > kWarpFill)
+  {
+    if (lane == 0)
+      bigList[atomicAdd(bigCount, 1u)] = (uint32_t)k;
+    return;
+  }
+  uint32_t *b = buf[w];
+  const unsigned lt = (1u << lane) - 1;
+  TileFrame f = tileFrame(a, gd, k);
+  uint32_t n = 0;
+  for (int j = f.j0; j <= f.j1; j++)
+    for (int i = f.i0; i <= f.i1; i++)
+    {
+      uint64_t c = (uint64_t)j * gd.nx + i;
+      uint32_t cb = gd.cellStart[c], ce = gd.cellStart[c + 1];
+      if (cb == ce || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
+        continue;
+      for (uint32_t t0 = cb; t0 < ce; t0 += 32)
+      {
+        uint32_t t = t0 + lane;
+        uint32_t gp = 0;
+        bool in = false;
+        if (t < ce)
+        {
+          gp = gd.gpos[t];
+          in = cylMember(a, gd, f, gp, gd.gx[t], gd.gy[t]);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, in);
+        if (in && n + __popc(m & lt) < kWarpFill)
+          b[n + __popc(m & lt)] = gp & 0x7fffffffu;
+        n += __popc(m);
+      }
+    }
+  int P = 32;
+  while (P < (int)M)
+    P <<= 1;
+  for (int t = lane + (int)M; t < P; t += 32)
+    b[t] = 0xffffffffu;
+  __syncwarp();
+  for (int kk = 2; kk <= P; kk <<= 1)
+    for (int jj = kk >> 1; jj > 0; jj >>= 1)
+    {
+      for (int t = lane; t < P; t += 32)
+      {
+        int u = t ^ jj;
+        if (u > t)
+        {
+          bool up = (t & kk) == 0;
+          uint32_t x = b[t], y = b[u];
+          if ((x > y) == up)
+          {
+            b[t] = y;
+            b[u] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  for (uint32_t t = lane; t < M; t += 32)
+  {
+    uint32_t jpos = b[t];
+    tilePts[base + t] = jpos;
+    atomicMax(&owner[jpos], (int32_t)k);
+  }
+}
+
+/* The block-wide fill for the tiles gridFillWarp listed (up to kFillMax points). */
+__global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd, const uint32_t *__restrict__ tileStart,
+                                                         uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
+                                                         int *__restrict__ overflow, const uint32_t *__restrict__ bigList,
+                                                         const uint32_t *__restrict__ bigCount)
+{
+  __shared__ uint32_t buf[kFillMax];
+  __shared__ uint32_t cnt;
+  for (uint32_t bi = blockIdx.x; bi < *bigCount; bi += gridDim.x)
+  {
+  uint64_t k = bigList[bi];
+  uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
   if (M > kFillMax)
   {
     if (threadIdx.x == 0)
       atomicExch(overflow, 1);
-    return;
+    continue;
   }
   if (threadIdx.x == 0)
     cnt = 0;
@@ -249,6 +332,8 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
     uint32_t j = buf[t];
     tilePts[base + t] = j;
     atomicMax(&owner[j], (int32_t)k);
+  }
+  __syncthreads();
   }
 }
 
@@ -814,8 +899,14 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
     return rc;
   { fillOwner<<<(unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(owner, nd); ++c->launches; }
   int *dOvf = (int *)((char *)c->small.p + 384);
-  WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 4, c->stream));
-  { gridFill<<<(unsigned)T, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner, dOvf); ++c->launches; }
+  uint32_t *dBig = (uint32_t *)((char *)c->small.p + 392);
+  if ((rc = wb_ensure(c, c->tileNg, T * 4 + 64)))
+    return rc;
+  WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 8, c->stream));
+  { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
+                                                           (uint32_t *)c->tileNg.p, dBig); ++c->launches; }
+  { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
+                                                                   dOvf, (const uint32_t *)c->tileNg.p, dBig); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   int ovf = 0;
   WB_CUDA(c, cudaMemcpyAsync(&ovf, dOvf, 4, cudaMemcpyDeviceToHost, c->stream));
