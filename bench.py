@@ -151,6 +151,136 @@ def workload(args, rank):
     return cloud, cfg
 
 
+def _gen_tile(spec):
+    from wolkenbase_gb300 import synth
+    kind, n, seed, frac = spec
+    if kind == "batch":
+        return synth.batch_tile(n, seed, frac)
+    return synth.density_tile(n, seed)
+
+
+def generate(specs, procs=None):
+    """Generates clouds in a spawn-started process pool (safe beside CUDA)."""
+    import multiprocessing as mp
+    procs = procs or min(len(specs), os.cpu_count() or 1, 32)
+    if procs <= 1:
+        return [_gen_tile(s) for s in specs]
+    order = sorted(range(len(specs)), key=lambda i: -specs[i][1])   # big ones first
+    with mp.get_context("spawn").Pool(procs) as pool:
+        got = pool.map(_gen_tile, [specs[i] for i in order], chunksize=1)
+    out = [None] * len(specs)
+    for i, c in zip(order, got):
+        out[i] = c
+    return out
+
+
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def served_form(args, device):
+    """Poisson arrivals of tile-classify requests replayed against the plain
+    per-request path (one context, one request at a time, in arrival order)
+    and against the server (admission by HBM budget, overlapping scans, fused
+    classify launches).  Host buffers in and out for both."""
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import synth
+    reqs = synth.serve_requests(args.serve_requests, rate=args.serve_rate, seed=args.seed + 5000)
+    clouds = generate([("serve", n, seed, 0.0) for _, n, seed in reqs])
+    arrivals = [t for t, _, _ in reqs]
+    pts = sum(c.n for c in clouds)
+
+    def plain_pass(clf):
+        lat = []
+        t0 = time.perf_counter()
+        for t, c in zip(arrivals, clouds):
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            clf.classify_cloud(c)
+            lat.append(time.perf_counter() - (t0 + t))
+        return time.perf_counter() - t0, lat
+
+    def served_pass(srv):
+        ids = [None] * len(clouds)
+        t0 = time.perf_counter()
+        s0 = srv.stats()["now"]
+
+        def feeder():
+            for i, (t, c) in enumerate(zip(arrivals, clouds)):
+                d = t0 + t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                ids[i] = srv.submit(c, tag=i)
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        sts = [srv.result(j)[1] for j in ids]
+        lat = [st["t_done"] - (s0 + arrivals[i]) for i, st in enumerate(sts)]
+        span = max(st["t_done"] for st in sts) - s0
+        return span, lat, sts
+
+    clf = wb.Classifier(device)
+    big = max(clouds, key=lambda c: c.n)
+    clf.classify_cloud(big)                       # buffers sized once
+    plain_span, plain_lat = plain_pass(clf)
+    clf.close()
+    srv = wb.Server(device, prep_slots=args.serve_slots, hbm_budget=int(args.serve_budget_gb * 2**30))
+    served_pass(srv)                              # contexts sized once
+    launches0 = srv.stats()["kernel_launches"]
+    span, lat, sts = served_pass(srv)
+    st = srv.stats()
+    srv.close()
+    batch = [s["batch_jobs"] for s in sts]
+    return {"workload": f"{len(clouds)} requests, Poisson arrivals at {args.serve_rate:g}/s, sizes log-uniform "
+                        f"10k-10M points (100 pts/m^2 tiles), {args.serve_budget_gb:g} GB HBM budget",
+            "points": pts,
+            "plain": {"value": pts / plain_span / 1e6, "unit": UNIT, "p50_ms": _pct(plain_lat, 50) * 1e3,
+                      "p99_ms": _pct(plain_lat, 99) * 1e3, "makespan_s": plain_span},
+            "served": {"value": pts / span / 1e6, "unit": UNIT, "p50_ms": _pct(lat, 50) * 1e3,
+                       "p99_ms": _pct(lat, 99) * 1e3, "makespan_s": span, "prep_slots": args.serve_slots,
+                       "fused_launches": st["fused_launches"], "mean_jobs_per_launch":
+                           float(np.mean(batch)), "peak_bytes": st["peak_bytes"],
+                       "gpu_launches": st["kernel_launches"] - launches0},
+            "served_over_plain": (pts / span) / (pts / plain_span)}
+
+
+def batched_form(args, device):
+    """256 independent tiles of uneven size: sequential plain launches (one
+    wb_classify_cloud per tile) against one wb_classify_batch (all tiles
+    scanned concurrently, one fused graph-captured classify).  Host buffers."""
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    specs = synth.batch_tiles(args.batch_tiles)
+    clouds = generate([("batch", n, seed, frac) for n, seed, frac in specs])
+    pts = sum(c.n for c in clouds)
+    clf = wb.Classifier(device)
+    plain_ref = [clf.classify_cloud(c) for c in clouds]          # warm-up, buffers sized
+    t0 = time.perf_counter()
+    for c in clouds:
+        clf.classify_cloud(c)
+    plain_s = time.perf_counter() - t0
+    clf.close()
+    srv = wb.Server(device, prep_slots=args.batch_slots, flush=_lib.WB_FLUSH_FULL)
+    got = srv.classify_batch(clouds)                              # warm-up, contexts sized
+    st0 = srv.stats()
+    launches0, fused0 = st0["kernel_launches"], st0["fused_launches"]
+    t0 = time.perf_counter()
+    got = srv.classify_batch(clouds)
+    batch_s = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    same = all(np.array_equal(a, b) for a, b in zip(plain_ref, got))
+    return {"workload": f"{len(clouds)} tiles, log-uniform 50k-5M points (100 pts/m^2), slopes to 35 deg, "
+                        "nonground 5-40%",
+            "points": pts,
+            "plain": {"value": pts / plain_s / 1e6, "unit": UNIT, "seconds": plain_s},
+            "batched": {"value": pts / batch_s / 1e6, "unit": UNIT, "seconds": batch_s,
+                        "fused_launches": st["fused_launches"] - fused0, "prep_slots": args.batch_slots,
+                        "gpu_launches": st["kernel_launches"] - launches0},
+            "batched_over_plain": plain_s / batch_s, "same_labels": same}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -185,6 +315,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=150_000, help="points in the CPU-baseline sample")
     ap.add_argument("--ref-sample", type=int, default=40_000, help="points per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the served and batched measurements")
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-budget-gb", type=float, default=80.0)
+    ap.add_argument("--batch-tiles", type=int, default=256)
+    ap.add_argument("--batch-slots", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -315,9 +452,14 @@ def main():
                      if build_ms else None, "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT},
            "octree": {"leaves": info["n_leaves"], "distinct": nd, "max_depth": info["max_depth"]},
            "labels": {"ground": int(labels[2]), "not_ground": int(labels[1]), "untouched": int(labels[0])}}
+    clf.close()
+    del dev_xyz, dev_cls, pin_xyz, pin_cls
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_forms:
+        out["served"] = served_form(args, local)
+        out["batched"] = batched_form(args, local)
     if rank == 0:
         print(json.dumps(out))
-    clf.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

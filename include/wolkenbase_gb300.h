@@ -33,6 +33,8 @@ extern "C" {
 #define WB_ESTATE -5      /* call out of order (e.g. classify before build)  */
 #define WB_ETIMEDOUT -6   /* a bounded device-side wait gave up              */
 #define WB_ENOTFOUND -7   /* no such job / entry                             */
+#define WB_EBUSY -8       /* job already running or finished (wb_cancel)     */
+#define WB_ECANCELED -9   /* job was cancelled before it ran                 */
 
 typedef struct wb_ctx wb_ctx;
 
@@ -174,6 +176,92 @@ int wb_launch_count(wb_ctx *ctx, uint64_t *count);
 int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out);
 int wb_check_hypot(const double *ab, uint64_t m, double *out);
 int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz, uint64_t m, uint8_t *out);
+
+/* ---- Serving and batching ----
+ *
+ * No reference counterpart as an API: the reference runs one cloud at a time
+ * through WolkenCanvas::startProcess and the TH_* phases of WolkenThread
+ * (wolkencanvas.cpp:469-532, threads.cpp:547-660).  A server takes
+ * tile-classify jobs as they arrive and runs each through the same path as
+ * wb_classify_cloud (same results, bit for bit): up to prep_slots jobs are
+ * built and scanned at once on their own streams, each job's octree and point
+ * buffers stay on the device until its class bytes are out, and jobs whose
+ * scan has finished are classified together by one fused, graph-captured
+ * launch over all their points.  A job is admitted only while the device
+ * memory all admitted jobs hold, plus its own estimate, stays within
+ * hbm_budget; jobs start in submission order. */
+typedef struct wb_server wb_server;
+
+#define WB_FLUSH_EAGER 0   /* classify whatever has been scanned (serving)            */
+#define WB_FLUSH_FULL 1    /* wait until every admitted job is scanned (batching)     */
+
+typedef struct
+{
+  int device;
+  int prep_slots;        /* jobs built and scanned concurrently; 0 = 4              */
+  uint64_t hbm_budget;   /* bytes all resident jobs may hold; 0 = 80% of free memory */
+  int flush;             /* WB_FLUSH_EAGER or WB_FLUSH_FULL                         */
+  int max_batch;         /* most jobs in one fused classify launch; 0 = 512 (max)   */
+  int block_warps;       /* warps per block of the fused launch (2, 4, 8); 0 = 4    */
+  int chunk;             /* points a warp takes per visit to the work counter; 0 = 16 */
+} wb_server_config;
+
+typedef struct
+{
+  wb_cloud cloud;        /* records stay valid and unchanged until the job ends     */
+  wb_params params;
+  uint8_t *cls;          /* n class bytes, host memory, as for wb_classify          */
+  uint64_t tag;          /* caller's value, returned in wb_job_status               */
+} wb_job;
+
+#define WB_JOB_QUEUED 0
+#define WB_JOB_PREP 1       /* building the octree and scanning the tiles */
+#define WB_JOB_READY 2      /* scanned, waiting for a fused classify      */
+#define WB_JOB_CLASSIFY 3
+#define WB_JOB_DONE 4
+#define WB_JOB_FAILED 5
+#define WB_JOB_CANCELLED 6
+
+typedef struct
+{
+  int state;                 /* WB_JOB_*                                              */
+  int rc;                    /* 0, or the WB_E* code of a failed or cancelled job     */
+  uint64_t tag;
+  uint64_t n_points, n_ground, n_ambiguous;
+  uint64_t reserved_bytes;   /* device memory the job was admitted against            */
+  double t_submit, t_admit, t_ready, t_done;   /* seconds on the server's clock      */
+  int batch_jobs;            /* jobs in the fused classify launch it ran in           */
+  int pad;
+} wb_job_status;
+
+typedef struct
+{
+  uint64_t submitted, completed, failed, cancelled;
+  uint64_t points;           /* input records of completed jobs                       */
+  uint64_t fused_launches, fused_jobs;
+  uint64_t held_bytes, peak_bytes, budget;
+  uint64_t kernel_launches;  /* kernels the server's contexts and graphs launched     */
+  int contexts, queued, running, pad;
+  double now;                /* the server's clock                                    */
+} wb_server_stats;
+
+wb_server *wb_server_open(const wb_server_config *cfg);   /* NULL on error: wb_last_error(NULL) */
+void wb_server_close(wb_server *s);                       /* cancels queued jobs, waits for running ones */
+const char *wb_server_error(const wb_server *s);
+/* Returns the job id (>= 0) or a WB_E* code. */
+int64_t wb_submit(wb_server *s, const wb_job *job);
+int wb_poll(wb_server *s, int64_t id, wb_job_status *st);
+/* Waits until the job is done, failed or cancelled, or timeout_s passes
+ * (WB_ETIMEDOUT); timeout_s < 0 waits without limit. */
+int wb_wait(wb_server *s, int64_t id, double timeout_s, wb_job_status *st);
+/* Cancels a queued job; WB_EBUSY once it has been admitted. */
+int wb_cancel(wb_server *s, int64_t id);
+/* Forgets a finished job's status. */
+int wb_release(wb_server *s, int64_t id);
+int wb_server_stats_get(wb_server *s, wb_server_stats *out);
+/* Runs k jobs (the C++ adapter's TH_SCAN/TH_SPLIT over many clouds) and waits
+ * for all; rcs[i] receives each job's code.  Returns 0 if all succeeded. */
+int wb_classify_batch(wb_server *s, const wb_job *jobs, int k, int *rcs);
 
 #ifdef __cplusplus
 }

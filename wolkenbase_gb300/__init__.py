@@ -12,6 +12,7 @@ mirror of the reference's interface for that path:
   scanCylinder + postscanCylinder (scan.cpp)      Classifier.scan(params)
   classifyCylinder (classify.cpp:96)              Classifier.classify(params, cls)
   Tile (tile.h:27-35)                             Classifier.tiles()
+  WolkenCanvas::startProcess per cloud, many      Server.submit / result, classify_batch
 
 Errors raise WolkenbaseError carrying the C status code.
 """
@@ -25,7 +26,7 @@ import numpy as np
 from . import _lib
 from ._lib import wb_cloud, wb_octree_stats, wb_params, wb_tile
 
-__all__ = ["Params", "Classifier", "WolkenbaseError", "cloud_struct"]
+__all__ = ["Params", "Classifier", "Server", "WolkenbaseError", "cloud_struct"]
 
 
 class WolkenbaseError(RuntimeError):
@@ -192,3 +193,106 @@ class Classifier:
         ms = (C.c_float * 64)()
         self._check(self.L.wb_stage_times(self.ctx, names, ms, 64, C.byref(cnt)))
         return [(names[i].decode(), ms[i]) for i in range(cnt.value)]
+
+
+class Server:
+    """Request loop over one GPU (wb_server_open): jobs arrive with wb_submit,
+    are admitted by an HBM budget, built and scanned concurrently, and
+    classified together by fused launches.  Results are identical to
+    Classifier.classify_cloud on the same cloud."""
+
+    def __init__(self, device=0, prep_slots=4, hbm_budget=0, flush=_lib.WB_FLUSH_EAGER, max_batch=0,
+                 block_warps=0, chunk=0):
+        self.L = _lib.load()
+        cfg = _lib.wb_server_config(device, prep_slots, hbm_budget, flush, max_batch, block_warps, chunk)
+        self.s = self.L.wb_server_open(C.byref(cfg))
+        if not self.s:
+            raise WolkenbaseError(_lib.WB_ECUDA, self.L.wb_last_error(None).decode())
+        self._alive = {}   # id -> arrays the job reads or writes
+
+    def close(self):
+        if self.s:
+            self.L.wb_server_close(self.s)
+            self.s = None
+            self._alive.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _job(self, cloud, params, cls, tag):
+        xyz = np.ascontiguousarray(cloud.xyz, dtype=np.int32)
+        if cls is None:
+            cls = np.zeros(xyz.shape[0], np.uint8)
+        cls = np.ascontiguousarray(cls, dtype=np.uint8)
+        j = _lib.wb_job()
+        j.cloud = cloud_struct(xyz, xyz.shape[0], 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+        j.params = (params or Params()).c()
+        j.cls = cls.ctypes.data
+        j.tag = tag
+        return j, xyz, cls
+
+    def submit(self, cloud, params=None, cls=None, tag=0):
+        """Queues one cloud; returns the job id.  The result lands in result(id)."""
+        j, xyz, cls = self._job(cloud, params, cls, tag)
+        jid = self.L.wb_submit(self.s, C.byref(j))
+        if jid < 0:
+            raise WolkenbaseError(jid, self.L.wb_server_error(self.s).decode())
+        self._alive[jid] = (xyz, cls)
+        return jid
+
+    def poll(self, jid):
+        st = _lib.wb_job_status()
+        rc = self.L.wb_poll(self.s, jid, C.byref(st))
+        if rc:
+            raise WolkenbaseError(rc, "wb_poll")
+        return _status(st)
+
+    def wait(self, jid, timeout=-1.0):
+        st = _lib.wb_job_status()
+        rc = self.L.wb_wait(self.s, jid, float(timeout), C.byref(st))
+        if rc == _lib.WB_ETIMEDOUT:
+            return None
+        if rc:
+            raise WolkenbaseError(rc, "wb_wait")
+        return _status(st)
+
+    def result(self, jid):
+        """Waits for the job; returns (class bytes, status) and forgets the job."""
+        st = self.wait(jid)
+        if st["rc"]:
+            raise WolkenbaseError(st["rc"], self.L.wb_server_error(self.s).decode())
+        cls = self._alive.pop(jid)[1]
+        self.L.wb_release(self.s, jid)
+        return cls, st
+
+    def cancel(self, jid):
+        return self.L.wb_cancel(self.s, jid)
+
+    def stats(self):
+        st = _lib.wb_server_stats()
+        rc = self.L.wb_server_stats_get(self.s, C.byref(st))
+        if rc:
+            raise WolkenbaseError(rc, "wb_server_stats_get")
+        return {f: getattr(st, f) for f, _ in st._fields_ if f != "pad"}
+
+    def classify_batch(self, clouds, params=None):
+        """wb_classify_batch over a list of clouds; returns their class bytes."""
+        k = len(clouds)
+        jobs = (_lib.wb_job * k)()
+        keep = []
+        for i, cl in enumerate(clouds):
+            j, xyz, cls = self._job(cl, params, None, i)
+            jobs[i] = j
+            keep.append((xyz, cls))
+        rcs = np.zeros(k, np.int32)
+        rc = self.L.wb_classify_batch(self.s, jobs, k, rcs.ctypes.data)
+        if rc:
+            raise WolkenbaseError(rc, self.L.wb_server_error(self.s).decode())
+        return [c for _, c in keep]
+
+
+def _status(st):
+    return {f: getattr(st, f) for f, _ in st._fields_ if f != "pad"}

@@ -12,8 +12,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libwolkenbase_gb300.so")
 
 WB_OK, WB_EINVAL, WB_ENOMEM, WB_ECUDA, WB_EDEPTH, WB_ESTATE, WB_ETIMEDOUT, WB_ENOTFOUND = 0, -1, -2, -3, -4, -5, -6, -7
+WB_EBUSY, WB_ECANCELED = -8, -9
 ERROR_NAMES = {WB_EINVAL: "WB_EINVAL", WB_ENOMEM: "WB_ENOMEM", WB_ECUDA: "WB_ECUDA", WB_EDEPTH: "WB_EDEPTH",
-               WB_ESTATE: "WB_ESTATE", WB_ETIMEDOUT: "WB_ETIMEDOUT", WB_ENOTFOUND: "WB_ENOTFOUND"}
+               WB_ESTATE: "WB_ESTATE", WB_ETIMEDOUT: "WB_ETIMEDOUT", WB_ENOTFOUND: "WB_ENOTFOUND",
+               WB_EBUSY: "WB_EBUSY", WB_ECANCELED: "WB_ECANCELED"}
+
+WB_FLUSH_EAGER, WB_FLUSH_FULL = 0, 1
+(WB_JOB_QUEUED, WB_JOB_PREP, WB_JOB_READY, WB_JOB_CLASSIFY, WB_JOB_DONE, WB_JOB_FAILED,
+ WB_JOB_CANCELLED) = range(7)
 
 
 class wb_params(C.Structure):
@@ -40,6 +46,30 @@ class wb_tile(C.Structure):
                 ("hyperboloid_size", C.c_double), ("height", C.c_double)]
 
 
+class wb_server_config(C.Structure):
+    _fields_ = [("device", C.c_int), ("prep_slots", C.c_int), ("hbm_budget", C.c_uint64), ("flush", C.c_int),
+                ("max_batch", C.c_int), ("block_warps", C.c_int), ("chunk", C.c_int)]
+
+
+class wb_job(C.Structure):
+    _fields_ = [("cloud", wb_cloud), ("params", wb_params), ("cls", C.c_void_p), ("tag", C.c_uint64)]
+
+
+class wb_job_status(C.Structure):
+    _fields_ = [("state", C.c_int), ("rc", C.c_int), ("tag", C.c_uint64), ("n_points", C.c_uint64),
+                ("n_ground", C.c_uint64), ("n_ambiguous", C.c_uint64), ("reserved_bytes", C.c_uint64),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_ready", C.c_double),
+                ("t_done", C.c_double), ("batch_jobs", C.c_int), ("pad", C.c_int)]
+
+
+class wb_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("points", C.c_uint64), ("fused_launches", C.c_uint64),
+                ("fused_jobs", C.c_uint64), ("held_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("budget", C.c_uint64), ("kernel_launches", C.c_uint64), ("contexts", C.c_int),
+                ("queued", C.c_int), ("running", C.c_int), ("pad", C.c_int), ("now", C.c_double)]
+
+
 # name -> (restype, argtypes); every symbol include/wolkenbase_gb300.h declares
 SIGNATURES = {
     "wb_open": (C.c_void_p, [C.c_int, C.c_size_t]),
@@ -64,6 +94,16 @@ SIGNATURES = {
     "wb_check_atan2i": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_check_hypot": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_check_hyperboloid": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
+    "wb_server_close": (None, [C.c_void_p]),
+    "wb_server_error": (C.c_char_p, [C.c_void_p]),
+    "wb_submit": (C.c_int64, [C.c_void_p, C.POINTER(wb_job)]),
+    "wb_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(wb_job_status)]),
+    "wb_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(wb_job_status)]),
+    "wb_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
+    "wb_release": (C.c_int, [C.c_void_p, C.c_int64]),
+    "wb_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(wb_server_stats)]),
+    "wb_classify_batch": (C.c_int, [C.c_void_p, C.POINTER(wb_job), C.c_int, C.c_void_p]),
 }
 
 _lib = None

@@ -22,6 +22,9 @@ int wb_fail(wb_ctx *c, int code, const std::string &msg)
   return code;
 }
 
+/* Buffers are stream-ordered allocations on the context's stream: growing
+ * one frees the old block after the work queued before it, and neither call
+ * waits for other streams (several contexts share a GPU in a server). */
 int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes)
 {
   if (bytes <= b.cap)
@@ -30,25 +33,27 @@ int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes)
   if (c->budget && c->used - b.cap + want > c->budget)
     return wb_fail(c, WB_ENOMEM, "device memory budget exceeded (" + std::to_string(c->used - b.cap + want) +
                                      " > " + std::to_string(c->budget) + " bytes)");
-  if (b.p)
-  {
-    // ordered free: earlier work on the stream may still read the old buffer
-    cudaStreamSynchronize(c->stream);
-    cudaFree(b.p);
-    c->used -= b.cap;
-    b.p = nullptr;
-    b.cap = 0;
-  }
-  cudaError_t e = cudaMalloc(&b.p, want);
+  wb_free_buf(c, b);
+  cudaError_t e = cudaMallocAsync(&b.p, want, c->stream);
   if (e != cudaSuccess)
   {
     b.p = nullptr;
     cudaGetLastError();
-    return wb_fail(c, WB_ENOMEM, std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
+    return wb_fail(c, WB_ENOMEM, std::string("cudaMallocAsync(") + std::to_string(want) + "): " + cudaGetErrorString(e));
   }
   b.cap = want;
   c->used += want;
   return 0;
+}
+
+void wb_free_buf(wb_ctx *c, DevBuf &b)
+{
+  if (!b.p)
+    return;
+  cudaFreeAsync(b.p, c->stream);
+  c->used -= b.cap;
+  b.p = nullptr;
+  b.cap = 0;
 }
 
 void wb_mark(wb_ctx *c, const char *name)
@@ -63,7 +68,7 @@ void wb_mark(wb_ctx *c, const char *name)
   c->events.push_back(ev);
 }
 
-static void releaseBuffers(wb_ctx *c)
+void wb_release_buffers(wb_ctx *c)
 {
   DevBuf *all[] = {&c->rec, &c->key0, &c->key1, &c->idx0, &c->idx1, &c->tmp32, &c->tmp32b, &c->tmp8, &c->scanTmp,
                    &c->small, &c->lev, &c->cpl, &c->pre, &c->suf, &c->leafId, &c->leafFirst, &c->leafCount,
@@ -74,12 +79,7 @@ static void releaseBuffers(wb_ctx *c)
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
                    &c->cellBox, &c->gx, &c->gy, &c->gz, &c->gpos, &c->superBox, &c->cellFlag, &c->ptSetup};
   for (DevBuf *b : all)
-    if (b->p)
-    {
-      cudaFree(b->p);
-      b->p = nullptr;
-      b->cap = 0;
-    }
+    wb_free_buf(c, *b);
   c->used = 0;
 }
 
@@ -155,7 +155,8 @@ void wb_close(wb_ctx *c)
     cudaStreamSynchronize(c->stream);
   for (cudaEvent_t e : c->events)
     cudaEventDestroy(e);
-  releaseBuffers(c);
+  wb_release_buffers(c);
+  cudaStreamSynchronize(c->stream);
   if (c->own_stream && c->stream)
     cudaStreamDestroy(c->stream);
   delete c;
@@ -542,11 +543,7 @@ int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
   DevBuf in, out;
   if ((rc = wb_ensure(c, in, m * 24)) || (rc = wb_ensure(c, out, m * 8)))
   {
-    if (in.p)
-    {
-      cudaFree(in.p);
-      c->used -= in.cap;
-    }
+    wb_free_buf(c, in);
     return rc;
   }
   WbRoot r;
@@ -559,10 +556,9 @@ int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
       (const double *)in.p, m, r, (const uint64_t *)c->leafKey.p, (const uint8_t *)c->leafLevel.p, c->n_leaves,
       (int64_t *)out.p); ++c->launches; }
   cudaMemcpyAsync(leaf, out.p, m * 8, cudaMemcpyDeviceToHost, c->stream);
+  wb_free_buf(c, in);
+  wb_free_buf(c, out);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  cudaFree(in.p);
-  cudaFree(out.p);
-  c->used -= in.cap + out.cap;
   if (e != cudaSuccess)
     return wb_fail(c, WB_ECUDA, std::string("wb_octree_find_block: ") + cudaGetErrorString(e));
   return 0;

@@ -33,6 +33,10 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
 #include "wb_internal.h"
 #include "wb_device.cuh"
 #include "angle_tables.h"
@@ -107,12 +111,16 @@ struct ClsArgs
   double zmin;
   int exactInts;   /* decode strictly increasing and 32-bit record differences exact */
   float fsx, fsy, fsz, fs2;   /* metres per record unit and slope^2, FP32 */
-  const PtSetup *setup;
+  PtSetup *setup;
   /* ambiguous points for the exact pass */
   uint32_t *ambList;
   uint32_t *ambCount;
   const uint32_t *work;   /* exact pass: store positions to classify */
   uint32_t nwork;
+  /* finishing (fused launch): records, their store positions and class bytes */
+  uint64_t n, nTiles;
+  const uint32_t *storeOf;
+  uint8_t *cls;
 };
 
 __device__ __forceinline__ double decA(const ClsArgs &a, int ax, int32_t q)
@@ -254,44 +262,44 @@ __device__ __forceinline__ uint32_t largestGap(const uint32_t *bmin, const uint3
   return worst;
 }
 
-/* Thread per point: the double-precision set-up of each point's query. */
-__global__ void classifySetup(ClsArgs a, PtSetup *__restrict__ out)
+/* The double-precision set-up of point j's query, one thread per point. */
+__device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
 {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < a.nd; j += (uint64_t)gridDim.x * blockDim.x)
-  {
-    int32_t k = a.owner[j];
-    if (k < 0)
-      continue;
-    double hs = a.tiles[k].h;
-    double px = decA(a, 0, a.sx[j]), py = decA(a, 1, a.sy[j]), pz = decA(a, 2, a.sz[j]);
-    double por = hs * (a.slope * a.slope);
-    double por2 = por * por;
-    double cz = (pz - a.thickness) + por;
-    PtSetup s;
-    s.czp = (float)(cz - pz);
-    s.por2f = (float)por2;
-    // horizontal reach of the hyperboloid at the lowest point of the cloud
-    double zdMax = cz - a.zmin;
-    double reach2 = (zdMax * zdMax - por2) / (a.slope * a.slope);
-    double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
-    double fi = floor((px - a.gx0) / a.cell), fj = floor((py - a.gy0) / a.cell);
-    s.ci = (int32_t)fmax(fmin(fi, 1e9), -1e9);
-    s.cj = (int32_t)fmax(fmin(fj, 1e9), -1e9);
-    s.kmax = (int32_t)fmin(ceil(reach / a.cell) + 1, 1e9);
-    s.smax = (int32_t)fmin(ceil(reach / (WB_SUPER * a.cell)) + 1, 1e9);
-    out[j] = s;
-  }
+  int32_t k = a.owner[j];
+  if (k < 0)
+    return;
+  double hs = a.tiles[k].h;
+  double px = decA(a, 0, a.sx[j]), py = decA(a, 1, a.sy[j]), pz = decA(a, 2, a.sz[j]);
+  double por = hs * (a.slope * a.slope);
+  double por2 = por * por;
+  double cz = (pz - a.thickness) + por;
+  PtSetup s;
+  s.czp = (float)(cz - pz);
+  s.por2f = (float)por2;
+  // horizontal reach of the hyperboloid at the lowest point of the cloud
+  double zdMax = cz - a.zmin;
+  double reach2 = (zdMax * zdMax - por2) / (a.slope * a.slope);
+  double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
+  double fi = floor((px - a.gx0) / a.cell), fj = floor((py - a.gy0) / a.cell);
+  s.ci = (int32_t)fmax(fmin(fi, 1e9), -1e9);
+  s.cj = (int32_t)fmax(fmin(fj, 1e9), -1e9);
+  s.kmax = (int32_t)fmin(ceil(reach / a.cell) + 1, 1e9);
+  s.smax = (int32_t)fmin(ceil(reach / (WB_SUPER * a.cell)) + 1, 1e9);
+  a.setup[j] = s;
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
+__global__ void classifySetup(ClsArgs a)
 {
-  __shared__ uint32_t bmin[kWarps][kBins], bmax[kWarps][kBins];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t item = (uint64_t)blockIdx.x * kWarps + w;
-  if (item >= (EXACT ? (uint64_t)a.nwork : a.nd))
-    return;
-  uint64_t j = EXACT ? a.work[item] : item;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < a.nd; j += (uint64_t)gridDim.x * blockDim.x)
+    setupPoint(a, j);
+}
+
+/* Classifies store position j with one warp; bminW/bmaxW are the warp's
+ * 64-bin direction extremes in shared memory. */
+template <bool EXACT>
+__device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int lane, uint32_t *bminW,
+                                              uint32_t *bmaxW)
+{
   int32_t k = a.owner[j];
   if (k < 0)
   {
@@ -313,8 +321,8 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
   h.por2f = ps.por2f;
   for (int b = lane; b < kBins; b += 32)
   {
-    bmin[w][b] = 0xffffffffu;
-    bmax[w][b] = 0;
+    bminW[b] = 0xffffffffu;
+    bmaxW[b] = 0;
   }
   __syncwarp();
   const int ci = ps.ci, cj = ps.cj, kmax = ps.kmax;
@@ -419,8 +427,8 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
       {
         if (lane == 0)
         {
-          atomicMin(&bmin[w][lo >> 25], lo);
-          atomicMax(&bmax[w][lo >> 25], hi);
+          atomicMin(&bminW[lo >> 25], lo);
+          atomicMax(&bmaxW[lo >> 25], hi);
         }
         if ((lo >> 25) < 32)
           occLo |= 1u << (lo >> 25);
@@ -431,8 +439,8 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
       {
         if (in)
         {
-          atomicMin(&bmin[w][bin], u);
-          atomicMax(&bmax[w][bin], u);
+          atomicMin(&bminW[bin], u);
+          atomicMax(&bmaxW[bin], u);
         }
         occLo |= __reduce_or_sync(0xffffffffu, in && bin < 32 ? 1u << bin : 0u);
         occHi |= __reduce_or_sync(0xffffffffu, in && bin >= 32 ? 1u << (bin - 32) : 0u);
@@ -460,7 +468,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
       return;
     __syncwarp();
     int nocc;
-    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
+    uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
     if (nocc >= 2)
       surrounded = (EXACT || !fast) ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
   };
@@ -564,7 +572,7 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
   {
     int nocc;
     __syncwarp();
-    uint32_t gap = largestGap(bmin[w], bmax[w], lane, nocc);
+    uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
     ambiguous = nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
   }
 #ifdef WB_CLASSIFY_STATS
@@ -582,6 +590,17 @@ __global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
     if (ambiguous)
       a.ambList[atomicAdd(a.ambCount, 1u)] = (uint32_t)j;
   }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
+{
+  __shared__ uint32_t bmin[kWarps][kBins], bmax[kWarps][kBins];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t item = (uint64_t)blockIdx.x * kWarps + w;
+  if (item >= (EXACT ? (uint64_t)a.nwork : a.nd))
+    return;
+  classifyPoint<EXACT>(a, EXACT ? a.work[item] : item, lane, bmin[w], bmax[w]);
 }
 
 __global__ void scatterCls(uint64_t n, const uint32_t *__restrict__ storeOf, const int32_t *__restrict__ owner,
@@ -626,7 +645,9 @@ static bool decodeIsExact(const WbGeom &g, const double mn[3], const double mx[3
   return true;
 }
 
-int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
+/* Checks the state, sizes the buffers, uploads the angle tables and the
+ * incoming class bytes, and forms the kernel arguments (on c's stream). */
+static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, ClsArgs &a)
 {
   if (c->stage < 2)
     return wb_fail(c, WB_ESTATE, "wb_classify: scan the tiles first");
@@ -649,7 +670,6 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   if (!onDevice && n)
     WB_CUDA(c, cudaMemcpyAsync(clsDev, cls, n, cudaMemcpyHostToDevice, c->stream));
   wb_mark(c, "cls_upload");
-  ClsArgs a;
   a.nd = nd;
   const WbGeom &g = c->g;
   double mn[3], mx[3];
@@ -702,16 +722,31 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   a.fsy = (float)(g.scale[1] * g.unit);
   a.fsz = (float)(g.scale[2] * g.unit);
   a.fs2 = (float)(p->max_slope * p->max_slope);
-  a.setup = (const PtSetup *)c->ptSetup.p;
+  a.setup = (PtSetup *)c->ptSetup.p;
   a.ambList = (uint32_t *)c->ambiguous.p;
   a.ambCount = (uint32_t *)((char *)c->small.p + 448);
   a.work = nullptr;
   a.nwork = 0;
+  a.n = n;
+  a.nTiles = c->n_tiles;
+  a.storeOf = (const uint32_t *)c->storeOf.p;
+  a.cls = clsDev;
   WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 4, c->stream));
+  return 0;
+}
+
+int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
+{
+  ClsArgs a;
+  int rc = classifyPrepare(c, p, cls, onDevice, a);
+  if (rc)
+    return rc;
+  uint64_t nd = c->nd, n = c->n;
+  uint8_t *clsDev = a.cls;
   if (nd)
   {
     unsigned sb = (unsigned)std::min<uint64_t>((nd + 255) / 256, (uint64_t)c->sm_count * 16);
-    { classifySetup<<<sb, 256, 0, c->stream>>>(a, (PtSetup *)c->ptSetup.p); ++c->launches; }
+    { classifySetup<<<sb, 256, 0, c->stream>>>(a); ++c->launches; }
     { classifyRings<false><<<(unsigned)((nd + kWarps - 1) / kWarps), 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
     WB_CUDA(c, cudaGetLastError());
   }
@@ -739,4 +774,389 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   wb_mark(c, "cls_download");
   c->stage = 3;
   return 0;
+}
+
+/* ---- Fused classify of many jobs: one persistent launch over all their points ----
+ *
+ * Each job is a context that has been built and scanned; wb_classify_stage
+ * formed its kernel arguments.  The job table (arguments and prefix sums of
+ * the jobs' point, record and tile counts) is uploaded from a pinned mirror
+ * by the first node of a captured CUDA graph, so one graph serves every
+ * batch: the kernels read the job count and offsets from device memory.
+ * Warps of the persistent ring kernel take chunks of consecutive points from
+ * a global counter and copy the owning job's arguments to shared memory when
+ * the job changes. */
+namespace
+{
+struct BatchHdr
+{
+  int k, chunk;
+  unsigned long long next[2];   /* work counters of the fast and the exact pass */
+  uint64_t startNd[WB_BATCH_MAX + 1], startN[WB_BATCH_MAX + 1], startT[WB_BATCH_MAX + 1];
+  ClsArgs jobs[WB_BATCH_MAX];
+};
+struct BatchOut
+{
+  uint64_t startAmb[WB_BATCH_MAX + 1];   /* prefix of the jobs' ambiguous counts */
+  unsigned long long ground[WB_BATCH_MAX];
+};
+
+/* The job q with start[q] <= g < start[q+1] (start non-decreasing, g < start[k]). */
+__device__ __forceinline__ int batchJob(const uint64_t *start, int k, uint64_t g)
+{
+  int lo = 0, hi = k;
+  while (hi - lo > 1)
+  {
+    int mid = (lo + hi) >> 1;
+    if (start[mid] <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void batchSetup(const BatchHdr *__restrict__ h)
+{
+  const int k = h->k;
+  const uint64_t total = h->startNd[k];
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int q = batchJob(h->startNd, k, g);
+    setupPoint(h->jobs[q], g - h->startNd[q]);
+  }
+}
+
+template <bool EXACT, int W>
+__global__ void __launch_bounds__(32 * W) batchRings(BatchHdr *h, const BatchOut *o)
+{
+  __shared__ uint32_t bmin[W][kBins], bmax[W][kBins];
+  __shared__ ClsArgs sa[W];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = h->k;
+  const uint64_t *start = EXACT ? o->startAmb : h->startNd;
+  const uint64_t total = start[k];
+  const unsigned chunk = EXACT ? 1u : (unsigned)h->chunk;
+  uint64_t lo = 1, hi = 0;
+  for (;;)
+  {
+    unsigned long long base = 0;
+    if (lane == 0)
+      base = atomicAdd(&h->next[EXACT ? 1 : 0], (unsigned long long)chunk);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total)
+      break;
+    uint64_t end = base + chunk < total ? base + chunk : total;
+    for (uint64_t g = base; g < end; g++)
+    {
+      if (g < lo || g >= hi)
+      {
+        int q = batchJob(start, k, g);
+        lo = start[q];
+        hi = start[q + 1];
+        __syncwarp();
+        const uint32_t *src = (const uint32_t *)&h->jobs[q];
+        uint32_t *dst = (uint32_t *)&sa[w];
+        for (int i = lane; i < (int)(sizeof(ClsArgs) / 4); i += 32)
+          dst[i] = src[i];
+        __syncwarp();
+      }
+      const ClsArgs &a = sa[w];
+      uint64_t item = g - lo;
+      classifyPoint<EXACT>(a, EXACT ? a.ambList[item] : item, lane, bmin[w], bmax[w]);
+    }
+  }
+}
+
+__global__ void batchAmbPrefix(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
+{
+  if (threadIdx.x || blockIdx.x)
+    return;
+  uint64_t s = 0;
+  for (int q = 0; q < h->k; q++)
+  {
+    o->startAmb[q] = s;
+    s += *h->jobs[q].ambCount;
+  }
+  o->startAmb[h->k] = s;
+}
+
+__global__ void batchZeroGround(const BatchHdr *__restrict__ h)
+{
+  const int k = h->k;
+  const uint64_t total = h->startT[k];
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int q = batchJob(h->startT, k, g);
+    ((TileRes *)h->jobs[q].tiles)[g - h->startT[q]].nGround = 0;
+  }
+}
+
+__global__ void batchGroundCount(const BatchHdr *__restrict__ h)
+{
+  const int k = h->k;
+  const uint64_t total = h->startNd[k];
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int q = batchJob(h->startNd, k, g);
+    const ClsArgs &a = h->jobs[q];
+    uint64_t j = g - h->startNd[q];
+    int32_t t = a.owner[j];
+    if (t >= 0 && a.label[j] == 2)
+      atomicAdd(&((TileRes *)a.tiles)[t].nGround, 1);
+  }
+}
+
+/* Block q sums job q's per-tile ground counts. */
+__global__ void batchGroundTotal(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
+{
+  __shared__ unsigned long long part[8];
+  const int q = blockIdx.x;
+  if (q >= h->k)
+    return;
+  const ClsArgs &a = h->jobs[q];
+  unsigned long long s = 0;
+  for (uint64_t t = threadIdx.x; t < a.nTiles; t += blockDim.x)
+    s += (unsigned)a.tiles[t].nGround;
+  for (int d = 16; d; d >>= 1)
+    s += __shfl_down_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0)
+    part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    unsigned long long tot = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+      tot += part[i];
+    o->ground[q] = tot;
+  }
+}
+
+__global__ void batchScatter(const BatchHdr *__restrict__ h)
+{
+  const int k = h->k;
+  const uint64_t total = h->startN[k];
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int q = batchJob(h->startN, k, g);
+    const ClsArgs &a = h->jobs[q];
+    uint64_t i = g - h->startN[q];
+    uint32_t j = a.storeOf[i];
+    if (a.owner[j] >= 0)
+      a.cls[i] = a.label[j];
+  }
+}
+}  // namespace
+
+static_assert(sizeof(ClsArgs) <= sizeof(((wb_ctx *)nullptr)->clsArgs), "wb_ctx::clsArgs too small");
+
+struct WbBatch
+{
+  int device = 0, sm = 0;
+  cudaStream_t capture = nullptr;
+  BatchHdr *dIn = nullptr, *hIn = nullptr;
+  BatchOut *dOut = nullptr, *hOut = nullptr;
+  struct Graph
+  {
+    int warps, chunk;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+};
+
+int wb_batch_create(int device, WbBatch **out, std::string &err)
+{
+  *out = nullptr;
+  WbBatch *b = new (std::nothrow) WbBatch;
+  if (!b)
+    return WB_ENOMEM;
+  b->device = device;
+  cudaSetDevice(device);
+  cudaDeviceGetAttribute(&b->sm, cudaDevAttrMultiProcessorCount, device);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&b->dIn, sizeof(BatchHdr));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&b->dOut, sizeof(BatchOut));
+  if (e == cudaSuccess)
+    e = cudaMallocHost(&b->hIn, sizeof(BatchHdr));
+  if (e == cudaSuccess)
+    e = cudaMallocHost(&b->hOut, sizeof(BatchOut));
+  if (e != cudaSuccess)
+  {
+    err = std::string("wb_batch_create: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    wb_batch_destroy(b);
+    return WB_ENOMEM;
+  }
+  *out = b;
+  return 0;
+}
+
+void wb_batch_destroy(WbBatch *b)
+{
+  if (!b)
+    return;
+  cudaSetDevice(b->device);
+  for (auto &g : b->graphs)
+    cudaGraphExecDestroy(g.exec);
+  if (b->capture)
+    cudaStreamDestroy(b->capture);
+  cudaFree(b->dIn);
+  cudaFree(b->dOut);
+  cudaFreeHost(b->hIn);
+  cudaFreeHost(b->hOut);
+  delete b;
+}
+
+int wb_classify_stage(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
+{
+  ClsArgs a;
+  int rc = classifyPrepare(c, p, cls, onDevice, a);
+  if (rc)
+    return rc;
+  memcpy(c->clsArgs, &a, sizeof a);
+  c->clsHost = onDevice ? nullptr : cls;
+  c->clsStaged = true;
+  return 0;
+}
+
+template <int W>
+static cudaError_t ringsGrid(WbBatch *b, bool exact, unsigned *grid)
+{
+  int per = 0;
+  cudaError_t e = exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batchRings<true, W>, 32 * W, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batchRings<false, W>, 32 * W, 0);
+  *grid = (unsigned)(b->sm * (per > 0 ? per : 1));
+  return e;
+}
+
+template <int W>
+static void launchRings(WbBatch *b, cudaStream_t s, bool exact, unsigned grid)
+{
+  if (exact)
+    batchRings<true, W><<<grid, 32 * W, 0, s>>>(b->dIn, b->dOut);
+  else
+    batchRings<false, W><<<grid, 32 * W, 0, s>>>(b->dIn, b->dOut);
+}
+
+/* Captures the fused classify: upload of the job table, set-up, the
+ * persistent fast pass, the ambiguous prefix, the persistent exact pass,
+ * ground counts, the class-byte scatter and the read-back of the totals. */
+static cudaError_t captureBatch(WbBatch *b, int warps, cudaGraphExec_t *exec)
+{
+  unsigned gFast = 0, gExact = 0;
+  cudaError_t e = warps == 2 ? ringsGrid<2>(b, false, &gFast) : warps == 8 ? ringsGrid<8>(b, false, &gFast)
+                                                                            : ringsGrid<4>(b, false, &gFast);
+  if (e == cudaSuccess)
+    e = ringsGrid<4>(b, true, &gExact);
+  if (e != cudaSuccess)
+    return e;
+  cudaStream_t s = b->capture;
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess)
+    return e;
+  const unsigned grid = (unsigned)b->sm * 8;
+  cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
+  batchSetup<<<grid, 256, 0, s>>>(b->dIn);
+  if (warps == 2)
+    launchRings<2>(b, s, false, gFast);
+  else if (warps == 8)
+    launchRings<8>(b, s, false, gFast);
+  else
+    launchRings<4>(b, s, false, gFast);
+  batchAmbPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut);
+  launchRings<4>(b, s, true, gExact);
+  batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
+  batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
+  batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
+  batchScatter<<<grid, 256, 0, s>>>(b->dIn);
+  cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDeviceToHost, s);
+  cudaError_t le = cudaGetLastError();
+  e = cudaStreamEndCapture(s, &graph);
+  if (e == cudaSuccess && le != cudaSuccess)
+    e = le;
+  if (e == cudaSuccess)
+    e = cudaGraphInstantiate(exec, graph, 0);
+  if (graph)
+    cudaGraphDestroy(graph);
+  return e;
+}
+
+int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int warps, int chunk,
+                    uint64_t *launches, std::string &err)
+{
+  if (k < 1 || k > WB_BATCH_MAX)
+  {
+    err = "wb_batch_launch: between 1 and " + std::to_string(WB_BATCH_MAX) + " jobs per launch";
+    return WB_EINVAL;
+  }
+  if (warps != 2 && warps != 4 && warps != 8)
+    warps = 4;
+  if (chunk < 1)
+    chunk = 16;
+  BatchHdr *h = b->hIn;
+  h->k = k;
+  h->chunk = chunk;
+  h->next[0] = h->next[1] = 0;
+  h->startNd[0] = h->startN[0] = h->startT[0] = 0;
+  for (int q = 0; q < k; q++)
+  {
+    wb_ctx *c = jobs[q];
+    if (!c->clsStaged)
+    {
+      err = "wb_batch_launch: job " + std::to_string(q) + " was not staged";
+      return WB_ESTATE;
+    }
+    memcpy(&h->jobs[q], c->clsArgs, sizeof(ClsArgs));
+    h->startNd[q + 1] = h->startNd[q] + c->nd;
+    h->startN[q + 1] = h->startN[q] + c->n;
+    h->startT[q + 1] = h->startT[q] + c->n_tiles;
+  }
+  cudaGraphExec_t exec = nullptr;
+  for (auto &g : b->graphs)
+    if (g.warps == warps && g.chunk == 0)
+      exec = g.exec;
+  cudaSetDevice(b->device);
+  if (!exec)
+  {
+    cudaError_t e = captureBatch(b, warps, &exec);
+    if (e != cudaSuccess)
+    {
+      cudaGetLastError();
+      err = std::string("wb_batch_launch: graph capture: ") + cudaGetErrorString(e);
+      return WB_ECUDA;
+    }
+    b->graphs.push_back({warps, 0, exec});
+  }
+  cudaError_t e = cudaGraphLaunch(exec, s);
+  for (int q = 0; q < k && e == cudaSuccess; q++)
+  {
+    wb_ctx *c = jobs[q];
+    ClsArgs *a = (ClsArgs *)c->clsArgs;
+    if (c->clsHost && c->n)
+      e = cudaMemcpyAsync(c->clsHost, a->cls, c->n, cudaMemcpyDeviceToHost, s);
+  }
+  if (e != cudaSuccess)
+  {
+    err = std::string("wb_batch_launch: ") + cudaGetErrorString(e);
+    return WB_ECUDA;
+  }
+  if (launches)
+    *launches += 8;   /* kernel nodes of the graph */
+  return 0;
+}
+
+void wb_batch_collect(WbBatch *b, wb_ctx *const *jobs, int k)
+{
+  for (int q = 0; q < k; q++)
+  {
+    wb_ctx *c = jobs[q];
+    c->n_ambiguous = b->hOut->startAmb[q + 1] - b->hOut->startAmb[q];
+    c->n_ground = b->hOut->ground[q];
+    c->clsStaged = false;
+    c->clsHost = nullptr;
+    c->stage = 3;
+  }
 }

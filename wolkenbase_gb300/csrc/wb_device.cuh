@@ -45,7 +45,9 @@ __device__ __forceinline__ double wb_decode(int32_t q, double off, double scale,
 __device__ __forceinline__ uint32_t wb_cell_index(double x, double lo, double cell)
 {
   const int kMax = (1 << WB_LEVELS) - 1;
-  double t = (x - lo) / cell;
+  // cell = root side / 2^21 and the root side is a power of two, so the
+  // product with its reciprocal is the exact quotient (no FP64 division)
+  double t = (x - lo) * (1.0 / cell);
   int k;
   if (!(t > 0))
     k = 0;

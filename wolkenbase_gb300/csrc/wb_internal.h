@@ -3,6 +3,7 @@
 #ifndef WB_INTERNAL_H
 #define WB_INTERNAL_H
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -44,7 +45,8 @@ struct wb_ctx
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  size_t budget = 0, used = 0;
+  size_t budget = 0;
+  std::atomic<size_t> used{0};      /* device bytes held (read by a server's scheduler) */
   std::string err;
   int sm_count = 0;
   uint64_t launches = 0;            /* kernels launched by this context */
@@ -72,6 +74,12 @@ struct wb_ctx
   int flowIdxCached = -1;
   int lookupX0 = 0, lookupY0 = 0, lookupW = 0, lookupH = 0;
 
+  /* classify arguments formed by wb_classify_stage for a fused launch */
+  alignas(16) unsigned char clsArgs[768];
+  bool clsStaged = false;
+  uint8_t *clsHost = nullptr;       /* host destination of the class bytes, or NULL */
+  uint64_t n_ground = 0;
+
   /* profiling */
   bool profile = false;
   std::vector<const char *> evNames;
@@ -98,6 +106,8 @@ int wb_fail(wb_ctx *c, int code, const std::string &msg);
   } while (0)
 
 int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes);
+void wb_free_buf(wb_ctx *c, DevBuf &b);   /* stream-ordered free */
+void wb_release_buffers(wb_ctx *c);       /* frees every buffer of c */
 void wb_mark(wb_ctx *c, const char *name);   /* profiling event after a stage */
 
 /* host geometry (wb_geom.cpp) */
@@ -117,5 +127,15 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1);
 int wb_scan_impl(wb_ctx *c, const wb_params *p);
 int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice);
 int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf);
+
+/* fused classify of many jobs in one captured graph (wb_classify.cu) */
+#define WB_BATCH_MAX 512
+struct WbBatch;
+int wb_batch_create(int device, WbBatch **out, std::string &err);
+void wb_batch_destroy(WbBatch *b);
+int wb_classify_stage(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice);
+int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int warps, int chunk,
+                    uint64_t *launches, std::string &err);
+void wb_batch_collect(WbBatch *b, wb_ctx *const *jobs, int k);
 
 #endif

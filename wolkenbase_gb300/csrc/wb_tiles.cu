@@ -902,7 +902,8 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   uint32_t *dBig = (uint32_t *)((char *)c->small.p + 392);
   if ((rc = wb_ensure(c, c->tileNg, T * 4 + 64)))
     return rc;
-  WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 8, c->stream));
+  // overflow flag and big-tile count (bytes 384..395 of the scratch block)
+  WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 16, c->stream));
   { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
                                                            (uint32_t *)c->tileNg.p, dBig); ++c->launches; }
   { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,

@@ -251,6 +251,20 @@ def batch_tiles(count=256, lo=50_000, hi=5_000_000, seed0=1000):
     return [(int(sizes[i]), seed0 + i, float(frac[i])) for i in range(count)]
 
 
+def batch_tile(n, seed, nonground):
+    """One tile of the mixed batch: 100 pts/m^2, slopes to 35 degrees."""
+    return density_tile(n, seed, nonground=nonground, max_slope=math.tan(math.radians(35.0)))
+
+
+def serve_requests(count, rate=200.0, lo=10_000, hi=10_000_000, seed=5000):
+    """Poisson arrivals (mean ``rate`` per second) of tile-classify requests:
+    (arrival time in seconds, point count, seed), sizes log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
+    return [(float(t[i]), int(sizes[i]), seed + 1 + i) for i in range(count)]
+
+
 def utm_tile(n=100_000_000, seed=4):
     """UTM-like offsets, 1 cm scale, slopes to 45 degrees with 2 m steps, 100 pts/m^2."""
     side = math.sqrt(n / 100.0)
