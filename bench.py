@@ -174,6 +174,13 @@ def generate(specs, procs=None):
     return out
 
 
+def _tuned(st):
+    from wolkenbase_gb300 import _lib
+    shapes = ["4 warps/6 blocks", "4 warps/8 blocks", "8 warps/3 blocks", "8 warps/4 blocks", "2 warps/12 blocks"]
+    return {"shape": shapes[st["shape"]], "chunk": st["chunk"], "grid_points": st["grid_points"],
+            "tune_ms": st["tune_ms"]}
+
+
 def _pct(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
@@ -225,7 +232,8 @@ def served_form(args, device):
     clf.classify_cloud(big)                       # buffers sized once
     plain_span, plain_lat = plain_pass(clf)
     clf.close()
-    srv = wb.Server(device, prep_slots=args.serve_slots, hbm_budget=int(args.serve_budget_gb * 2**30))
+    srv = wb.Server(device, prep_slots=args.serve_slots, hbm_budget=int(args.serve_budget_gb * 2**30),
+                    autotune=True)
     served_pass(srv)                              # contexts sized once
     launches0 = srv.stats()["kernel_launches"]
     span, lat, sts = served_pass(srv)
@@ -241,7 +249,7 @@ def served_form(args, device):
                        "p99_ms": _pct(lat, 99) * 1e3, "makespan_s": span, "prep_slots": args.serve_slots,
                        "fused_launches": st["fused_launches"], "mean_jobs_per_launch":
                            float(np.mean(batch)), "peak_bytes": st["peak_bytes"],
-                       "gpu_launches": st["kernel_launches"] - launches0},
+                       "gpu_launches": st["kernel_launches"] - launches0, "tuned": _tuned(st)},
             "served_over_plain": (pts / span) / (pts / plain_span)}
 
 
@@ -261,7 +269,7 @@ def batched_form(args, device):
         clf.classify_cloud(c)
     plain_s = time.perf_counter() - t0
     clf.close()
-    srv = wb.Server(device, prep_slots=args.batch_slots, flush=_lib.WB_FLUSH_FULL)
+    srv = wb.Server(device, prep_slots=args.batch_slots, flush=_lib.WB_FLUSH_FULL, autotune=True)
     got = srv.classify_batch(clouds)                              # warm-up, contexts sized
     st0 = srv.stats()
     launches0, fused0 = st0["kernel_launches"], st0["fused_launches"]
@@ -277,7 +285,7 @@ def batched_form(args, device):
             "plain": {"value": pts / plain_s / 1e6, "unit": UNIT, "seconds": plain_s},
             "batched": {"value": pts / batch_s / 1e6, "unit": UNIT, "seconds": batch_s,
                         "fused_launches": st["fused_launches"] - fused0, "prep_slots": args.batch_slots,
-                        "gpu_launches": st["kernel_launches"] - launches0},
+                        "gpu_launches": st["kernel_launches"] - launches0, "tuned": _tuned(st)},
             "batched_over_plain": plain_s / batch_s, "same_labels": same}
 
 

@@ -192,6 +192,10 @@ int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz,
  * hbm_budget; jobs start in submission order. */
 typedef struct wb_server wb_server;
 
+/* Fused fast-pass kernel shapes: warps per block / resident blocks per SM
+ * (register cap): 0 = 4/6, 1 = 4/8, 2 = 8/3, 3 = 8/4, 4 = 2/12. */
+#define WB_N_SHAPES 5
+
 #define WB_FLUSH_EAGER 0   /* classify whatever has been scanned (serving)            */
 #define WB_FLUSH_FULL 1    /* wait until every admitted job is scanned (batching)     */
 
@@ -202,8 +206,12 @@ typedef struct
   uint64_t hbm_budget;   /* bytes all resident jobs may hold; 0 = 80% of free memory */
   int flush;             /* WB_FLUSH_EAGER or WB_FLUSH_FULL                         */
   int max_batch;         /* most jobs in one fused classify launch; 0 = 512 (max)   */
-  int block_warps;       /* warps per block of the fused launch (2, 4, 8); 0 = 4    */
+  int shape;             /* fused fast-pass kernel shape, 0..WB_N_SHAPES-1 (below)  */
   int chunk;             /* points a warp takes per visit to the work counter; 0 = 16 */
+  double grid_points;    /* points per column of the neighbour grid; 0 = 32         */
+  int autotune;          /* 1: on the first batch, time column densities, kernel
+                            shapes and chunks on a sample and keep the fastest     */
+  int pad;
 } wb_server_config;
 
 typedef struct
@@ -243,6 +251,10 @@ typedef struct
   uint64_t kernel_launches;  /* kernels the server's contexts and graphs launched     */
   int contexts, queued, running, pad;
   double now;                /* the server's clock                                    */
+  int tuned;                 /* 1 once the autotuner has run                          */
+  int shape, chunk, pad2;    /* fast-pass shape and chunk in use                      */
+  double grid_points;        /* column density in use                                 */
+  double tune_ms;            /* time the autotuner took                               */
 } wb_server_stats;
 
 wb_server *wb_server_open(const wb_server_config *cfg);   /* NULL on error: wb_last_error(NULL) */

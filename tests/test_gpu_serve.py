@@ -72,15 +72,36 @@ def test_batch_one_fused_launch_equals_alone(clouds_alone):
         srv.close()
 
 
-@pytest.mark.parametrize("warps,chunk", [(2, 1), (8, 64)])
-def test_fused_launch_shapes_agree(clouds_alone, warps, chunk):
+@pytest.mark.parametrize("shape,chunk,grid_points", [(4, 1, 16.0), (3, 64, 48.0), (2, 4, 0.0)])
+def test_fused_launch_shapes_agree(clouds_alone, shape, chunk, grid_points):
+    """Kernel shape, chunk and column density change speed, never labels."""
     import wolkenbase_gb300 as wb
     from wolkenbase_gb300 import _lib
     clouds, alone = clouds_alone
-    srv = wb.Server(0, prep_slots=2, flush=_lib.WB_FLUSH_FULL, block_warps=warps, chunk=chunk)
+    srv = wb.Server(0, prep_slots=2, flush=_lib.WB_FLUSH_FULL, shape=shape, chunk=chunk, grid_points=grid_points)
     try:
         got = srv.classify_batch(clouds[:4])
         for i in range(4):
+            assert np.array_equal(got[i], alone[i])
+    finally:
+        srv.close()
+
+
+def test_autotuner_picks_a_shape_and_keeps_labels(clouds_alone):
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib
+    clouds, alone = clouds_alone
+    srv = wb.Server(0, prep_slots=3, flush=_lib.WB_FLUSH_FULL, autotune=True)
+    try:
+        got = srv.classify_batch(clouds)
+        for i in range(len(clouds)):
+            assert np.array_equal(got[i], alone[i])
+        s = srv.stats()
+        assert s["tuned"] == 1 and 0 <= s["shape"] < _lib.WB_N_SHAPES
+        assert s["chunk"] in (4, 16, 64) and s["grid_points"] in (16, 24, 32, 48, 64)
+        assert s["tune_ms"] > 0
+        got = srv.classify_batch(clouds)          # jobs prepared with the tuned column density
+        for i in range(len(clouds)):
             assert np.array_equal(got[i], alone[i])
     finally:
         srv.close()

@@ -202,9 +202,10 @@ class Server:
     Classifier.classify_cloud on the same cloud."""
 
     def __init__(self, device=0, prep_slots=4, hbm_budget=0, flush=_lib.WB_FLUSH_EAGER, max_batch=0,
-                 block_warps=0, chunk=0):
+                 shape=0, chunk=0, grid_points=0.0, autotune=False):
         self.L = _lib.load()
-        cfg = _lib.wb_server_config(device, prep_slots, hbm_budget, flush, max_batch, block_warps, chunk)
+        cfg = _lib.wb_server_config(device, prep_slots, hbm_budget, flush, max_batch, shape, chunk, grid_points,
+                                    1 if autotune else 0, 0)
         self.s = self.L.wb_server_open(C.byref(cfg))
         if not self.s:
             raise WolkenbaseError(_lib.WB_ECUDA, self.L.wb_last_error(None).decode())
@@ -276,7 +277,7 @@ class Server:
         rc = self.L.wb_server_stats_get(self.s, C.byref(st))
         if rc:
             raise WolkenbaseError(rc, "wb_server_stats_get")
-        return {f: getattr(st, f) for f, _ in st._fields_ if f != "pad"}
+        return {f: getattr(st, f) for f, _ in st._fields_ if not f.startswith("pad")}
 
     def classify_batch(self, clouds, params=None):
         """wb_classify_batch over a list of clouds; returns their class bytes."""

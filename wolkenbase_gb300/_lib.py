@@ -46,9 +46,13 @@ class wb_tile(C.Structure):
                 ("hyperboloid_size", C.c_double), ("height", C.c_double)]
 
 
+WB_N_SHAPES = 5
+
+
 class wb_server_config(C.Structure):
     _fields_ = [("device", C.c_int), ("prep_slots", C.c_int), ("hbm_budget", C.c_uint64), ("flush", C.c_int),
-                ("max_batch", C.c_int), ("block_warps", C.c_int), ("chunk", C.c_int)]
+                ("max_batch", C.c_int), ("shape", C.c_int), ("chunk", C.c_int), ("grid_points", C.c_double),
+                ("autotune", C.c_int), ("pad", C.c_int)]
 
 
 class wb_job(C.Structure):
@@ -67,7 +71,9 @@ class wb_server_stats(C.Structure):
                 ("cancelled", C.c_uint64), ("points", C.c_uint64), ("fused_launches", C.c_uint64),
                 ("fused_jobs", C.c_uint64), ("held_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
                 ("budget", C.c_uint64), ("kernel_launches", C.c_uint64), ("contexts", C.c_int),
-                ("queued", C.c_int), ("running", C.c_int), ("pad", C.c_int), ("now", C.c_double)]
+                ("queued", C.c_int), ("running", C.c_int), ("pad", C.c_int), ("now", C.c_double),
+                ("tuned", C.c_int), ("shape", C.c_int), ("chunk", C.c_int), ("pad2", C.c_int),
+                ("grid_points", C.c_double), ("tune_ms", C.c_double)]
 
 
 # name -> (restype, argtypes); every symbol include/wolkenbase_gb300.h declares

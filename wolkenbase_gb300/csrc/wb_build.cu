@@ -624,6 +624,10 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   { nodeLinkKernel<<<gridFor(c, L), 256, 0, c->stream>>>(L, D, leafLev, leafKey, flag, flagEx, child, box, nbox, N); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "nodes");
+  c->grid_bounds[0] = mn[0];
+  c->grid_bounds[1] = mn[1];
+  c->grid_bounds[2] = mx[0];
+  c->grid_bounds[3] = mx[1];
   if ((rc = wb_grid_impl(c, mn[0], mn[1], mx[0], mx[1])))
     return rc;
   wb_mark(c, "grid");

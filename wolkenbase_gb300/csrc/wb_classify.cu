@@ -827,8 +827,8 @@ __global__ void batchSetup(const BatchHdr *__restrict__ h)
   }
 }
 
-template <bool EXACT, int W>
-__global__ void __launch_bounds__(32 * W) batchRings(BatchHdr *h, const BatchOut *o)
+template <bool EXACT, int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) batchRings(BatchHdr *h, const BatchOut *o)
 {
   __shared__ uint32_t bmin[W][kBins], bmax[W][kBins];
   __shared__ ClsArgs sa[W];
@@ -958,7 +958,7 @@ struct WbBatch
   BatchOut *dOut = nullptr, *hOut = nullptr;
   struct Graph
   {
-    int warps, chunk;
+    int shape;
     cudaGraphExec_t exec;
   };
   std::vector<Graph> graphs;
@@ -1021,53 +1021,73 @@ int wb_classify_stage(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   return 0;
 }
 
-template <int W>
-static cudaError_t ringsGrid(WbBatch *b, bool exact, unsigned *grid)
+const WbShape kWbShapes[WB_N_SHAPES] = {{4, 6}, {4, 8}, {8, 3}, {8, 4}, {2, 12}};
+
+namespace
 {
-  int per = 0;
-  cudaError_t e = exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batchRings<true, W>, 32 * W, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batchRings<false, W>, 32 * W, 0);
-  *grid = (unsigned)(b->sm * (per > 0 ? per : 1));
-  return e;
+typedef void (*RingsFn)(BatchHdr *, const BatchOut *);
+
+RingsFn ringsFn(int shape, bool exact)
+{
+  // kWbShapes: about 85 or 64 registers a thread
+  if (exact)
+    return batchRings<true, 4, 6>;
+  switch (shape)
+  {
+  case 1: return batchRings<false, 4, 8>;
+  case 2: return batchRings<false, 8, 3>;
+  case 3: return batchRings<false, 8, 4>;
+  case 4: return batchRings<false, 2, 12>;
+  default: return batchRings<false, 4, 6>;
+  }
 }
 
-template <int W>
-static void launchRings(WbBatch *b, cudaStream_t s, bool exact, unsigned grid)
+/* Persistent grid of a ring kernel: every SM filled to its occupancy. */
+cudaError_t ringsLaunch(WbBatch *b, cudaStream_t s, int shape, bool exact)
 {
-  if (exact)
-    batchRings<true, W><<<grid, 32 * W, 0, s>>>(b->dIn, b->dOut);
-  else
-    batchRings<false, W><<<grid, 32 * W, 0, s>>>(b->dIn, b->dOut);
+  RingsFn fn = ringsFn(shape, exact);
+  int warps = exact ? 4 : kWbShapes[shape].warps;
+  int per = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32 * warps, 0);
+  if (e != cudaSuccess)
+    return e;
+  unsigned grid = (unsigned)(b->sm * (per > 0 ? per : 1));
+  fn<<<grid, 32 * warps, 0, s>>>(b->dIn, b->dOut);
+  return cudaGetLastError();
 }
+
+__global__ void batchAmbReset(const BatchHdr *__restrict__ h)
+{
+  for (int q = threadIdx.x; q < h->k; q += blockDim.x)
+    *h->jobs[q].ambCount = 0;
+}
+}  // namespace
 
 /* Captures the fused classify: upload of the job table, set-up, the
  * persistent fast pass, the ambiguous prefix, the persistent exact pass,
  * ground counts, the class-byte scatter and the read-back of the totals. */
-static cudaError_t captureBatch(WbBatch *b, int warps, cudaGraphExec_t *exec)
+static cudaError_t captureBatch(WbBatch *b, int shape, cudaGraphExec_t *exec)
 {
-  unsigned gFast = 0, gExact = 0;
-  cudaError_t e = warps == 2 ? ringsGrid<2>(b, false, &gFast) : warps == 8 ? ringsGrid<8>(b, false, &gFast)
-                                                                            : ringsGrid<4>(b, false, &gFast);
-  if (e == cudaSuccess)
-    e = ringsGrid<4>(b, true, &gExact);
-  if (e != cudaSuccess)
-    return e;
   cudaStream_t s = b->capture;
   cudaGraph_t graph = nullptr;
+  // occupancy queries are not stream work: resolve the grids before capturing
+  int per[2] = {0, 0};
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], ringsFn(shape, false),
+                                                                32 * kWbShapes[shape].warps, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], ringsFn(shape, true), 128, 0);
+  if (e != cudaSuccess)
+    return e;
   e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess)
     return e;
   const unsigned grid = (unsigned)b->sm * 8;
   cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
   batchSetup<<<grid, 256, 0, s>>>(b->dIn);
-  if (warps == 2)
-    launchRings<2>(b, s, false, gFast);
-  else if (warps == 8)
-    launchRings<8>(b, s, false, gFast);
-  else
-    launchRings<4>(b, s, false, gFast);
+  ringsFn(shape, false)<<<(unsigned)(b->sm * (per[0] > 0 ? per[0] : 1)), 32 * kWbShapes[shape].warps, 0, s>>>(
+      b->dIn, b->dOut);
   batchAmbPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut);
-  launchRings<4>(b, s, true, gExact);
+  ringsFn(shape, true)<<<(unsigned)(b->sm * (per[1] > 0 ? per[1] : 1)), 128, 0, s>>>(b->dIn, b->dOut);
   batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
   batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
   batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
@@ -1084,21 +1104,18 @@ static cudaError_t captureBatch(WbBatch *b, int warps, cudaGraphExec_t *exec)
   return e;
 }
 
-int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int warps, int chunk,
-                    uint64_t *launches, std::string &err)
+/* Fills the pinned job table from the staged contexts; with sample > 0 the
+ * point ranges are cut after the first `sample` points. */
+static int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample, std::string &err)
 {
   if (k < 1 || k > WB_BATCH_MAX)
   {
-    err = "wb_batch_launch: between 1 and " + std::to_string(WB_BATCH_MAX) + " jobs per launch";
+    err = "between 1 and " + std::to_string(WB_BATCH_MAX) + " jobs per launch";
     return WB_EINVAL;
   }
-  if (warps != 2 && warps != 4 && warps != 8)
-    warps = 4;
-  if (chunk < 1)
-    chunk = 16;
   BatchHdr *h = b->hIn;
   h->k = k;
-  h->chunk = chunk;
+  h->chunk = chunk < 1 ? 16 : chunk;
   h->next[0] = h->next[1] = 0;
   h->startNd[0] = h->startN[0] = h->startT[0] = 0;
   for (int q = 0; q < k; q++)
@@ -1106,29 +1123,82 @@ int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int 
     wb_ctx *c = jobs[q];
     if (!c->clsStaged)
     {
-      err = "wb_batch_launch: job " + std::to_string(q) + " was not staged";
+      err = "job " + std::to_string(q) + " was not staged";
       return WB_ESTATE;
     }
     memcpy(&h->jobs[q], c->clsArgs, sizeof(ClsArgs));
-    h->startNd[q + 1] = h->startNd[q] + c->nd;
+    uint64_t nd = c->nd;
+    if (sample && h->startNd[q] + nd > sample)
+      nd = sample > h->startNd[q] ? sample - h->startNd[q] : 0;
+    h->startNd[q + 1] = h->startNd[q] + nd;
     h->startN[q + 1] = h->startN[q] + c->n;
     h->startT[q + 1] = h->startT[q] + c->n_tiles;
   }
+  return 0;
+}
+
+int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int shape, int chunk, cudaStream_t s,
+                  float *ms, std::string &err)
+{
+  if (shape < 0 || shape >= WB_N_SHAPES)
+    shape = 0;
+  int rc = fillTable(b, jobs, k, chunk, sample, err);
+  if (rc)
+    return rc;
+  cudaSetDevice(b->device);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess)
+    e = cudaEventCreate(&e1);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+  {
+    batchSetup<<<(unsigned)b->sm * 8, 256, 0, s>>>(b->dIn);
+    cudaEventRecord(e0, s);
+    e = ringsLaunch(b, s, shape, false);
+    cudaEventRecord(e1, s);
+    batchAmbReset<<<1, 256, 0, s>>>(b->dIn);
+  }
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess)
+    e = cudaEventElapsedTime(ms, e0, e1);
+  if (e0)
+    cudaEventDestroy(e0);
+  if (e1)
+    cudaEventDestroy(e1);
+  if (e != cudaSuccess)
+  {
+    err = std::string("wb_batch_time: ") + cudaGetErrorString(e);
+    return WB_ECUDA;
+  }
+  return 0;
+}
+
+int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int shape, int chunk,
+                    uint64_t *launches, std::string &err)
+{
+  if (shape < 0 || shape >= WB_N_SHAPES)
+    shape = 0;
+  int rc = fillTable(b, jobs, k, chunk, 0, err);
+  if (rc)
+    return rc;
   cudaGraphExec_t exec = nullptr;
   for (auto &g : b->graphs)
-    if (g.warps == warps && g.chunk == 0)
+    if (g.shape == shape)
       exec = g.exec;
   cudaSetDevice(b->device);
   if (!exec)
   {
-    cudaError_t e = captureBatch(b, warps, &exec);
+    cudaError_t e = captureBatch(b, shape, &exec);
     if (e != cudaSuccess)
     {
       cudaGetLastError();
       err = std::string("wb_batch_launch: graph capture: ") + cudaGetErrorString(e);
       return WB_ECUDA;
     }
-    b->graphs.push_back({warps, 0, exec});
+    b->graphs.push_back({shape, exec});
   }
   cudaError_t e = cudaGraphLaunch(exec, s);
   for (int q = 0; q < k && e == cudaSuccess; q++)

@@ -189,8 +189,8 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   uint64_t nd = c->nd;
   WbGeom &g = c->g;
   double w = fmax(x1 - x0, 1e-9), h = fmax(y1 - y0, 1e-9);
-  // about 32 points per occupied column, at most 2^24 columns
-  double cell = sqrt(w * h * 32.0 / (double)(nd ? nd : 1));
+  // about grid_points points per occupied column, at most 2^24 columns
+  double cell = sqrt(w * h * c->grid_points / (double)(nd ? nd : 1));
   double minCell = sqrt(w * h / (double)(1u << 24));
   if (cell < minCell)
     cell = minCell;

@@ -69,6 +69,8 @@ struct wb_ctx
   DevBuf label, clsDev, ambiguous, angleT;
   DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox, cellFlag, ptSetup;
   GridInfo grid;
+  double grid_points = 32;          /* target points per occupied column (autotuned by a server) */
+  double grid_bounds[4] = {0, 0, 0, 0};   /* x0, y0, x1, y1 the column grid spans */
   DevBuf flowCache;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
   int flowIdxCached = -1;
@@ -134,8 +136,20 @@ struct WbBatch;
 int wb_batch_create(int device, WbBatch **out, std::string &err);
 void wb_batch_destroy(WbBatch *b);
 int wb_classify_stage(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice);
-int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int warps, int chunk,
+int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int shape, int chunk,
                     uint64_t *launches, std::string &err);
 void wb_batch_collect(WbBatch *b, wb_ctx *const *jobs, int k);
+/* Kernel shapes of the fused fast pass: warps per block and a register cap
+ * (minimum resident blocks per SM, 0 = none). */
+struct WbShape
+{
+  int warps, minBlocks;
+};
+extern const WbShape kWbShapes[WB_N_SHAPES];
+/* Times the fused fast pass alone over the first `sample` points of the
+ * staged jobs (set-up included, untimed); the jobs' ambiguous lists are
+ * cleared afterwards, so the batch can be launched normally. */
+int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int shape, int chunk, cudaStream_t s,
+                  float *ms, std::string &err);
 
 #endif

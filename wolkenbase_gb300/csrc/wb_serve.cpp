@@ -190,9 +190,10 @@ void finish(wb_server *s, JobRec *j, int rc, const std::string &msg)
   }
 }
 
-int runPrep(JobRec *j, wb_ctx *c)
+int runPrep(JobRec *j, wb_ctx *c, double gridPoints)
 {
   c->budget = std::max<uint64_t>(c->used, j->est);
+  c->grid_points = gridPoints;
   int rc = wb_build_impl(c, &j->spec.cloud);
   if (rc == 0)
     rc = wb_scan_impl(c, &j->spec.params);
@@ -224,8 +225,9 @@ void prepLoop(wb_server *s)
     j->st.reserved_bytes = j->est;
     s->prepBusy++;
     s->stats.peak_bytes = std::max<uint64_t>(s->stats.peak_bytes, heldBytes(s));
+    double gp = s->cfg.grid_points;
     lk.unlock();
-    int rc = runPrep(j, c);
+    int rc = runPrep(j, c, gp);
     std::string msg = rc ? c->err : std::string();
     lk.lock();
     s->prepBusy--;
@@ -262,6 +264,82 @@ bool flushNow(const wb_server *s)
   return s->prepBusy == 0 && (s->queue.empty() || s->headBlocked);
 }
 
+/* The autotuner (first batch, classifier thread, lock not held).  On the
+ * batch's largest job it times the fused fast pass over a sample of up to
+ * 2M points: first each column density (the job's grid is rebuilt for each),
+ * then each kernel shape, then each chunk size, keeping the fastest of each
+ * (coordinate descent).  Labels do not depend on any of these choices. */
+void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk, double &gridPoints)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  JobRec *big = batch[0];
+  for (JobRec *j : batch)
+    if (j->ctx->nd > big->ctx->nd)
+      big = j;
+  wb_ctx *c = big->ctx;
+  const uint64_t sample = std::min<uint64_t>(c->nd, 2000000);
+  std::string err;
+  auto timeIt = [&](int sh, int ch) -> float {
+    float ms = 0;
+    if (wb_batch_time(s->batch, &c, 1, sample, sh, ch, s->clsStream, &ms, err))
+      return 1e30f;
+    return ms;
+  };
+  auto regrid = [&](double gp) -> bool {
+    c->grid_points = gp;
+    const double *b = c->grid_bounds;
+    return wb_grid_impl(c, b[0], b[1], b[2], b[3]) == 0 &&
+           wb_classify_stage(c, &big->spec.params, big->spec.cls, 0) == 0 &&
+           cudaStreamSynchronize(c->stream) == cudaSuccess;
+  };
+  timeIt(shape, chunk);   // warm-up
+  static const double kDensity[] = {16, 24, 32, 48, 64};
+  double bestGp = gridPoints;
+  float best = timeIt(shape, chunk);
+  for (double gp : kDensity)
+  {
+    if (gp == gridPoints || !regrid(gp))
+      continue;
+    float t = timeIt(shape, chunk);
+    if (t < best)
+    {
+      best = t;
+      bestGp = gp;
+    }
+  }
+  if (c->grid_points != bestGp)
+    regrid(bestGp);
+  int bestShape = shape;
+  for (int sh = 0; sh < WB_N_SHAPES; sh++)
+  {
+    if (sh == shape)
+      continue;
+    float t = timeIt(sh, chunk);
+    if (t < best)
+    {
+      best = t;
+      bestShape = sh;
+    }
+  }
+  int bestChunk = chunk;
+  static const int kChunk[] = {4, 16, 64};
+  for (int ch : kChunk)
+  {
+    if (ch == chunk)
+      continue;
+    float t = timeIt(bestShape, ch);
+    if (t < best)
+    {
+      best = t;
+      bestChunk = ch;
+    }
+  }
+  shape = bestShape;
+  chunk = bestChunk;
+  gridPoints = bestGp;
+  s->stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 void classifyLoop(wb_server *s)
 {
   cudaSetDevice(s->cfg.device);
@@ -287,9 +365,20 @@ void classifyLoop(wb_server *s)
     for (JobRec *j : batch)
       if (cudaStreamWaitEvent(s->clsStream, j->ev, 0) != cudaSuccess)
         rc = WB_ECUDA;
+    if (rc == 0 && s->cfg.autotune && !s->stats.tuned)
+    {
+      int shape = s->cfg.shape, chunk = s->cfg.chunk;
+      double gp = s->cfg.grid_points;
+      autotune(s, batch, shape, chunk, gp);
+      std::lock_guard<std::mutex> g(s->m);
+      s->cfg.shape = shape;
+      s->cfg.chunk = chunk;
+      s->cfg.grid_points = gp;
+      s->stats.tuned = 1;
+    }
     uint64_t launches = 0;
     if (rc == 0)
-      rc = wb_batch_launch(s->batch, ctxs.data(), k, s->clsStream, s->cfg.block_warps, s->cfg.chunk, &launches, err);
+      rc = wb_batch_launch(s->batch, ctxs.data(), k, s->clsStream, s->cfg.shape, s->cfg.chunk, &launches, err);
     if (rc == 0)
     {
       cudaError_t e = cudaStreamSynchronize(s->clsStream);
@@ -347,8 +436,10 @@ wb_server *wb_server_open(const wb_server_config *cfg)
     s->cfg.prep_slots = 4;
   if (s->cfg.max_batch <= 0 || s->cfg.max_batch > WB_BATCH_MAX)
     s->cfg.max_batch = WB_BATCH_MAX;
-  if (s->cfg.block_warps != 2 && s->cfg.block_warps != 8)
-    s->cfg.block_warps = 4;
+  if (s->cfg.shape < 0 || s->cfg.shape >= WB_N_SHAPES)
+    s->cfg.shape = 0;
+  if (!(s->cfg.grid_points > 0))
+    s->cfg.grid_points = 32;
   if (s->cfg.chunk <= 0)
     s->cfg.chunk = 16;
   size_t freeB = 0, totalB = 0;
@@ -550,6 +641,9 @@ int wb_server_stats_get(wb_server *s, wb_server_stats *out)
     l += c->launches;
   out->kernel_launches = l;
   out->now = s->now();
+  out->shape = s->cfg.shape;
+  out->chunk = s->cfg.chunk;
+  out->grid_points = s->cfg.grid_points;
   return 0;
 }
 
