@@ -176,7 +176,7 @@ def generate(specs, procs=None):
 
 def _tuned(st):
     from wolkenbase_gb300 import _lib
-    shapes = ["4 warps/6 blocks", "4 warps/8 blocks", "8 warps/3 blocks", "8 warps/4 blocks", "2 warps/12 blocks"]
+    shapes = ["8 warps/3 blocks", "4 warps/6 blocks", "4 warps/8 blocks", "8 warps/4 blocks", "2 warps/12 blocks"]
     return {"shape": shapes[st["shape"]], "chunk": st["chunk"], "grid_points": st["grid_points"],
             "tune_ms": st["tune_ms"]}
 

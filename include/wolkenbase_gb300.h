@@ -36,6 +36,10 @@ extern "C" {
 #define WB_EBUSY -8       /* job already running or finished (wb_cancel)     */
 #define WB_ECANCELED -9   /* job was cancelled before it ran                 */
 
+/* Classify kernel shapes: warps per block / resident blocks per SM
+ * (register cap): 0 = 8/3 (default), 1 = 4/6, 2 = 4/8, 3 = 8/4, 4 = 2/12. */
+#define WB_N_SHAPES 5
+
 typedef struct wb_ctx wb_ctx;
 
 /* Classification settings; defaults as MainWindow::readSettings
@@ -156,6 +160,24 @@ int wb_classify(wb_ctx *ctx, const wb_params *params, uint8_t *cls, int cls_on_d
 /* Build + scan + postscan + classify in one call. */
 int wb_classify_cloud(wb_ctx *ctx, const wb_cloud *cloud, const wb_params *params, uint8_t *cls);
 
+/* Settings of the classify kernel (no reference counterpart; they change
+ * speed, never labels): the kernel shape (see WB_N_SHAPES), the points a
+ * warp takes per visit to the work counter, and the points per column of
+ * the neighbour grid (applies from the next wb_octree_build).  In
+ * wb_set_tuning, a negative shape or a zero chunk/grid_points keeps the
+ * current value.  wb_autotune times the candidates on the scanned cloud
+ * (a sample of up to 2M points), keeps the fastest, and rebuilds the grid
+ * with the chosen density. */
+typedef struct
+{
+  int shape;
+  int chunk;
+  double grid_points;
+} wb_tuning;
+int wb_set_tuning(wb_ctx *ctx, const wb_tuning *t);
+int wb_get_tuning(wb_ctx *ctx, wb_tuning *t);
+int wb_autotune(wb_ctx *ctx, const wb_params *params);
+
 /* Timing of the last pipeline run, per stage, from CUDA events on the
  * context's stream (milliseconds).  names/ms arrays of capacity entries;
  * returns the number of stages via *count. */
@@ -192,10 +214,6 @@ int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz,
  * hbm_budget; jobs start in submission order. */
 typedef struct wb_server wb_server;
 
-/* Fused fast-pass kernel shapes: warps per block / resident blocks per SM
- * (register cap): 0 = 4/6, 1 = 4/8, 2 = 8/3, 3 = 8/4, 4 = 2/12. */
-#define WB_N_SHAPES 5
-
 #define WB_FLUSH_EAGER 0   /* classify whatever has been scanned (serving)            */
 #define WB_FLUSH_FULL 1    /* wait until every admitted job is scanned (batching)     */
 
@@ -207,8 +225,8 @@ typedef struct
   int flush;             /* WB_FLUSH_EAGER or WB_FLUSH_FULL                         */
   int max_batch;         /* most jobs in one fused classify launch; 0 = 512 (max)   */
   int shape;             /* fused fast-pass kernel shape, 0..WB_N_SHAPES-1 (below)  */
-  int chunk;             /* points a warp takes per visit to the work counter; 0 = 16 */
-  double grid_points;    /* points per column of the neighbour grid; 0 = 32         */
+  int chunk;             /* points a warp takes per visit to the work counter; 0 = 4 */
+  double grid_points;    /* points per column of the neighbour grid; 0 = 64         */
   int autotune;          /* 1: on the first batch, time column densities, kernel
                             shapes and chunks on a sample and keep the fastest     */
   int pad;

@@ -91,8 +91,17 @@ def test_autotuner_picks_a_shape_and_keeps_labels(clouds_alone):
     import wolkenbase_gb300 as wb
     from wolkenbase_gb300 import _lib
     clouds, alone = clouds_alone
+    from wolkenbase_gb300 import synth
     srv = wb.Server(0, prep_slots=3, flush=_lib.WB_FLUSH_FULL, autotune=True)
     try:
+        got = srv.classify_batch(clouds)
+        for i in range(len(clouds)):
+            assert np.array_equal(got[i], alone[i])
+        assert srv.stats()["tuned"] == 0          # no job large enough to time yet
+        clouds = clouds + [synth.batch_tile(1_100_000, 909, 0.2)]
+        clf = wb.Classifier(0)
+        alone = alone + [clf.classify_cloud(clouds[-1])]
+        clf.close()
         got = srv.classify_batch(clouds)
         for i in range(len(clouds)):
             assert np.array_equal(got[i], alone[i])
@@ -105,6 +114,24 @@ def test_autotuner_picks_a_shape_and_keeps_labels(clouds_alone):
             assert np.array_equal(got[i], alone[i])
     finally:
         srv.close()
+
+
+def test_classifier_tuning_keeps_labels(clouds_alone):
+    import wolkenbase_gb300 as wb
+    clouds, alone = clouds_alone
+    clf = wb.Classifier(0)
+    try:
+        clf.set_tuning(shape=3, chunk=16, grid_points=24.0)
+        assert clf.tuning() == {"shape": 3, "chunk": 16, "grid_points": 24.0}
+        assert np.array_equal(clf.classify_cloud(clouds[2]), alone[2])
+        clf.build(clouds[5])
+        clf.scan()
+        t = clf.autotune()
+        assert 0 <= t["shape"] < 5 and t["chunk"] in (4, 16, 64) and t["grid_points"] in (16, 24, 32, 48, 64)
+        assert np.array_equal(clf.classify(), alone[5])
+        assert np.array_equal(clf.classify_cloud(clouds[0]), alone[0])
+    finally:
+        clf.close()
 
 
 def test_admission_keeps_within_budget(clouds_alone):

@@ -178,6 +178,22 @@ class Classifier:
         self._check(self.L.wb_classify_cloud(self.ctx, C.byref(cs), C.byref(p), cls.ctypes.data))
         return cls
 
+    # -- kernel settings (speed only; labels do not depend on them) --
+    def tuning(self):
+        t = _lib.wb_tuning()
+        self._check(self.L.wb_get_tuning(self.ctx, C.byref(t)))
+        return {"shape": t.shape, "chunk": t.chunk, "grid_points": t.grid_points}
+
+    def set_tuning(self, shape=-1, chunk=0, grid_points=0.0):
+        t = _lib.wb_tuning(shape, chunk, grid_points)
+        self._check(self.L.wb_set_tuning(self.ctx, C.byref(t)))
+
+    def autotune(self, params=None):
+        """Times the classify kernel's settings on the scanned cloud and keeps the fastest."""
+        p = (params or Params()).c()
+        self._check(self.L.wb_autotune(self.ctx, C.byref(p)))
+        return self.tuning()
+
     # -- profiling --
     def profile(self, enable=True):
         self._check(self.L.wb_profile(self.ctx, 1 if enable else 0))

@@ -49,6 +49,10 @@ class wb_tile(C.Structure):
 WB_N_SHAPES = 5
 
 
+class wb_tuning(C.Structure):
+    _fields_ = [("shape", C.c_int), ("chunk", C.c_int), ("grid_points", C.c_double)]
+
+
 class wb_server_config(C.Structure):
     _fields_ = [("device", C.c_int), ("prep_slots", C.c_int), ("hbm_budget", C.c_uint64), ("flush", C.c_int),
                 ("max_batch", C.c_int), ("shape", C.c_int), ("chunk", C.c_int), ("grid_points", C.c_double),
@@ -100,6 +104,9 @@ SIGNATURES = {
     "wb_check_atan2i": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_check_hypot": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_check_hyperboloid": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),
+    "wb_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),
+    "wb_autotune": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
     "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
     "wb_server_close": (None, [C.c_void_p]),
     "wb_server_error": (C.c_char_p, [C.c_void_p]),

@@ -157,6 +157,7 @@ void wb_close(wb_ctx *c)
     cudaEventDestroy(e);
   wb_release_buffers(c);
   cudaStreamSynchronize(c->stream);
+  wb_batch_destroy(c->batch);
   if (c->own_stream && c->stream)
     cudaStreamDestroy(c->stream);
   delete c;
@@ -405,6 +406,58 @@ int wb_classify(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   }
   endRun(c);
   return rc;
+}
+
+int wb_set_tuning(wb_ctx *c, const wb_tuning *t)
+{
+  if (!c || !t)
+    return WB_EINVAL;
+  if (t->shape >= WB_N_SHAPES || t->shape < -1 || t->chunk < 0 || t->grid_points < 0)
+    return wb_fail(c, WB_EINVAL, "wb_set_tuning: shape in 0..WB_N_SHAPES-1 (or -1), chunk and grid_points >= 0");
+  if (t->shape >= 0)
+    c->shape = t->shape;
+  if (t->chunk > 0)
+    c->chunk = t->chunk;
+  if (t->grid_points > 0)
+    c->grid_points = t->grid_points;
+  return 0;
+}
+
+int wb_get_tuning(wb_ctx *c, wb_tuning *t)
+{
+  if (!c || !t)
+    return WB_EINVAL;
+  t->shape = c->shape;
+  t->chunk = c->chunk;
+  t->grid_points = c->grid_points;
+  return 0;
+}
+
+int wb_autotune(wb_ctx *c, const wb_params *p)
+{
+  if (!c || !p)
+    return WB_EINVAL;
+  if (c->stage < 2)
+    return wb_fail(c, WB_ESTATE, "wb_autotune: scan the tiles first");
+  cudaSetDevice(c->device);
+  std::string err;
+  int rc = 0;
+  if (!c->batch && (rc = wb_batch_create(c->device, &c->batch, err)))
+    return wb_fail(c, rc, err);
+  // stage against the context's own device class buffer; the timing runs
+  // write labels only, never class bytes
+  if ((rc = wb_ensure(c, c->clsDev, c->n + 64)))
+    return rc;
+  int shape = c->shape, chunk = c->chunk;
+  double gp = c->grid_points;
+  if ((rc = wb_classify_stage(c, p, (uint8_t *)c->clsDev.p, 1)) ||
+      (rc = wb_autotune_job(c->batch, c, p, (uint8_t *)c->clsDev.p, 1, c->stream, &shape, &chunk, &gp, err)))
+    return wb_fail(c, rc, "wb_autotune: " + (err.empty() ? c->err : err));
+  c->shape = shape;
+  c->chunk = chunk;
+  c->grid_points = gp;
+  c->clsStaged = false;
+  return 0;
 }
 
 int wb_classify_cloud(wb_ctx *c, const wb_cloud *cloud, const wb_params *p, uint8_t *cls)

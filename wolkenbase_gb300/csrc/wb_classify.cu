@@ -66,7 +66,6 @@ extern "C" int wb_classify_stats(unsigned long long *out, int reset)
 
 namespace
 {
-constexpr int kWarps = 4;
 constexpr int kBins = 64;
 constexpr uint32_t kStray = 0x80000000u;
 /* bound on |FP32 direction - atan2i| in angle units (2^31 per turn); the
@@ -286,12 +285,6 @@ __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
   s.kmax = (int32_t)fmin(ceil(reach / a.cell) + 1, 1e9);
   s.smax = (int32_t)fmin(ceil(reach / (WB_SUPER * a.cell)) + 1, 1e9);
   a.setup[j] = s;
-}
-
-__global__ void classifySetup(ClsArgs a)
-{
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < a.nd; j += (uint64_t)gridDim.x * blockDim.x)
-    setupPoint(a, j);
 }
 
 /* Classifies store position j with one warp; bminW/bmaxW are the warp's
@@ -592,41 +585,6 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   }
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(32 * kWarps) classifyRings(ClsArgs a)
-{
-  __shared__ uint32_t bmin[kWarps][kBins], bmax[kWarps][kBins];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t item = (uint64_t)blockIdx.x * kWarps + w;
-  if (item >= (EXACT ? (uint64_t)a.nwork : a.nd))
-    return;
-  classifyPoint<EXACT>(a, EXACT ? a.work[item] : item, lane, bmin[w], bmax[w]);
-}
-
-__global__ void scatterCls(uint64_t n, const uint32_t *__restrict__ storeOf, const int32_t *__restrict__ owner,
-                           const uint8_t *__restrict__ label, uint8_t *__restrict__ cls)
-{
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-  {
-    uint32_t j = storeOf[i];
-    if (owner[j] >= 0)
-      cls[i] = label[j];
-  }
-}
-
-__global__ void groundCount(uint64_t nd, const int32_t *__restrict__ owner, const uint8_t *__restrict__ label,
-                            TileRes *__restrict__ tiles)
-{
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
-    if (owner[j] >= 0 && label[j] == 2)
-      atomicAdd(&tiles[owner[j]].nGround, 1);
-}
-
-__global__ void zeroGround(uint64_t T, TileRes *__restrict__ tiles)
-{
-  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
-    tiles[k].nGround = 0;
-}
 }  // namespace
 
 /* Decoding is strictly increasing in every record integer when the step
@@ -732,47 +690,6 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.storeOf = (const uint32_t *)c->storeOf.p;
   a.cls = clsDev;
   WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 4, c->stream));
-  return 0;
-}
-
-int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
-{
-  ClsArgs a;
-  int rc = classifyPrepare(c, p, cls, onDevice, a);
-  if (rc)
-    return rc;
-  uint64_t nd = c->nd, n = c->n;
-  uint8_t *clsDev = a.cls;
-  if (nd)
-  {
-    unsigned sb = (unsigned)std::min<uint64_t>((nd + 255) / 256, (uint64_t)c->sm_count * 16);
-    { classifySetup<<<sb, 256, 0, c->stream>>>(a); ++c->launches; }
-    { classifyRings<false><<<(unsigned)((nd + kWarps - 1) / kWarps), 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
-    WB_CUDA(c, cudaGetLastError());
-  }
-  wb_mark(c, "classify");
-  uint32_t namb = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&namb, a.ambCount, 4, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->n_ambiguous = namb;
-  if (namb)
-  {
-    a.work = a.ambList;
-    a.nwork = namb;
-    { classifyRings<true><<<(namb + kWarps - 1) / kWarps, 32 * kWarps, 0, c->stream>>>(a); ++c->launches; }
-    WB_CUDA(c, cudaGetLastError());
-  }
-  wb_mark(c, "classify_exact");
-  unsigned gsz = (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
-  { zeroGround<<<gsz, 256, 0, c->stream>>>(c->n_tiles, (TileRes *)c->tileRes.p); ++c->launches; }
-  { groundCount<<<gsz, 256, 0, c->stream>>>(nd, a.owner, a.label, (TileRes *)c->tileRes.p); ++c->launches; }
-  if (n)
-    { scatterCls<<<gsz, 256, 0, c->stream>>>(n, (const uint32_t *)c->storeOf.p, a.owner, a.label, clsDev); ++c->launches; }
-  if (!onDevice && n)
-    WB_CUDA(c, cudaMemcpyAsync(cls, clsDev, n, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaGetLastError());
-  wb_mark(c, "cls_download");
-  c->stage = 3;
   return 0;
 }
 
@@ -956,13 +873,148 @@ struct WbBatch
   cudaStream_t capture = nullptr;
   BatchHdr *dIn = nullptr, *hIn = nullptr;
   BatchOut *dOut = nullptr, *hOut = nullptr;
-  struct Graph
-  {
-    int shape;
-    cudaGraphExec_t exec;
-  };
-  std::vector<Graph> graphs;
+  int per[WB_N_SHAPES + 1] = {0};   /* resident blocks per SM of each ring kernel (+ exact) */
+  cudaGraphExec_t graphs[WB_N_SHAPES] = {nullptr};
 };
+
+const WbShape kWbShapes[WB_N_SHAPES] = {{8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}};
+
+namespace
+{
+typedef void (*RingsFn)(BatchHdr *, const BatchOut *);
+
+/* shape WB_N_SHAPES is the exact pass */
+RingsFn ringsFn(int shape)
+{
+  // kWbShapes: about 85 or 64 registers a thread
+  switch (shape)
+  {
+  case 1: return batchRings<false, 4, 6>;
+  case 2: return batchRings<false, 4, 8>;
+  case 3: return batchRings<false, 8, 4>;
+  case 4: return batchRings<false, 2, 12>;
+  case WB_N_SHAPES: return batchRings<true, 4, 6>;
+  default: return batchRings<false, 8, 3>;
+  }
+}
+
+int ringsWarps(int shape)
+{
+  return shape == WB_N_SHAPES ? 4 : kWbShapes[shape].warps;
+}
+
+__global__ void batchAmbReset(const BatchHdr *__restrict__ h)
+{
+  for (int q = threadIdx.x; q < h->k; q += blockDim.x)
+    *h->jobs[q].ambCount = 0;
+}
+
+/* Persistent grid of a ring kernel: every SM filled to its occupancy
+ * (queried once; occupancy queries are not stream work, so this also runs
+ * before a capture begins). */
+cudaError_t ringsGrid(WbBatch *b, int shape, unsigned *grid)
+{
+  if (!b->per[shape])
+  {
+    int per = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ringsFn(shape), 32 * ringsWarps(shape), 0);
+    if (e != cudaSuccess)
+      return e;
+    b->per[shape] = per > 0 ? per : 1;
+  }
+  *grid = (unsigned)(b->sm * b->per[shape]);
+  return cudaSuccess;
+}
+
+/* The fused classify on stream s: upload of the job table, set-up, the
+ * persistent fast pass, the ambiguous prefix, the persistent exact pass,
+ * ground counts, the class-byte scatter and the read-back of the per-job
+ * totals (8 kernels).  With mark, stage events go on mark's stream. */
+cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned grids[2], wb_ctx *mark)
+{
+  const unsigned grid = (unsigned)b->sm * 8;
+  cudaError_t e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess)
+    return e;
+  batchSetup<<<grid, 256, 0, s>>>(b->dIn);
+  ringsFn(shape)<<<grids[0], 32 * ringsWarps(shape), 0, s>>>(b->dIn, b->dOut);
+  if (mark)
+    wb_mark(mark, "classify");
+  batchAmbPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut);
+  ringsFn(WB_N_SHAPES)<<<grids[1], 32 * ringsWarps(WB_N_SHAPES), 0, s>>>(b->dIn, b->dOut);
+  if (mark)
+    wb_mark(mark, "classify_exact");
+  batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
+  batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
+  batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
+  batchScatter<<<grid, 256, 0, s>>>(b->dIn);
+  e = cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaGetLastError();
+  return e;
+}
+
+cudaError_t captureBatch(WbBatch *b, int shape, cudaGraphExec_t *exec)
+{
+  unsigned grids[2];
+  cudaError_t e = ringsGrid(b, shape, &grids[0]);
+  if (e == cudaSuccess)
+    e = ringsGrid(b, WB_N_SHAPES, &grids[1]);
+  if (e != cudaSuccess)
+    return e;
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess)
+    return e;
+  cudaError_t le = enqueueBatch(b, b->capture, shape, grids, nullptr);
+  e = cudaStreamEndCapture(b->capture, &graph);
+  if (e == cudaSuccess && le != cudaSuccess)
+    e = le;
+  if (e == cudaSuccess)
+    e = cudaGraphInstantiate(exec, graph, 0);
+  if (graph)
+    cudaGraphDestroy(graph);
+  return e;
+}
+
+/* Fills the pinned job table from the staged contexts; with sample > 0 the
+ * point ranges are cut after the first `sample` points. */
+int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample, std::string &err)
+{
+  if (k < 1 || k > WB_BATCH_MAX)
+  {
+    err = "between 1 and " + std::to_string(WB_BATCH_MAX) + " jobs per launch";
+    return WB_EINVAL;
+  }
+  BatchHdr *h = b->hIn;
+  h->k = k;
+  h->chunk = chunk < 1 ? 4 : chunk;
+  h->next[0] = h->next[1] = 0;
+  h->startNd[0] = h->startN[0] = h->startT[0] = 0;
+  for (int q = 0; q < k; q++)
+  {
+    wb_ctx *c = jobs[q];
+    if (!c->clsStaged)
+    {
+      err = "job " + std::to_string(q) + " was not staged";
+      return WB_ESTATE;
+    }
+    memcpy(&h->jobs[q], c->clsArgs, sizeof(ClsArgs));
+    uint64_t nd = c->nd;
+    if (sample && h->startNd[q] + nd > sample)
+      nd = sample > h->startNd[q] ? sample - h->startNd[q] : 0;
+    h->startNd[q + 1] = h->startNd[q] + nd;
+    h->startN[q + 1] = h->startN[q] + c->n;
+    h->startT[q + 1] = h->startT[q] + c->n_tiles;
+  }
+  return 0;
+}
+
+int clampShape(int shape)
+{
+  return shape < 0 || shape >= WB_N_SHAPES ? 0 : shape;
+}
+}  // namespace
 
 int wb_batch_create(int device, WbBatch **out, std::string &err)
 {
@@ -998,8 +1050,9 @@ void wb_batch_destroy(WbBatch *b)
   if (!b)
     return;
   cudaSetDevice(b->device);
-  for (auto &g : b->graphs)
-    cudaGraphExecDestroy(g.exec);
+  for (cudaGraphExec_t g : b->graphs)
+    if (g)
+      cudaGraphExecDestroy(g);
   if (b->capture)
     cudaStreamDestroy(b->capture);
   cudaFree(b->dIn);
@@ -1021,133 +1074,19 @@ int wb_classify_stage(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   return 0;
 }
 
-const WbShape kWbShapes[WB_N_SHAPES] = {{4, 6}, {4, 8}, {8, 3}, {8, 4}, {2, 12}};
-
-namespace
-{
-typedef void (*RingsFn)(BatchHdr *, const BatchOut *);
-
-RingsFn ringsFn(int shape, bool exact)
-{
-  // kWbShapes: about 85 or 64 registers a thread
-  if (exact)
-    return batchRings<true, 4, 6>;
-  switch (shape)
-  {
-  case 1: return batchRings<false, 4, 8>;
-  case 2: return batchRings<false, 8, 3>;
-  case 3: return batchRings<false, 8, 4>;
-  case 4: return batchRings<false, 2, 12>;
-  default: return batchRings<false, 4, 6>;
-  }
-}
-
-/* Persistent grid of a ring kernel: every SM filled to its occupancy. */
-cudaError_t ringsLaunch(WbBatch *b, cudaStream_t s, int shape, bool exact)
-{
-  RingsFn fn = ringsFn(shape, exact);
-  int warps = exact ? 4 : kWbShapes[shape].warps;
-  int per = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32 * warps, 0);
-  if (e != cudaSuccess)
-    return e;
-  unsigned grid = (unsigned)(b->sm * (per > 0 ? per : 1));
-  fn<<<grid, 32 * warps, 0, s>>>(b->dIn, b->dOut);
-  return cudaGetLastError();
-}
-
-__global__ void batchAmbReset(const BatchHdr *__restrict__ h)
-{
-  for (int q = threadIdx.x; q < h->k; q += blockDim.x)
-    *h->jobs[q].ambCount = 0;
-}
-}  // namespace
-
-/* Captures the fused classify: upload of the job table, set-up, the
- * persistent fast pass, the ambiguous prefix, the persistent exact pass,
- * ground counts, the class-byte scatter and the read-back of the totals. */
-static cudaError_t captureBatch(WbBatch *b, int shape, cudaGraphExec_t *exec)
-{
-  cudaStream_t s = b->capture;
-  cudaGraph_t graph = nullptr;
-  // occupancy queries are not stream work: resolve the grids before capturing
-  int per[2] = {0, 0};
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], ringsFn(shape, false),
-                                                                32 * kWbShapes[shape].warps, 0);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], ringsFn(shape, true), 128, 0);
-  if (e != cudaSuccess)
-    return e;
-  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess)
-    return e;
-  const unsigned grid = (unsigned)b->sm * 8;
-  cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
-  batchSetup<<<grid, 256, 0, s>>>(b->dIn);
-  ringsFn(shape, false)<<<(unsigned)(b->sm * (per[0] > 0 ? per[0] : 1)), 32 * kWbShapes[shape].warps, 0, s>>>(
-      b->dIn, b->dOut);
-  batchAmbPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut);
-  ringsFn(shape, true)<<<(unsigned)(b->sm * (per[1] > 0 ? per[1] : 1)), 128, 0, s>>>(b->dIn, b->dOut);
-  batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
-  batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
-  batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
-  batchScatter<<<grid, 256, 0, s>>>(b->dIn);
-  cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDeviceToHost, s);
-  cudaError_t le = cudaGetLastError();
-  e = cudaStreamEndCapture(s, &graph);
-  if (e == cudaSuccess && le != cudaSuccess)
-    e = le;
-  if (e == cudaSuccess)
-    e = cudaGraphInstantiate(exec, graph, 0);
-  if (graph)
-    cudaGraphDestroy(graph);
-  return e;
-}
-
-/* Fills the pinned job table from the staged contexts; with sample > 0 the
- * point ranges are cut after the first `sample` points. */
-static int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample, std::string &err)
-{
-  if (k < 1 || k > WB_BATCH_MAX)
-  {
-    err = "between 1 and " + std::to_string(WB_BATCH_MAX) + " jobs per launch";
-    return WB_EINVAL;
-  }
-  BatchHdr *h = b->hIn;
-  h->k = k;
-  h->chunk = chunk < 1 ? 16 : chunk;
-  h->next[0] = h->next[1] = 0;
-  h->startNd[0] = h->startN[0] = h->startT[0] = 0;
-  for (int q = 0; q < k; q++)
-  {
-    wb_ctx *c = jobs[q];
-    if (!c->clsStaged)
-    {
-      err = "job " + std::to_string(q) + " was not staged";
-      return WB_ESTATE;
-    }
-    memcpy(&h->jobs[q], c->clsArgs, sizeof(ClsArgs));
-    uint64_t nd = c->nd;
-    if (sample && h->startNd[q] + nd > sample)
-      nd = sample > h->startNd[q] ? sample - h->startNd[q] : 0;
-    h->startNd[q + 1] = h->startNd[q] + nd;
-    h->startN[q + 1] = h->startN[q] + c->n;
-    h->startT[q + 1] = h->startT[q] + c->n_tiles;
-  }
-  return 0;
-}
-
 int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int shape, int chunk, cudaStream_t s,
                   float *ms, std::string &err)
 {
-  if (shape < 0 || shape >= WB_N_SHAPES)
-    shape = 0;
+  shape = clampShape(shape);
   int rc = fillTable(b, jobs, k, chunk, sample, err);
   if (rc)
     return rc;
   cudaSetDevice(b->device);
+  unsigned grid = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaError_t e = cudaEventCreate(&e0);
+  cudaError_t e = ringsGrid(b, shape, &grid);
+  if (e == cudaSuccess)
+    e = cudaEventCreate(&e0);
   if (e == cudaSuccess)
     e = cudaEventCreate(&e1);
   if (e == cudaSuccess)
@@ -1156,9 +1095,10 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
   {
     batchSetup<<<(unsigned)b->sm * 8, 256, 0, s>>>(b->dIn);
     cudaEventRecord(e0, s);
-    e = ringsLaunch(b, s, shape, false);
+    ringsFn(shape)<<<grid, 32 * ringsWarps(shape), 0, s>>>(b->dIn, b->dOut);
     cudaEventRecord(e1, s);
     batchAmbReset<<<1, 256, 0, s>>>(b->dIn);
+    e = cudaGetLastError();
   }
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(s);
@@ -1179,28 +1119,23 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
 int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int shape, int chunk,
                     uint64_t *launches, std::string &err)
 {
-  if (shape < 0 || shape >= WB_N_SHAPES)
-    shape = 0;
+  shape = clampShape(shape);
   int rc = fillTable(b, jobs, k, chunk, 0, err);
   if (rc)
     return rc;
-  cudaGraphExec_t exec = nullptr;
-  for (auto &g : b->graphs)
-    if (g.shape == shape)
-      exec = g.exec;
   cudaSetDevice(b->device);
-  if (!exec)
+  if (!b->graphs[shape])
   {
-    cudaError_t e = captureBatch(b, shape, &exec);
+    cudaError_t e = captureBatch(b, shape, &b->graphs[shape]);
     if (e != cudaSuccess)
     {
       cudaGetLastError();
+      b->graphs[shape] = nullptr;
       err = std::string("wb_batch_launch: graph capture: ") + cudaGetErrorString(e);
       return WB_ECUDA;
     }
-    b->graphs.push_back({shape, exec});
   }
-  cudaError_t e = cudaGraphLaunch(exec, s);
+  cudaError_t e = cudaGraphLaunch(b->graphs[shape], s);
   for (int q = 0; q < k && e == cudaSuccess; q++)
   {
     wb_ctx *c = jobs[q];
@@ -1229,4 +1164,119 @@ void wb_batch_collect(WbBatch *b, wb_ctx *const *jobs, int k)
     c->clsHost = nullptr;
     c->stage = 3;
   }
+}
+
+/* One cloud: the fused sequence with one job, launched directly on the
+ * context's stream (stage events between the passes), then the class bytes
+ * copied out.  Synchronous. */
+int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
+{
+  int rc = wb_classify_stage(c, p, cls, onDevice);
+  if (rc)
+    return rc;
+  std::string err;
+  if (!c->batch && (rc = wb_batch_create(c->device, &c->batch, err)))
+    return wb_fail(c, rc, err);
+  WbBatch *b = c->batch;
+  int shape = clampShape(c->shape);
+  if ((rc = fillTable(b, &c, 1, c->chunk, 0, err)))
+    return wb_fail(c, rc, "wb_classify: " + err);
+  unsigned grids[2];
+  WB_CUDA(c, ringsGrid(b, shape, &grids[0]));
+  WB_CUDA(c, ringsGrid(b, WB_N_SHAPES, &grids[1]));
+  WB_CUDA(c, enqueueBatch(b, c->stream, shape, grids, c));
+  c->launches += 8;
+  ClsArgs *a = (ClsArgs *)c->clsArgs;
+  if (!onDevice && c->n)
+    WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDeviceToHost, c->stream));
+  wb_mark(c, "cls_download");
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  wb_batch_collect(b, &c, 1);
+  return 0;
+}
+
+/* Coordinate descent over the fused fast pass's settings on one staged
+ * context: column density (the grid is rebuilt for each), kernel shape, then
+ * chunk, each timed over a sample of up to 2M points.  Labels do not depend
+ * on any of them.  Leaves c staged with the chosen density. */
+int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, cudaStream_t s,
+                    int *shape, int *chunk, double *gridPoints, std::string &err)
+{
+  const uint64_t sample = std::min<uint64_t>(c->nd, 2000000);
+  int sh0 = clampShape(*shape), ch0 = *chunk > 0 ? *chunk : 4;
+  double gp0 = *gridPoints > 0 ? *gridPoints : 64;
+  int rc = 0;
+  auto timeIt = [&](int sh, int ch) -> float {   // best of two runs
+    float best = 1e30f;
+    for (int r = 0; r < 2; r++)
+    {
+      float ms = 0;
+      if (rc == 0 && (rc = wb_batch_time(b, &c, 1, sample, sh, ch, s, &ms, err)) == 0)
+        best = std::min(best, ms);
+    }
+    return best;
+  };
+  auto regrid = [&](double gp) -> bool {
+    c->grid_points = gp;
+    const double *g = c->grid_bounds;
+    if (rc == 0)
+      rc = wb_grid_impl(c, g[0], g[1], g[2], g[3]);
+    if (rc == 0)
+      rc = wb_classify_stage(c, p, cls, onDevice);
+    if (rc == 0 && cudaStreamSynchronize(c->stream) != cudaSuccess)
+      rc = WB_ECUDA;
+    if (rc && err.empty())
+      err = c->err;
+    return rc == 0;
+  };
+  if (c->grid_points != gp0)
+    regrid(gp0);
+  timeIt(sh0, ch0);   // warm-up
+  static const double kDensity[] = {16, 24, 32, 48, 64};
+  double bestGp = gp0;
+  float best = timeIt(sh0, ch0);
+  for (double gp : kDensity)
+  {
+    if (gp == gp0 || !regrid(gp))
+      continue;
+    float t = timeIt(sh0, ch0);
+    if (t < best)
+    {
+      best = t;
+      bestGp = gp;
+    }
+  }
+  if (c->grid_points != bestGp)
+    regrid(bestGp);
+  int bestShape = sh0;
+  for (int sh = 0; sh < WB_N_SHAPES; sh++)
+  {
+    if (sh == sh0)
+      continue;
+    float t = timeIt(sh, ch0);
+    if (t < best)
+    {
+      best = t;
+      bestShape = sh;
+    }
+  }
+  int bestChunk = ch0;
+  static const int kChunk[] = {4, 16, 64};
+  for (int ch : kChunk)
+  {
+    if (ch == ch0)
+      continue;
+    float t = timeIt(bestShape, ch);
+    if (t < best)
+    {
+      best = t;
+      bestChunk = ch;
+    }
+  }
+  if (rc)
+    return rc;
+  *shape = bestShape;
+  *chunk = bestChunk;
+  *gridPoints = bestGp;
+  return 0;
 }

@@ -69,7 +69,11 @@ struct wb_ctx
   DevBuf label, clsDev, ambiguous, angleT;
   DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox, cellFlag, ptSetup;
   GridInfo grid;
-  double grid_points = 32;          /* target points per occupied column (autotuned by a server) */
+  /* fused fast-pass settings (wb_set_tuning; a server's autotuner picks them
+     per batch): kernel shape, work chunk and points per grid column */
+  int shape = 0, chunk = 4;
+  double grid_points = 64;
+  struct WbBatch *batch = nullptr;  /* job table of the batch-of-one launch */
   double grid_bounds[4] = {0, 0, 0, 0};   /* x0, y0, x1, y1 the column grid spans */
   DevBuf flowCache;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
@@ -151,5 +155,7 @@ extern const WbShape kWbShapes[WB_N_SHAPES];
  * cleared afterwards, so the batch can be launched normally. */
 int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int shape, int chunk, cudaStream_t s,
                   float *ms, std::string &err);
+int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, cudaStream_t s,
+                    int *shape, int *chunk, double *gridPoints, std::string &err);
 
 #endif

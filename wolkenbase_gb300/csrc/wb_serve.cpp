@@ -264,11 +264,8 @@ bool flushNow(const wb_server *s)
   return s->prepBusy == 0 && (s->queue.empty() || s->headBlocked);
 }
 
-/* The autotuner (first batch, classifier thread, lock not held).  On the
- * batch's largest job it times the fused fast pass over a sample of up to
- * 2M points: first each column density (the job's grid is rebuilt for each),
- * then each kernel shape, then each chunk size, keeping the fastest of each
- * (coordinate descent).  Labels do not depend on any of these choices. */
+/* The autotuner (first batch, classifier thread, lock not held): tunes on
+ * the batch's largest job (wb_autotune_job). */
 void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk, double &gridPoints)
 {
   auto t0 = std::chrono::steady_clock::now();
@@ -276,67 +273,10 @@ void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk
   for (JobRec *j : batch)
     if (j->ctx->nd > big->ctx->nd)
       big = j;
-  wb_ctx *c = big->ctx;
-  const uint64_t sample = std::min<uint64_t>(c->nd, 2000000);
   std::string err;
-  auto timeIt = [&](int sh, int ch) -> float {
-    float ms = 0;
-    if (wb_batch_time(s->batch, &c, 1, sample, sh, ch, s->clsStream, &ms, err))
-      return 1e30f;
-    return ms;
-  };
-  auto regrid = [&](double gp) -> bool {
-    c->grid_points = gp;
-    const double *b = c->grid_bounds;
-    return wb_grid_impl(c, b[0], b[1], b[2], b[3]) == 0 &&
-           wb_classify_stage(c, &big->spec.params, big->spec.cls, 0) == 0 &&
-           cudaStreamSynchronize(c->stream) == cudaSuccess;
-  };
-  timeIt(shape, chunk);   // warm-up
-  static const double kDensity[] = {16, 24, 32, 48, 64};
-  double bestGp = gridPoints;
-  float best = timeIt(shape, chunk);
-  for (double gp : kDensity)
-  {
-    if (gp == gridPoints || !regrid(gp))
-      continue;
-    float t = timeIt(shape, chunk);
-    if (t < best)
-    {
-      best = t;
-      bestGp = gp;
-    }
-  }
-  if (c->grid_points != bestGp)
-    regrid(bestGp);
-  int bestShape = shape;
-  for (int sh = 0; sh < WB_N_SHAPES; sh++)
-  {
-    if (sh == shape)
-      continue;
-    float t = timeIt(sh, chunk);
-    if (t < best)
-    {
-      best = t;
-      bestShape = sh;
-    }
-  }
-  int bestChunk = chunk;
-  static const int kChunk[] = {4, 16, 64};
-  for (int ch : kChunk)
-  {
-    if (ch == chunk)
-      continue;
-    float t = timeIt(bestShape, ch);
-    if (t < best)
-    {
-      best = t;
-      bestChunk = ch;
-    }
-  }
-  shape = bestShape;
-  chunk = bestChunk;
-  gridPoints = bestGp;
+  if (wb_autotune_job(s->batch, big->ctx, &big->spec.params, big->spec.cls, 0, s->clsStream, &shape, &chunk,
+                      &gridPoints, err))
+    s->err = "autotune: " + err;
   s->stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -365,7 +305,11 @@ void classifyLoop(wb_server *s)
     for (JobRec *j : batch)
       if (cudaStreamWaitEvent(s->clsStream, j->ev, 0) != cudaSuccess)
         rc = WB_ECUDA;
-    if (rc == 0 && s->cfg.autotune && !s->stats.tuned)
+    // tune on a batch whose largest job gives a sample big enough to time
+    size_t biggest = 0;
+    for (JobRec *j : batch)
+      biggest = std::max<size_t>(biggest, j->ctx->nd);
+    if (rc == 0 && s->cfg.autotune && !s->stats.tuned && biggest >= 1000000)
     {
       int shape = s->cfg.shape, chunk = s->cfg.chunk;
       double gp = s->cfg.grid_points;
@@ -439,9 +383,9 @@ wb_server *wb_server_open(const wb_server_config *cfg)
   if (s->cfg.shape < 0 || s->cfg.shape >= WB_N_SHAPES)
     s->cfg.shape = 0;
   if (!(s->cfg.grid_points > 0))
-    s->cfg.grid_points = 32;
+    s->cfg.grid_points = 64;
   if (s->cfg.chunk <= 0)
-    s->cfg.chunk = 16;
+    s->cfg.chunk = 4;
   size_t freeB = 0, totalB = 0;
   cudaMemGetInfo(&freeB, &totalB);
   s->budget = cfg->hbm_budget ? cfg->hbm_budget : (uint64_t)(freeB * 0.8);
