@@ -289,6 +289,39 @@ def batched_form(args, device):
             "batched_over_plain": plain_s / batch_s, "same_labels": same}
 
 
+def _gen_utm(spec):
+    from wolkenbase_gb300 import synth
+    n, side, bi, bj = spec
+    return synth.utm_block(n, side, bi, bj)
+
+
+def precision_form(args, device):
+    """The 100M-point UTM-like tile (1 cm scale, offsets 500 km / 4500 km /
+    1500 m, slopes to 45 degrees, 2 m steps), generated as a 4 x 4 mosaic of
+    one terrain: scan + classify exact (FP64 decisions) and in the FP32
+    precision mode on one built octree; flips and fit errors of the FP32 mode."""
+    import multiprocessing as mp
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import precision, synth
+    nb = 4
+    side = math.sqrt(args.precision_points / 100.0) / nb
+    specs = [(args.precision_points // (nb * nb), side, i, j) for i in range(nb) for j in range(nb)]
+    with mp.get_context("spawn").Pool(min(len(specs), os.cpu_count() or 1)) as pool:
+        blocks = pool.map(_gen_utm, specs, chunksize=1)
+    cloud = synth.mosaic(blocks)
+    del blocks
+    clf = wb.Classifier(device)
+    clf.build(cloud)
+    precision.compare(clf, cloud, built=True)     # warm-up
+    r = precision.compare(clf, cloud, built=True)
+    clf.close()
+    r["workload"] = (f"{cloud.n} pts over {nb * side:.0f} x {nb * side:.0f} m, 1 cm int32, offsets (500000, 4500000, "
+                     "1500) m, slopes to 45 deg + 2 m steps")
+    for k in ("fp64_ms", "fp32_ms"):
+        r[k + "_mpts_s"] = cloud.n / ((r[k]["scan"] + r[k]["classify"]) / 1e3) / 1e6
+    return r
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -330,6 +363,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=80.0)
     ap.add_argument("--batch-tiles", type=int, default=256)
     ap.add_argument("--batch-slots", type=int, default=8)
+    ap.add_argument("--precision-points", type=int, default=100_000_000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -466,6 +500,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_forms:
         out["served"] = served_form(args, local)
         out["batched"] = batched_form(args, local)
+        out["precision"] = precision_form(args, local)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

@@ -175,6 +175,25 @@ typedef struct
   double grid_points;
 } wb_tuning;
 int wb_set_tuning(wb_ctx *ctx, const wb_tuning *t);
+
+/* Precision mode (no reference counterpart).  WB_PRECISION_EXACT (default)
+ * reproduces the reference bit for bit: FP32 work is only a filter, and
+ * every decision inside its error band is re-run in FP64.  WB_PRECISION_FP32
+ * runs neighbour distances and the tile fit sums in FP32 in a tile-local
+ * frame (Kahan-compensated sums, FP64 3x3 solve) and lets FP32 decisions
+ * stand; labels can then differ from the reference for points whose
+ * decision margin is within FP32 rounding.  Applies from the next
+ * wb_scan_tiles / wb_classify.  Clouds whose record differences do not fit
+ * FP32 exactly always run exact. */
+#define WB_PRECISION_EXACT 0
+#define WB_PRECISION_FP32 1
+int wb_set_precision(wb_ctx *ctx, int mode);
+
+/* The least-squares plane of every tile from the last wb_scan_tiles, in
+ * flowsnake order: 3 doubles per tile (a, b, c of z = a*x + b*y + c, x and y
+ * measured from the tile centre); NaN where the fit is singular.  With
+ * WB_PRECISION_FP32 this is the FP32-sum fit. */
+int wb_tile_planes(wb_ctx *ctx, double *abc, uint64_t capacity);
 int wb_get_tuning(wb_ctx *ctx, wb_tuning *t);
 int wb_autotune(wb_ctx *ctx, const wb_params *params);
 

@@ -178,6 +178,17 @@ class Classifier:
         self._check(self.L.wb_classify_cloud(self.ctx, C.byref(cs), C.byref(p), cls.ctypes.data))
         return cls
 
+    def planes(self):
+        """(T, 3) least-squares planes of the last scan (z = a*x + b*y + c from the tile centre)."""
+        T = self.info()["n_tiles"]
+        out = np.zeros((T, 3))
+        self._check(self.L.wb_tile_planes(self.ctx, out.ctypes.data, T))
+        return out
+
+    def set_precision(self, mode):
+        """_lib.WB_PRECISION_EXACT (bit-exact, default) or _lib.WB_PRECISION_FP32."""
+        self._check(self.L.wb_set_precision(self.ctx, int(mode)))
+
     # -- kernel settings (speed only; labels do not depend on them) --
     def tuning(self):
         t = _lib.wb_tuning()

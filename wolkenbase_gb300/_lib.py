@@ -18,6 +18,7 @@ ERROR_NAMES = {WB_EINVAL: "WB_EINVAL", WB_ENOMEM: "WB_ENOMEM", WB_ECUDA: "WB_ECU
                WB_EBUSY: "WB_EBUSY", WB_ECANCELED: "WB_ECANCELED"}
 
 WB_FLUSH_EAGER, WB_FLUSH_FULL = 0, 1
+WB_PRECISION_EXACT, WB_PRECISION_FP32 = 0, 1
 (WB_JOB_QUEUED, WB_JOB_PREP, WB_JOB_READY, WB_JOB_CLASSIFY, WB_JOB_DONE, WB_JOB_FAILED,
  WB_JOB_CANCELLED) = range(7)
 
@@ -107,6 +108,8 @@ SIGNATURES = {
     "wb_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),
     "wb_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),
     "wb_autotune": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
+    "wb_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
+    "wb_tile_planes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
     "wb_server_close": (None, [C.c_void_p]),
     "wb_server_error": (C.c_char_p, [C.c_void_p]),

@@ -423,6 +423,36 @@ int wb_set_tuning(wb_ctx *c, const wb_tuning *t)
   return 0;
 }
 
+int wb_set_precision(wb_ctx *c, int mode)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (mode != WB_PRECISION_EXACT && mode != WB_PRECISION_FP32)
+    return wb_fail(c, WB_EINVAL, "wb_set_precision: WB_PRECISION_EXACT or WB_PRECISION_FP32");
+  c->precision = mode;
+  return 0;
+}
+
+int wb_tile_planes(wb_ctx *c, double *abc, uint64_t capacity)
+{
+  if (!c || !abc)
+    return WB_EINVAL;
+  if (c->stage < 2)
+    return wb_fail(c, WB_ESTATE, "wb_tile_planes: scan the tiles first");
+  uint64_t T = c->n_tiles;
+  if (capacity < T)
+    return wb_fail(c, WB_EINVAL, "wb_tile_planes: capacity below the tile count");
+  cudaSetDevice(c->device);
+  std::vector<TileRes> r(T);
+  if (T)
+    WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint64_t k = 0; k < T; k++)
+    for (int i = 0; i < 3; i++)
+      abc[3 * k + i] = r[k].plane[i];
+  return 0;
+}
+
 int wb_get_tuning(wb_ctx *c, wb_tuning *t)
 {
   if (!c || !t)

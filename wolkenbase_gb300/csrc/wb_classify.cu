@@ -109,6 +109,7 @@ struct ClsArgs
   const int32_t *superBox;
   double zmin;
   int exactInts;   /* decode strictly increasing and 32-bit record differences exact */
+  int fp32Only;    /* precision mode: FP32 decisions stand, no exact re-run */
   float fsx, fsy, fsz, fs2;   /* metres per record unit and slope^2, FP32 */
   PtSetup *setup;
   /* ambiguous points for the exact pass */
@@ -391,6 +392,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
                 in = true;
               else if (zd < -ztol || f < -tol)
                 in = false;
+              else if (a.fp32Only)
+                in = zd > 0 && f > 0;
               else
                 in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
             }
@@ -463,7 +466,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     int nocc;
     uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
     if (nocc >= 2)
-      surrounded = (EXACT || !fast) ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+      surrounded = (EXACT || !fast || a.fp32Only) ? gap < (uint32_t)WB_DEG144
+                                                  : gap + 2 * kMargin < (uint32_t)WB_DEG144;
   };
   // Near field: rings of single columns around the point's column, each ring
   // visited in an order that alternates sides (stride 4k-1 over its 8k
@@ -561,7 +565,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       }
     }
   }
-  if (!surrounded && fast)
+  if (!surrounded && fast && !a.fp32Only)
   {
     int nocc;
     __syncwarp();
@@ -676,6 +680,7 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   for (int k = 0; k < 3; k++)
     fits32 = fits32 && (int64_t)c->grid.imax[k] - (int64_t)c->grid.imin[k] < ((int64_t)1 << 30);
   a.exactInts = (decodeIsExact(g, mn, mx) && fits32) ? 1 : 0;
+  a.fp32Only = (c->precision == WB_PRECISION_FP32 && a.exactInts) ? 1 : 0;
   a.fsx = (float)(g.scale[0] * g.unit);
   a.fsy = (float)(g.scale[1] * g.unit);
   a.fsz = (float)(g.scale[2] * g.unit);

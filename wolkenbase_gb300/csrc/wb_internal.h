@@ -58,6 +58,7 @@ struct wb_ctx
   uint64_t n_ambiguous = 0;         /* points the exact classify pass re-ran */
   WbGeom g{};
   wb_params params{};
+  int precision = WB_PRECISION_EXACT;   /* wb_set_precision */
 
   /* named device buffers */
   DevBuf rec, key0, key1, idx0, idx1, tmp32, tmp32b, tmp8, scanTmp, small;
@@ -99,6 +100,7 @@ struct TileRes
 {
   int32_t nPoints, nGround, treeFlags, pad;
   double density, hScan, h, height;
+  double plane[3];   /* least-squares plane z = a*x + b*y + c, x and y from the tile centre */
 };
 
 /* error helpers */

@@ -594,6 +594,9 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
       v0 = NAN;
     if (m[1][1] == 0)
       v1 = NAN;
+    r.plane[0] = v0;
+    r.plane[1] = v1;
+    r.plane[2] = m[2][2] == 0 ? NAN : bv[2];
     sx = v0;
     sy = v1;
     double len = wb_hypot(sx, sy);
@@ -706,6 +709,262 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
     r.density = density;
     r.hScan = r.h = sqrt(1 / density + s.minH * s.minH);
     r.height = top - bottom;
+    res[k] = r;
+  }
+}
+
+/* Error-free sum of two floats (Knuth's two-sum): s + e == a + b exactly. */
+__device__ __forceinline__ void twoSumF(float a, float b, float &s, float &e)
+{
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+/* scanCylinder in the precision mode: coordinates are FP32 in a tile-local
+ * frame.  The normal-equation sums are taken about the points' centroid
+ * (found exactly in record integers), accumulated per lane with Kahan
+ * compensation and merged across the warp with two-sums; the sums of the
+ * tile-centre frame are rebuilt from them in FP64, and only the 3x3 solve
+ * (the reference's Gauss-Jordan with ratio pivoting) runs in FP64.  The
+ * untilting, bottom, bottom2, top and the sector histogram run in FP32 with
+ * coordinates from an integer anchor next to the tile centre.  Untilting, bottom,
+ * bottom2, top and the sector histogram run in FP32 in the same frame. */
+__global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, TileRes *__restrict__ res)
+{
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const TileArgs &a = s.t;
+  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
+  if (k >= a.T)
+    return;
+  uint32_t b0 = s.tileStart[k], M = s.tileStart[k + 1] - b0;
+  TileRes r{};
+  if (M == 0)
+  {
+    if (lane == 0)
+      res[k] = r;
+    return;
+  }
+  double cx, cy;
+  tileCenter(a, k, cx, cy);
+  // integer anchor next to the centre and the FP32 offset of the centre from it
+  int32_t ax = (int32_t)llrint((cx / a.unit - a.off[0]) / a.scale[0]);
+  int32_t ay = (int32_t)llrint((cy / a.unit - a.off[1]) / a.scale[1]);
+  const float fx = (float)(dec(a, 0, ax) - cx), fy = (float)(dec(a, 1, ay) - cy);
+  const float ssx = (float)(a.scale[0] * a.unit), ssy = (float)(a.scale[1] * a.unit), ssz = (float)(a.scale[2] * a.unit);
+  const int32_t az = a.sz[s.tilePts[b0]];
+  const double z0 = dec(a, 2, az);
+  auto local = [&](uint32_t j, float &x, float &y, float &z) {
+    x = __fadd_rn(__fmul_rn((float)(a.sx[j] - ax), ssx), fx);
+    y = __fadd_rn(__fmul_rn((float)(a.sy[j] - ay), ssy), fy);
+    z = __fmul_rn((float)(a.sz[j] - az), ssz);
+  };
+  // Compensated sums of n quantities per lane (Kahan), merged across the warp
+  // with two-sums; every lane receives the totals as doubles.
+  auto warpSum = [&](auto quantities, double *tot, int n) {
+    float sum[kQ], cmp[kQ];
+    for (int u = 0; u < n; u++)
+      sum[u] = cmp[u] = 0.f;
+    for (uint32_t i = lane; i < M; i += 32)
+    {
+      float q[kQ];
+      quantities(s.tilePts[b0 + i], q);
+      for (int u = 0; u < n; u++)
+      {
+        float yv = __fsub_rn(q[u], cmp[u]);
+        float t = __fadd_rn(sum[u], yv);
+        cmp[u] = __fsub_rn(__fsub_rn(t, sum[u]), yv);
+        sum[u] = t;
+      }
+    }
+    for (int u = 0; u < n; u++)
+    {
+      float hi = sum[u], lo = -cmp[u];
+      for (int o = 16; o; o >>= 1)
+      {
+        float ohi = __shfl_xor_sync(0xffffffffu, hi, o), olo = __shfl_xor_sync(0xffffffffu, lo, o);
+        float sh, se;
+        twoSumF(hi, ohi, sh, se);
+        hi = sh;
+        lo = __fadd_rn(__fadd_rn(lo, olo), se);
+      }
+      tot[u] = (double)hi + (double)lo;
+    }
+  };
+  // Pass 1: the centroid in record integers (exact int64 sums).  Pass 2:
+  // FP32 coordinates about it in record units, u = X - centroid (exact in
+  // FP32), and the compensated sums of their products, which are exact while
+  // a product stays below 2^24 (|u| * |v| of a 1.5 m tile at 1 mm is below
+  // 2^20); the scales are applied in FP64.
+  long long isum[3] = {0, 0, 0};
+  for (uint32_t i = lane; i < M; i += 32)
+  {
+    uint32_t j = s.tilePts[b0 + i];
+    isum[0] += a.sx[j] - ax;
+    isum[1] += a.sy[j] - ay;
+    isum[2] += a.sz[j] - az;
+  }
+  for (int d = 0; d < 3; d++)
+    for (int o = 16; o; o >>= 1)
+      isum[d] += __shfl_xor_sync(0xffffffffu, isum[d], o);
+  const int32_t cX = ax + (int32_t)llrint((double)isum[0] / M), cY = ay + (int32_t)llrint((double)isum[1] / M),
+                cZ = az + (int32_t)llrint((double)isum[2] / M);
+  double cs[kQ];
+  warpSum([&](uint32_t j, float *q) {
+    float u = (float)(a.sx[j] - cX), v = (float)(a.sy[j] - cY), t = (float)(a.sz[j] - cZ);
+    q[0] = __fmul_rn(u, u);
+    q[1] = __fmul_rn(v, u);
+    q[2] = __fmul_rn(v, v);
+    q[3] = u;
+    q[4] = v;
+    q[5] = __fmul_rn(u, t);
+    q[6] = __fmul_rn(v, t);
+    q[7] = t;
+  }, cs, kQ);
+  // the sums of the tile-centre frame (heights from z0), rebuilt in FP64:
+  // x = u*kx + X, y = v*ky + Y, z - z0 = t*kz + Z
+  const double kx = a.scale[0] * a.unit, ky = a.scale[1] * a.unit, kz = a.scale[2] * a.unit;
+  const double X = dec(a, 0, cX) - cx, Y = dec(a, 1, cY) - cy, Z = dec(a, 2, cZ) - z0, Md = (double)M;
+  const double uu = cs[0] * kx * kx, uv = cs[1] * kx * ky, vv = cs[2] * ky * ky, su = cs[3] * kx, sv = cs[4] * ky,
+               ut = cs[5] * kx * kz, vt = cs[6] * ky * kz, st = cs[7] * kz;
+  double tot[kQ];
+  tot[0] = uu + 2 * X * su + Md * X * X;
+  tot[1] = uv + X * sv + Y * su + Md * X * Y;
+  tot[2] = vv + 2 * Y * sv + Md * Y * Y;
+  tot[3] = su + Md * X;
+  tot[4] = sv + Md * Y;
+  tot[5] = ut + Z * su + X * st + Md * X * Z;
+  tot[6] = vt + Z * sv + Y * st + Md * Y * Z;
+  tot[7] = st + Md * Z;
+  double sx = 0, sy = 0;
+  if (lane == 0)
+  {
+    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)M}};
+    double bv[3] = {tot[5], tot[6], tot[7]};
+    for (int i = 0; i < 3; i++)
+    {
+      findPivot3(m, bv, i, i);
+      for (int j = 0; j < 3; j++)
+        rowOp3(m, bv, i, j, i);
+    }
+    for (int i = 2; i >= 0; i--)
+      for (int j = 0; j < i; j++)
+        rowOp3(m, bv, i, j, i);
+    double v0 = bv[0], v1 = bv[1];
+    if (m[0][0] == 0)
+      v0 = NAN;
+    if (m[1][1] == 0)
+      v1 = NAN;
+    r.plane[0] = v0;
+    r.plane[1] = v1;
+    r.plane[2] = m[2][2] == 0 ? NAN : bv[2] + z0;
+    sx = v0;
+    sy = v1;
+    double len = wb_hypot(sx, sy);
+    if (len > 1)
+    {
+      sx /= len;
+      sy /= len;
+    }
+    if (isnan(sx) || isnan(sy))
+      sx = sy = 0;
+  }
+  const float fsx = (float)__shfl_sync(0xffffffffu, sx, 0), fsy = (float)__shfl_sync(0xffffffffu, sy, 0);
+  auto untilt = [&](float x, float y, float z) { return __fsub_rn(z, __fadd_rn(__fmul_rn(fsy, y), __fmul_rn(fsx, x))); };
+  float bottom = INFINITY, top = -INFINITY;
+  uint32_t argmin = 0xffffffffu;
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    float uz = INFINITY, ut = -INFINITY;
+    if (i < M)
+    {
+      float x, y, z;
+      local(s.tilePts[b0 + i], x, y, z);
+      uz = ut = untilt(x, y, z);
+    }
+    float mv = uz;
+    uint32_t mi = i < M ? i : 0xffffffffu;
+    for (int o = 16; o; o >>= 1)
+    {
+      float ov = __shfl_xor_sync(0xffffffffu, mv, o);
+      uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
+      if (ov < mv || (ov == mv && oi < mi))
+      {
+        mv = ov;
+        mi = oi;
+      }
+    }
+    if (mv < bottom)
+    {
+      bottom = mv;
+      argmin = mi;
+    }
+    for (int o = 16; o; o >>= 1)
+      ut = fmaxf(ut, __shfl_xor_sync(0xffffffffu, ut, o));
+    top = fmaxf(top, ut);
+  }
+  float bottom2 = INFINITY;
+  for (uint32_t c0 = 0; c0 < M && c0 < argmin; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    float v = INFINITY;
+    if (i < M && i < argmin)
+    {
+      float x, y, z;
+      local(s.tilePts[b0 + i], x, y, z);
+      v = untilt(x, y, z);
+    }
+    for (int o = 16; o; o >>= 1)
+      v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    bottom2 = fminf(bottom2, v);
+  }
+  if (isinf(bottom2))
+    bottom2 = bottom;
+  const float lim = __fadd_rn(bottom2, (float)(2 * a.rad)), inner = (float)(a.rad / 2.6457513110645905905016);
+  uint32_t nBottom = 0;
+  int histo[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    int sector = -1;
+    if (i < M)
+    {
+      float x, y, z;
+      local(s.tilePts[b0 + i], x, y, z);
+      if (untilt(x, y, z) < lim)
+      {
+        sector = (int)rintf(atan2f(y, x) * 0.954929658551372f);   // 3 / pi
+        if (sector < 0)
+          sector += 6;
+        sector = (sector % 6) + 1;
+        if (hypotf(x, y) < inner)
+          sector = 0;
+      }
+    }
+    for (int sct = 0; sct < 7; sct++)
+      histo[sct] += __popc(__ballot_sync(0xffffffffu, sector == sct));
+    nBottom += __popc(__ballot_sync(0xffffffffu, sector >= 0));
+  }
+  if (lane == 0)
+  {
+    double density = 0;
+    int treeFlags = 0;
+    for (int i = 0; i < 7; i++)
+      density += (double)histo[i] * (double)histo[i];
+    if (M > nBottom && density < 7)
+      treeFlags = 1;
+    density = sqrt(density) * 2.6457513110645905905016 / (a.rad * a.rad) / M_PI;
+    if (M > nBottom && density < 0.5)
+      treeFlags = 1;
+    if ((double)top - (double)bottom > 1.5)
+      treeFlags = 1;
+    r.nPoints = (int32_t)M;
+    r.nGround = 0;
+    r.treeFlags = treeFlags;
+    r.density = density;
+    r.hScan = r.h = sqrt(1 / density + s.minH * s.minH);
+    r.height = (double)top - (double)bottom;
     res[k] = r;
   }
 }
@@ -921,7 +1180,10 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   s.tilePts = (const uint32_t *)c->tilePts.p;
   s.minH = p->min_hyp_size;
   TileRes *res = (TileRes *)c->tileRes.p;
-  { scanKernel<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
+  if (c->precision == WB_PRECISION_FP32 && a.fast)
+    { scanKernel32<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
+  else
+    { scanKernel<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "scan");
   unsigned pb = (unsigned)std::min<uint64_t>((T + 255) / 256, (uint64_t)c->sm_count * 16);

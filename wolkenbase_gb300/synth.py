@@ -130,16 +130,20 @@ def _vegetation_xy(rng, n, x0, y0, sx, sy, boxes, cover):
 def terrain_cloud(n, size_x, size_y, seed, *, scale=(0.001, 0.001, 0.001), offset=(0.0, 0.0, 0.0),
                   nonground=0.2, amp=(0.5, 2.0), wavelen=(20.0, 80.0), noise=0.02,
                   max_slope=None, steps=0.0, origin=(0.0, 0.0), unit=1.0, shuffle=True,
-                  veg_cover=0.15) -> Cloud:
+                  veg_cover=0.15, terrain_seed=None) -> Cloud:
     """One tile: ground sinusoids + noise, box buildings (3-15 m) and vegetation (0.5-10 m).
 
     Half of the nonground points lie on building roofs and walls (uniform by
     area), half are vegetation 0.5-10 m above ground inside copses covering
     ``veg_cover`` of the tile (None: spread over the whole tile).  Points are
-    shuffled into a random order unless ``shuffle`` is false.
+    shuffled into a random order unless ``shuffle`` is false.  With
+    ``terrain_seed`` the ground surface comes from that seed and the points
+    from ``seed``, so tiles with one terrain seed and different origins join
+    into one seamless mosaic.
     """
     rng = np.random.default_rng(seed)
-    params = _terrain_params(rng, amp, wavelen, max_slope)
+    params = _terrain_params(rng if terrain_seed is None else np.random.default_rng(terrain_seed), amp, wavelen,
+                             max_slope)
     x0 = origin[0] + offset[0]
     y0 = origin[1] + offset[1]
     area = size_x * size_y
@@ -263,6 +267,24 @@ def serve_requests(count, rate=200.0, lo=10_000, hi=10_000_000, seed=5000):
     t = np.cumsum(rng.exponential(1.0 / rate, count))
     sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
     return [(float(t[i]), int(sizes[i]), seed + 1 + i) for i in range(count)]
+
+
+def mosaic(blocks):
+    """Joins tiles that share scale and offset (e.g. utm_block results) into one cloud."""
+    xyz = np.concatenate([b.xyz for b in blocks])
+    first = blocks[0]
+    cl = Cloud(xyz, first.scale, first.offset, first.unit, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
+               sum(b.n_ground_truth for b in blocks), np.concatenate([b.truth for b in blocks]))
+    cl.minc = tuple(float(min(b.minc[a] for b in blocks)) for a in range(3))
+    cl.maxc = tuple(float(max(b.maxc[a] for b in blocks)) for a in range(3))
+    return cl
+
+
+def utm_block(n, side, bi, bj, seed=4):
+    """Block (bi, bj) of the UTM-like tile, ``side`` metres square, n points."""
+    return terrain_cloud(n, side, side, seed * 1000 + bi * 64 + bj, scale=(0.01, 0.01, 0.01),
+                         offset=(500000.0, 4500000.0, 1500.0), max_slope=1.0, steps=2.0,
+                         origin=(bi * side, bj * side), terrain_seed=seed)
 
 
 def utm_tile(n=100_000_000, seed=4):
