@@ -77,7 +77,7 @@ void wb_release_buffers(wb_ctx *c)
                    &c->tileEx, &c->tileEy, &c->tileLookup, &c->tileStart, &c->tilePts, &c->owner, &c->tileRes,
                    &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->angleT,
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
-                   &c->cellBox, &c->gx, &c->gy, &c->gz, &c->gpos, &c->superBox, &c->cellFlag, &c->ptSetup};
+                   &c->gpt, &c->cellRec, &c->superRec, &c->ptSetup};
   for (DevBuf *b : all)
     wb_free_buf(c, *b);
   c->used = 0;

@@ -100,13 +100,10 @@ struct ClsArgs
   double gx0, gy0, cell;
   int nx, ny;
   uint64_t ncell;
-  const uint32_t *cellStart;
-  const int32_t *cellBox;
-  const int32_t *gx, *gy, *gz;
-  const uint32_t *gpos;
-  const uint8_t *cellFlag;
+  const int4 *col;     /* two int4 per column: {x0, y0, x1, y1}, {zmin, begin, end, flags} */
+  const int4 *gpt;     /* int4 {X, Y, Z, position | stray bit} per point, column order */
   int snx, sny;
-  const int32_t *superBox;
+  const int4 *super;   /* super-cell records, the column layout */
   double zmin;
   int exactInts;   /* decode strictly increasing and 32-bit record differences exact */
   int fp32Only;    /* precision mode: FP32 decisions stand, no exact re-run */
@@ -185,14 +182,15 @@ __device__ __noinline__ bool memberExact(const ClsArgs &a, const HypExact &h, ui
 /* Can any point of a box (integer bounds, 6 planes of N entries) be inside?
  * FP32 with generous slack.  Record differences are exact in 32 bits: the
  * host checks that the cloud's integer extent fits. */
-__device__ __forceinline__ bool boxMeets(const Hyp &h, const int32_t *box, uint64_t N, uint64_t c)
+__device__ __forceinline__ bool boxMeets(const Hyp &h, const int4 *rec, uint64_t c)
 {
-  int32_t bx0 = box[c];
-  if (bx0 == INT32_MAX)
+  int4 b = rec[2 * c];
+  if (b.x == INT32_MAX)
     return false;   // empty block
-  float xl = (float)(bx0 - h.qx) * h.sx, xh = (float)(box[3 * N + c] - h.qx) * h.sx;
-  float yl = (float)(box[N + c] - h.qy) * h.sy, yh = (float)(box[4 * N + c] - h.qy) * h.sy;
-  float zd = (float)(h.qz - box[2 * N + c]) * h.sz + h.czp;
+  int32_t zmin = rec[2 * c + 1].x;
+  float xl = (float)(b.x - h.qx) * h.sx, xh = (float)(b.z - h.qx) * h.sx;
+  float yl = (float)(b.y - h.qy) * h.sy, yh = (float)(b.w - h.qy) * h.sy;
+  float zd = (float)(h.qz - zmin) * h.sz + h.czp;
   float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
   float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
   float r2 = h.s2 * (dx * dx + dy * dy);
@@ -334,18 +332,18 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   auto column = [&](uint64_t cc) -> bool {
     WB_STAT(stat[7], 1);
     bool got = false;
-    uint32_t b = a.cellStart[cc], e = a.cellStart[cc + 1];
+    const int4 box = a.col[2 * cc], r1 = a.col[2 * cc + 1];
+    uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
     // Points of a column are sorted by height.  None above pz + (czp -
     // sqrt(por^2 + s^2 d^2)) / sz, d the column's nearest distance, can be
     // inside, so the scan stops at the first chunk past that height (with
     // slack).  Columns holding points outside the root cube in x or y are
     // read in full (their blocks' cubes decide for them).
     int32_t zlim = INT32_MAX;
-    if (fast && !a.cellFlag[cc] && h.sz > 0)
+    if (fast && !r1.w && h.sz > 0)
     {
-      const uint64_t N = a.ncell;
-      float xl = (float)(a.cellBox[cc] - h.qx) * h.sx, xh = (float)(a.cellBox[3 * N + cc] - h.qx) * h.sx;
-      float yl = (float)(a.cellBox[N + cc] - h.qy) * h.sy, yh = (float)(a.cellBox[4 * N + cc] - h.qy) * h.sy;
+      float xl = (float)(box.x - h.qx) * h.sx, xh = (float)(box.z - h.qx) * h.sx;
+      float yl = (float)(box.y - h.qy) * h.sy, yh = (float)(box.w - h.qy) * h.sy;
       float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
       float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
       float need = sqrtf(h.por2f + h.s2 * (dx * dx + dy * dy));
@@ -356,12 +354,13 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     {
       uint32_t t = t0 + lane;
       bool low = false;
-      int32_t qz = 0;
+      int4 pt = make_int4(0, 0, 0, 0);
       if (t < e)
       {
-        qz = a.gz[t];
-        low = zlim == INT32_MAX || qz - h.qz <= zlim;
+        pt = a.gpt[t];
+        low = zlim == INT32_MAX || pt.z - h.qz <= zlim;
       }
+      const int32_t qz = pt.z;
       if (!__any_sync(0xffffffffu, low))
         break;
       WB_STAT(stat[4], __popc(__ballot_sync(0xffffffffu, low)));
@@ -369,8 +368,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       uint32_t u = 0;
       if (low)
       {
-        int32_t qx = a.gx[t], qy = a.gy[t];
-        uint32_t gp = a.gpos[t];
+        int32_t qx = pt.x, qy = pt.y;
+        uint32_t gp = (uint32_t)pt.w;
         if (fast)
         {
           int32_t dxi = qx - h.qx, dyi = qy - h.qy;
@@ -493,7 +492,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
           c = (uint64_t)jj * a.nx + i;
-          ok = a.cellStart[c] != a.cellStart[c + 1] && boxMeets(h, a.cellBox, a.ncell, c);
+          ok = boxMeets(h, a.col, c);
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
@@ -511,7 +510,6 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   const int S = WB_SUPER;
   int si = ci >= 0 ? ci / S : -((-ci + S - 1) / S), sj = cj >= 0 ? cj / S : -((-cj + S - 1) / S);
   const int smax = ps.smax;
-  const uint64_t NS = (uint64_t)a.snx * a.sny;
   for (int sr = 0; sr <= smax && !surrounded && kmax > kNear; sr++)
   {
     if (si + sr < 0 || si - sr >= a.snx || sj + sr < 0 || sj - sr >= a.sny)
@@ -530,7 +528,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         SI = si + di;
         SJ = sj + dj;
         if (SI >= 0 && SI < a.snx && SJ >= 0 && SJ < a.sny)
-          ok = boxMeets(h, a.superBox, NS, (uint64_t)SJ * a.snx + SI);
+          ok = boxMeets(h, a.super, (uint64_t)SJ * a.snx + SI);
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
       while (mask && !surrounded)
@@ -548,7 +546,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           if (i < a.nx && jj < a.ny && cheb > kNear)
           {
             c = (uint64_t)jj * a.nx + i;
-            cok = a.cellStart[c] != a.cellStart[c + 1] && boxMeets(h, a.cellBox, a.ncell, c);
+            cok = boxMeets(h, a.col, c);
           }
         }
         unsigned cm = __ballot_sync(0xffffffffu, cok);
@@ -665,16 +663,11 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.nx = c->grid.nx;
   a.ny = c->grid.ny;
   a.ncell = c->grid.ncell;
-  a.cellStart = (const uint32_t *)c->cellStart.p;
-  a.cellBox = (const int32_t *)c->cellBox.p;
-  a.gx = (const int32_t *)c->gx.p;
-  a.gy = (const int32_t *)c->gy.p;
-  a.gz = (const int32_t *)c->gz.p;
-  a.gpos = (const uint32_t *)c->gpos.p;
-  a.cellFlag = (const uint8_t *)c->cellFlag.p;
+  a.col = (const int4 *)c->cellRec.p;
+  a.gpt = (const int4 *)c->gpt.p;
   a.snx = c->grid.snx;
   a.sny = c->grid.sny;
-  a.superBox = (const int32_t *)c->superBox.p;
+  a.super = (const int4 *)c->superRec.p;
   a.zmin = (g.off[2] + g.scale[2] * (double)c->grid.zminInt) * g.unit;
   bool fits32 = true;
   for (int k = 0; k < 3; k++)

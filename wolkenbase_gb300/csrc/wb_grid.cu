@@ -75,12 +75,12 @@ __global__ void cellStartKernel(uint64_t nd, uint64_t ncell, const uint64_t *__r
   }
 }
 
-/* Gathers X/Y/Z into grid order and forms each cell's bounds; one warp per cell. */
+/* Gathers the points into column order as int4 {X, Y, Z, position} and
+ * forms each column's record; one warp per column. */
 __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ start, const uint32_t *__restrict__ pos,
                                const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                                const int32_t *__restrict__ sz, const uint8_t *__restrict__ stray,
-                               int32_t *__restrict__ gx, int32_t *__restrict__ gy, int32_t *__restrict__ gz,
-                               uint32_t *__restrict__ gpos, int32_t *__restrict__ box, uint8_t *__restrict__ flags)
+                               int4 *__restrict__ gpt, int4 *__restrict__ rec)
 {
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -93,11 +93,8 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
   {
     uint32_t j = pos[i];
     int32_t q[3] = {sx[j], sy[j], sz[j]};
-    gx[i] = q[0];
-    gy[i] = q[1];
-    gz[i] = q[2];
     uint8_t st = stray[j];
-    gpos[i] = j | ((st & 1) ? 0x80000000u : 0u);
+    gpt[i] = make_int4(q[0], q[1], q[2], (int)(j | ((st & 1) ? 0x80000000u : 0u)));
     xyStray |= (st & 2) != 0;
     for (int a = 0; a < 3; a++)
     {
@@ -111,15 +108,13 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
       mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
       mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
     }
-  if (lane < 6)
-  {
-    int32_t v = lane < 3 ? mn[lane] : mx[lane - 3];
-    box[(uint64_t)lane * ncell + c] = v;
-  }
   // a column holding a point outside the root cube in x or y is read in full
   unsigned any = __ballot_sync(0xffffffffu, xyStray);
   if (lane == 0)
-    flags[c] = any ? 1 : 0;
+  {
+    rec[2 * c] = make_int4(mn[0], mn[1], mx[0], mx[1]);
+    rec[2 * c + 1] = make_int4(mn[2], (int)b, (int)e, any ? 1 : 0);
+  }
 }
 
 /* Record-integer extent of the cloud: out[0..2] minima, out[3..5] maxima. */
@@ -150,16 +145,15 @@ __global__ void extentKernel(uint64_t nd, const int32_t *__restrict__ sx, const 
     }
 }
 
-/* Bounds of each block of WB_SUPER x WB_SUPER columns (same layout as the
- * column bounds: 6 planes of snx*sny int32). */
-__global__ void superKernel(int nx, int ny, int snx, int sny, uint64_t ncell, const uint32_t *__restrict__ start,
-                            const int32_t *__restrict__ box, int32_t *__restrict__ sbox)
+/* Records of each block of WB_SUPER x WB_SUPER columns (the column record
+ * layout; begin/end unused). */
+__global__ void superKernel(int nx, int ny, int snx, int sny, const int4 *__restrict__ rec, int4 *__restrict__ srec)
 {
   uint64_t ns = (uint64_t)snx * sny;
   for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += (uint64_t)gridDim.x * blockDim.x)
   {
     int si = (int)(s % snx), sj = (int)(s / snx);
-    int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[2] = {INT32_MIN, INT32_MIN};
     for (int dj = 0; dj < WB_SUPER; dj++)
       for (int di = 0; di < WB_SUPER; di++)
       {
@@ -167,19 +161,17 @@ __global__ void superKernel(int nx, int ny, int snx, int sny, uint64_t ncell, co
         if (i >= nx || j >= ny)
           continue;
         uint64_t c = (uint64_t)j * nx + i;
-        if (start[c] == start[c + 1])
+        int4 r0 = rec[2 * c], r1 = rec[2 * c + 1];
+        if (r1.y == r1.z)
           continue;
-        for (int a = 0; a < 3; a++)
-        {
-          mn[a] = min(mn[a], box[(uint64_t)a * ncell + c]);
-          mx[a] = max(mx[a], box[(uint64_t)(3 + a) * ncell + c]);
-        }
+        mn[0] = min(mn[0], r0.x);
+        mn[1] = min(mn[1], r0.y);
+        mx[0] = max(mx[0], r0.z);
+        mx[1] = max(mx[1], r0.w);
+        mn[2] = min(mn[2], r1.x);
       }
-    for (int a = 0; a < 3; a++)
-    {
-      sbox[(uint64_t)a * ns + s] = mn[a];
-      sbox[(uint64_t)(3 + a) * ns + s] = mx[a];
-    }
+    srec[2 * s] = make_int4(mn[0], mn[1], mx[0], mx[1]);
+    srec[2 * s + 1] = make_int4(mn[2], 0, 0, 0);
   }
 }
 }  // namespace
@@ -206,9 +198,7 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   if ((rc = wb_ensure(c, c->gKey0, nd * 8 + 64)) || (rc = wb_ensure(c, c->gKey1, nd * 8 + 64)) ||
       (rc = wb_ensure(c, c->gVal0, nd * 4 + 64)) || (rc = wb_ensure(c, c->gVal1, nd * 4 + 64)) ||
       (rc = wb_ensure(c, c->stray, nd + 64)) || (rc = wb_ensure(c, c->cellStart, (ncell + 1) * 4 + 64)) ||
-      (rc = wb_ensure(c, c->cellBox, ncell * 24 + 64)) || (rc = wb_ensure(c, c->gx, nd * 4 + 64)) ||
-      (rc = wb_ensure(c, c->gy, nd * 4 + 64)) || (rc = wb_ensure(c, c->gz, nd * 4 + 64)) ||
-      (rc = wb_ensure(c, c->gpos, nd * 4 + 64)) || (rc = wb_ensure(c, c->cellFlag, ncell + 64)))
+      (rc = wb_ensure(c, c->gpt, nd * 16 + 64)) || (rc = wb_ensure(c, c->cellRec, ncell * 32 + 64)))
     return rc;
   GridArgs a;
   a.nd = nd;
@@ -246,16 +236,15 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   { cellStartKernel<<<blocks, 256, 0, c->stream>>>(nd, ncell, key, start); ++c->launches; }
   { cellFillKernel<<<(unsigned)((ncell * 32 + 255) / 256), 256, 0, c->stream>>>(
         ncell, start, val, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p, (const int32_t *)c->sz.p,
-        (const uint8_t *)c->stray.p, (int32_t *)c->gx.p, (int32_t *)c->gy.p, (int32_t *)c->gz.p,
-        (uint32_t *)c->gpos.p, (int32_t *)c->cellBox.p, (uint8_t *)c->cellFlag.p); ++c->launches; }
+        (const uint8_t *)c->stray.p, (int4 *)c->gpt.p, (int4 *)c->cellRec.p); ++c->launches; }
   int snx = (nx + WB_SUPER - 1) / WB_SUPER, sny = (ny + WB_SUPER - 1) / WB_SUPER;
   c->grid.snx = snx;
   c->grid.sny = sny;
   uint64_t nsup = (uint64_t)snx * sny;
-  if ((rc = wb_ensure(c, c->superBox, nsup * 24 + 64)))
+  if ((rc = wb_ensure(c, c->superRec, nsup * 32 + 64)))
     return rc;
   { superKernel<<<(unsigned)std::min<uint64_t>((nsup + 255) / 256, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(
-        nx, ny, snx, sny, ncell, start, (const int32_t *)c->cellBox.p, (int32_t *)c->superBox.p); ++c->launches; }
+        nx, ny, snx, sny, (const int4 *)c->cellRec.p, (int4 *)c->superRec.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   unsigned long long ns = 0;
   int ext[6];

@@ -68,7 +68,11 @@ struct wb_ctx
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
   DevBuf label, clsDev, ambiguous, angleT;
-  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, cellBox, gx, gy, gz, gpos, superBox, cellFlag, ptSetup;
+  /* column grid (wb_grid.cu): gpt holds one int4 {X, Y, Z, store position |
+     stray bit} per point in column order; cellRec two int4 per column,
+     {x0, y0, x1, y1} and {zmin, begin, end, flags}, x0 == INT32_MAX for an
+     empty column; superRec the same two int4 per super-cell */
+  DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, gpt, cellRec, superRec, ptSetup;
   GridInfo grid;
   /* fused fast-pass settings (wb_set_tuning; a server's autotuner picks them
      per batch): kernel shape, work chunk and points per grid column */

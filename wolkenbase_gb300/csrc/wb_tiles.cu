@@ -57,11 +57,9 @@ struct GridDev
 {
   double x0, y0, cell;
   int nx, ny;
-  const uint32_t *cellStart;
-  const int32_t *cellBox;
+  const int4 *cell2;   /* two int4 per column: {x0, y0, x1, y1}, {zmin, begin, end, flags} */
   uint64_t ncell;
-  const int32_t *gx, *gy;
-  const uint32_t *gpos;
+  const int4 *gpt;     /* int4 {X, Y, Z, position | stray bit} per point, column order */
   const uint32_t *leafId;
 };
 
@@ -136,10 +134,10 @@ __device__ __forceinline__ bool cylMember(const TileArgs &a, const GridDev &gd, 
   return cylExact(a, gd, f.cx, f.cy, gp, qx, qy);
 }
 
-__device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const GridDev &gd, uint64_t c, double cx, double cy)
+__device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const int4 &box, double cx, double cy)
 {
-  double x0 = dec(a, 0, gd.cellBox[c]), x1 = dec(a, 0, gd.cellBox[3 * gd.ncell + c]);
-  double y0 = dec(a, 1, gd.cellBox[gd.ncell + c]), y1 = dec(a, 1, gd.cellBox[4 * gd.ncell + c]);
+  double x0 = dec(a, 0, box.x), x1 = dec(a, 0, box.z);
+  double y0 = dec(a, 1, box.y), y1 = dec(a, 1, box.w);
   double dx = cx < x0 ? x0 - cx : (cx > x1 ? cx - x1 : 0.0);
   double dy = cy < y0 ? y0 - cy : (cy > y1 ? cy - y1 : 0.0);
   double r = a.rad * (1 + 1e-6) + 1e-6;
@@ -159,13 +157,19 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridCount(TileArgs a, GridDev
     for (int i = f.i0; i <= f.i1; i++)
     {
       uint64_t c = (uint64_t)j * gd.nx + i;
-      uint32_t b = gd.cellStart[c], e = gd.cellStart[c + 1];
-      if (b == e || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
+      int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
+      uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
+      if (b == e || !cellMeetsCyl(a, box, f.cx, f.cy))
         continue;
       for (uint32_t t0 = b; t0 < e; t0 += 32)
       {
         uint32_t t = t0 + lane;
-        bool in = t < e && cylMember(a, gd, f, gd.gpos[t], gd.gx[t], gd.gy[t]);
+        bool in = false;
+        if (t < e)
+        {
+          int4 p = gd.gpt[t];
+          in = cylMember(a, gd, f, (uint32_t)p.w, p.x, p.y);
+        }
         found += __popc(__ballot_sync(0xffffffffu, in));
       }
     }
@@ -209,8 +213,9 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
     for (int i = f.i0; i <= f.i1; i++)
     {
       uint64_t c = (uint64_t)j * gd.nx + i;
-      uint32_t cb = gd.cellStart[c], ce = gd.cellStart[c + 1];
-      if (cb == ce || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
+      int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
+      uint32_t cb = (uint32_t)r1.y, ce = (uint32_t)r1.z;
+      if (cb == ce || !cellMeetsCyl(a, box, f.cx, f.cy))
         continue;
       for (uint32_t t0 = cb; t0 < ce; t0 += 32)
       {
@@ -219,8 +224,9 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
         bool in = false;
         if (t < ce)
         {
-          gp = gd.gpos[t];
-          in = cylMember(a, gd, f, gp, gd.gx[t], gd.gy[t]);
+          int4 p = gd.gpt[t];
+          gp = (uint32_t)p.w;
+          in = cylMember(a, gd, f, gp, p.x, p.y);
         }
         unsigned m = __ballot_sync(0xffffffffu, in);
         if (in && n + __popc(m & lt) < kWarpFill)
@@ -287,13 +293,15 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
     for (int i = f.i0; i <= f.i1; i++)
     {
       uint64_t c = (uint64_t)j * gd.nx + i;
-      uint32_t b = gd.cellStart[c], e = gd.cellStart[c + 1];
-      if (b == e || !cellMeetsCyl(a, gd, c, f.cx, f.cy))
+      int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
+      uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
+      if (b == e || !cellMeetsCyl(a, box, f.cx, f.cy))
         continue;
       for (uint32_t t = b + threadIdx.x; t < e; t += kFillThreads)
       {
-        uint32_t gp = gd.gpos[t];
-        if (cylMember(a, gd, f, gp, gd.gx[t], gd.gy[t]))
+        int4 p = gd.gpt[t];
+        uint32_t gp = (uint32_t)p.w;
+        if (cylMember(a, gd, f, gp, p.x, p.y))
         {
           uint32_t slot = atomicAdd(&cnt, 1u);
           if (slot < kFillMax)
@@ -1135,11 +1143,8 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   gd.nx = c->grid.nx;
   gd.ny = c->grid.ny;
   gd.ncell = c->grid.ncell;
-  gd.cellStart = (const uint32_t *)c->cellStart.p;
-  gd.cellBox = (const int32_t *)c->cellBox.p;
-  gd.gx = (const int32_t *)c->gx.p;
-  gd.gy = (const int32_t *)c->gy.p;
-  gd.gpos = (const uint32_t *)c->gpos.p;
+  gd.cell2 = (const int4 *)c->cellRec.p;
+  gd.gpt = (const int4 *)c->gpt.p;
   gd.leafId = (const uint32_t *)c->leafId.p;
   uint32_t *tileN = (uint32_t *)c->tileN.p, *tileStart = (uint32_t *)c->tileStart.p;
   int32_t *owner = (int32_t *)c->owner.p;
