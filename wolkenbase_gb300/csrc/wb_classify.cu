@@ -45,16 +45,17 @@
  * -DWB_CLASSIFY_STATS (an instrumented build for tuning): per label,
  * 0 points, 1 near columns tested, 2 super-cells tested, 3 far columns
  * tested, 4 candidates read, 5 candidates inside, 6 surround tests,
- * 7 columns scanned. */
+ * 7 columns scanned; SM clock cycles 8 near field, 9 far field, 10 final
+ * gap, 11 whole point, 12 inside column scans, 13 inside surround tests. */
 #ifdef WB_CLASSIFY_STATS
-__device__ unsigned long long gClassifyStats[3][8];
+__device__ unsigned long long gClassifyStats[3][16];
 extern "C" int wb_classify_stats(unsigned long long *out, int reset)
 {
   if (cudaMemcpyFromSymbol(out, gClassifyStats, sizeof(gClassifyStats)) != cudaSuccess)
     return -3;
   if (reset)
   {
-    unsigned long long z[24] = {0};
+    unsigned long long z[48] = {0};
     cudaMemcpyToSymbol(gClassifyStats, z, sizeof(z));
   }
   return 0;
@@ -326,31 +327,120 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   // Directions are kept as exact per-bin extremes in shared memory plus a
   // 64-bit occupancy mask in registers (uniform across the warp).
   uint32_t occLo = 0, occHi = 0;
-  unsigned long long stat[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long stat[16] = {0};
+#ifdef WB_CLASSIFY_STATS
+  const long long tStart = clock64();
+#endif
   (void)stat;
-  // Adds the directions of column c's inside points; returns whether any was.
+  // Points of a column are sorted by height.  None above pz + (czp -
+  // sqrt(por^2 + s^2 d^2)) / sz, d the column's nearest distance, can be
+  // inside: colZlim gives that bound (with slack) in record units relative to
+  // the point.  Columns holding points outside the root cube in x or y get no
+  // bound (their blocks' cubes decide for them).
+  auto colZlim = [&](const int4 &box, const int4 &r1) -> int32_t {
+    if (!fast || r1.w || !(h.sz > 0))
+      return INT32_MAX;
+    float xl = (float)(box.x - h.qx) * h.sx, xh = (float)(box.z - h.qx) * h.sx;
+    float yl = (float)(box.y - h.qy) * h.sy, yh = (float)(box.w - h.qy) * h.sy;
+    float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
+    float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
+    float need = sqrtf(h.por2f + h.s2 * (dx * dx + dy * dy));
+    float dz = (h.czp - need + 1e-4f * (fabsf(h.czp) + need) + 1e-6f) / h.sz + 2.f;
+    return dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
+  };
+  // Whether candidate pt lies inside the hyperboloid, and its direction u.
+  auto testPoint = [&](const int4 &pt, uint32_t &u) -> bool {
+    bool in = false;
+    const int32_t qx = pt.x, qy = pt.y, qz = pt.z;
+    const uint32_t gp = (uint32_t)pt.w;
+    if (fast)
+    {
+      int32_t dxi = qx - h.qx, dyi = qy - h.qy;
+      // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
+      if (dxi != 0 || dyi != 0)
+      {
+        float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
+        if (gp & kStray)
+          in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
+        else
+        {
+          float dzm = (float)(h.qz - qz) * h.sz;
+          float zd = dzm + h.czp;
+          float r2 = h.s2 * (dx * dx + dy * dy);
+          float f = zd * zd - r2 - h.por2f;
+          float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
+          float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
+          if (zd > ztol && f > tol)
+            in = true;
+          else if (zd < -ztol || f < -tol)
+            in = false;
+          else if (a.fp32Only)
+            in = zd > 0 && f > 0;
+          else
+            in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
+        }
+        if (in)
+          u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+      }
+    }
+    else
+    {
+      double x = decA(a, 0, qx), y = decA(a, 1, qy);
+      if (wb_hypot(hx.px - x, hx.py - y) != 0 && memberExact(a, hx, gp, qx, qy, qz))
+      {
+        in = true;
+        int d = wb_atan2i(y - hx.py, x - hx.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
+        u = (uint32_t)d & 0x7fffffffu;
+      }
+    }
+    return in;
+  };
+  // Merges the directions of a chunk's inside lanes into the bins; returns
+  // whether any lane was inside.
+  auto merge = [&](bool in, uint32_t u) -> bool {
+    if (!__any_sync(0xffffffffu, in))
+      return false;
+    // Directions of nearby points usually share one bin: then one lane
+    // merges the warp's extremes; otherwise each lane does.
+    uint32_t bin = u >> 25;
+    uint32_t lo = __reduce_min_sync(0xffffffffu, in ? u : 0xffffffffu);
+    uint32_t hi = __reduce_max_sync(0xffffffffu, in ? u : 0u);
+    if ((lo >> 25) == (hi >> 25))
+    {
+      if (lane == 0)
+      {
+        atomicMin(&bminW[lo >> 25], lo);
+        atomicMax(&bmaxW[lo >> 25], hi);
+      }
+      if ((lo >> 25) < 32)
+        occLo |= 1u << (lo >> 25);
+      else
+        occHi |= 1u << ((lo >> 25) - 32);
+    }
+    else
+    {
+      if (in)
+      {
+        atomicMin(&bminW[bin], u);
+        atomicMax(&bmaxW[bin], u);
+      }
+      occLo |= __reduce_or_sync(0xffffffffu, in && bin < 32 ? 1u << bin : 0u);
+      occHi |= __reduce_or_sync(0xffffffffu, in && bin >= 32 ? 1u << (bin - 32) : 0u);
+    }
+    WB_STAT(stat[5], __popc(__ballot_sync(0xffffffffu, in)));
+    return true;
+  };
+  // Adds the directions of column cc's inside points; returns whether any was.
   auto column = [&](uint64_t cc) -> bool {
     WB_STAT(stat[7], 1);
+#ifdef WB_CLASSIFY_STATS
+    const long long tc = clock64();
+#endif
     bool got = false;
     const int4 box = a.col[2 * cc], r1 = a.col[2 * cc + 1];
-    uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
-    // Points of a column are sorted by height.  None above pz + (czp -
-    // sqrt(por^2 + s^2 d^2)) / sz, d the column's nearest distance, can be
-    // inside, so the scan stops at the first chunk past that height (with
-    // slack).  Columns holding points outside the root cube in x or y are
-    // read in full (their blocks' cubes decide for them).
-    int32_t zlim = INT32_MAX;
-    if (fast && !r1.w && h.sz > 0)
-    {
-      float xl = (float)(box.x - h.qx) * h.sx, xh = (float)(box.z - h.qx) * h.sx;
-      float yl = (float)(box.y - h.qy) * h.sy, yh = (float)(box.w - h.qy) * h.sy;
-      float dx = xl > 0 ? xl : (xh < 0 ? -xh : 0.f);
-      float dy = yl > 0 ? yl : (yh < 0 ? -yh : 0.f);
-      float need = sqrtf(h.por2f + h.s2 * (dx * dx + dy * dy));
-      float dz = (h.czp - need + 1e-4f * (fabsf(h.czp) + need) + 1e-6f) / h.sz + 2.f;
-      zlim = dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
-    }
-    for (uint32_t t0 = b; t0 < e; t0 += 32)
+    const uint32_t e = (uint32_t)r1.z;
+    const int32_t zlim = colZlim(box, r1);
+    for (uint32_t t0 = (uint32_t)r1.y; t0 < e; t0 += 32)
     {
       uint32_t t = t0 + lane;
       bool low = false;
@@ -360,95 +450,21 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         pt = a.gpt[t];
         low = zlim == INT32_MAX || pt.z - h.qz <= zlim;
       }
-      const int32_t qz = pt.z;
+      // the scan stops at the first chunk wholly past the height bound
       if (!__any_sync(0xffffffffu, low))
         break;
       WB_STAT(stat[4], __popc(__ballot_sync(0xffffffffu, low)));
-      bool in = false;
       uint32_t u = 0;
-      if (low)
-      {
-        int32_t qx = pt.x, qy = pt.y;
-        uint32_t gp = (uint32_t)pt.w;
-        if (fast)
-        {
-          int32_t dxi = qx - h.qx, dyi = qy - h.qy;
-          // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
-          if (dxi != 0 || dyi != 0)
-          {
-            float dx = (float)dxi * h.sx, dy = (float)dyi * h.sy;
-            if (gp & kStray)
-              in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
-            else
-            {
-              float dzm = (float)(h.qz - qz) * h.sz;
-              float zd = dzm + h.czp;
-              float r2 = h.s2 * (dx * dx + dy * dy);
-              float f = zd * zd - r2 - h.por2f;
-              float tol = 1e-5f * (zd * zd + r2 + h.por2f) + 1e-12f;
-              float ztol = 1e-5f * (fabsf(dzm) + fabsf(h.czp)) + 1e-12f;
-              if (zd > ztol && f > tol)
-                in = true;
-              else if (zd < -ztol || f < -tol)
-                in = false;
-              else if (a.fp32Only)
-                in = zd > 0 && f > 0;
-              else
-                in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
-            }
-            if (in)
-              u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
-          }
-        }
-        else
-        {
-          double x = decA(a, 0, qx), y = decA(a, 1, qy);
-          if (wb_hypot(hx.px - x, hx.py - y) != 0 && memberExact(a, hx, gp, qx, qy, qz))
-          {
-            in = true;
-            int d = wb_atan2i(y - hx.py, x - hx.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
-            u = (uint32_t)d & 0x7fffffffu;
-          }
-        }
-      }
-      if (!__any_sync(0xffffffffu, in))
-        continue;
-      // A chunk comes from one column, so its directions usually share one
-      // bin: then one lane merges the warp's extremes; otherwise each lane does.
-      uint32_t bin = u >> 25;
-      uint32_t lo = __reduce_min_sync(0xffffffffu, in ? u : 0xffffffffu);
-      uint32_t hi = __reduce_max_sync(0xffffffffu, in ? u : 0u);
-      if ((lo >> 25) == (hi >> 25))
-      {
-        if (lane == 0)
-        {
-          atomicMin(&bminW[lo >> 25], lo);
-          atomicMax(&bmaxW[lo >> 25], hi);
-        }
-        if ((lo >> 25) < 32)
-          occLo |= 1u << (lo >> 25);
-        else
-          occHi |= 1u << ((lo >> 25) - 32);
-      }
-      else
-      {
-        if (in)
-        {
-          atomicMin(&bminW[bin], u);
-          atomicMax(&bmaxW[bin], u);
-        }
-        occLo |= __reduce_or_sync(0xffffffffu, in && bin < 32 ? 1u << bin : 0u);
-        occHi |= __reduce_or_sync(0xffffffffu, in && bin >= 32 ? 1u << (bin - 32) : 0u);
-      }
-      WB_STAT(stat[5], __popc(__ballot_sync(0xffffffffu, in)));
-      got = true;
+      bool in = low && testPoint(pt, u);
+      got |= merge(in, u);
     }
+    WB_STAT(stat[12], clock64() - tc);
     return got;
   };
   // Surround test.  A circular run of 27 empty bins (151.9 degrees) already
   // proves a gap above 144 degrees plus both margins; only otherwise is the
   // exact largest gap formed from the bin extremes.
-  auto decide = [&]() {
+  auto decideBody = [&]() {
     WB_STAT(stat[6], 1);
     uint64_t occ = ((uint64_t)occHi << 32) | occLo;
     if (__popcll(occ) < 2)
@@ -467,6 +483,13 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     if (nocc >= 2)
       surrounded = (EXACT || !fast || a.fp32Only) ? gap < (uint32_t)WB_DEG144
                                                   : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+  };
+  auto decide = [&]() {
+#ifdef WB_CLASSIFY_STATS
+    const long long td = clock64();
+#endif
+    decideBody();
+    WB_STAT(stat[13], clock64() - td);
   };
   // Near field: rings of single columns around the point's column, each ring
   // visited in an order that alternates sides (stride 4k-1 over its 8k
@@ -505,6 +528,10 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       }
     }
   }
+#ifdef WB_CLASSIFY_STATS
+  const long long tNear = clock64();
+  stat[8] += tNear - tStart;
+#endif
   // Far field: rings of super-cells (WB_SUPER x WB_SUPER columns) pruned as a
   // block; columns already visited in the near field are skipped.
   const int S = WB_SUPER;
@@ -563,6 +590,10 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       }
     }
   }
+#ifdef WB_CLASSIFY_STATS
+  const long long tFar = clock64();
+  stat[9] += tFar - tNear;
+#endif
   if (!surrounded && fast && !a.fp32Only)
   {
     int nocc;
@@ -571,11 +602,13 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     ambiguous = nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
   }
 #ifdef WB_CLASSIFY_STATS
+  stat[10] += clock64() - tFar;
+  stat[11] += clock64() - tStart;
   if (lane == 0 && !EXACT)
   {
     int L = surrounded ? 1 : 2;
     atomicAdd(&gClassifyStats[L][0], 1ull);
-    for (int q = 1; q < 8; q++)
+    for (int q = 1; q < 16; q++)
       atomicAdd(&gClassifyStats[L][q], stat[q]);
   }
 #endif
