@@ -38,6 +38,12 @@ struct KeyArgs
   uint32_t stride;
   double off[3], scale[3], unit;
   double lo[3], cell;
+  /* Fixed-point form of the level-21 cell coordinate, per axis:
+     t(X) = (C + (X - x0) * R) / 2^shift, with |X - x0| <= dmax.  A point
+     whose fraction lies more than eps from an integer takes floor(t); the
+     rest (and all of an axis with fixed = 0) take the exact FP64 path. */
+  int fixed[3], shift[3];
+  long long x0[3], dmax[3], rfix[3], cfix[3], eps[3];
 };
 
 __device__ __forceinline__ void loadXYZ(const uint8_t *rec, uint32_t stride, uint64_t i, int32_t &x, int32_t &y,
@@ -71,8 +77,22 @@ __global__ void keyKernel(KeyArgs a, uint64_t *__restrict__ keys, uint32_t *__re
 #pragma unroll
     for (int ax = 0; ax < 3; ax++)
     {
-      double v = wb_decode(q[ax], a.off[ax], a.scale[ax], a.unit);
-      k[ax] = wb_cell_index(v, a.lo[ax], a.cell);
+      const long long d = (long long)q[ax] - a.x0[ax];
+      bool done = false;
+      if (a.fixed[ax] && d >= -a.dmax[ax] && d <= a.dmax[ax])
+      {
+        const long long tf = d * a.rfix[ax] + a.cfix[ax];
+        const long long k0 = tf >> a.shift[ax];
+        const long long fr = tf - k0 * (1ll << a.shift[ax]);
+        if (fr > a.eps[ax] && fr < (1ll << a.shift[ax]) - a.eps[ax])
+        {
+          const long long kMax = (1 << WB_LEVELS) - 1;
+          k[ax] = (uint32_t)(k0 < 0 ? 0 : (k0 > kMax ? kMax : k0));
+          done = true;
+        }
+      }
+      if (!done)
+        k[ax] = wb_cell_index(wb_decode(q[ax], a.off[ax], a.scale[ax], a.unit), a.lo[ax], a.cell);
     }
     keys[i] = wb_morton(k[0], k[1], k[2]);
     idx[i] = (uint32_t)i;
@@ -446,6 +466,46 @@ static unsigned gridFor(wb_ctx *c, uint64_t n, int threads = 256)
   return (unsigned)b;
 }
 
+/* Sets up the fixed-point cell coordinate of axis k (see KeyArgs).  t is
+ * the coordinate in cell units, (decode(X) - lo) / cell, linear in X up to
+ * the rounding of decode; the error allowed for (eps) covers the rounding of
+ * R and C to 2^-shift, the decode's two roundings and the double arithmetic
+ * here, with a factor of 16 to spare. */
+static void keyFixedPoint(const WbGeom &g, double mn, double mx, int k, KeyArgs &a)
+{
+  a.fixed[k] = 0;
+  a.shift[k] = 0;
+  a.x0[k] = a.dmax[k] = a.rfix[k] = a.cfix[k] = a.eps[k] = 0;
+  const double u = g.scale[k] * g.unit;
+  if (!(u > 0) || !(g.unit > 0) || !(g.cell > 0))
+    return;
+  const double R = u / g.cell;   // the cell is a power of two: exact
+  double xlo = (fmin(mn, mx) / g.unit - g.off[k]) / g.scale[k], xhi = (fmax(mn, mx) / g.unit - g.off[k]) / g.scale[k];
+  if (!(fabs(xlo) < 2e9) || !(fabs(xhi) < 2e9))
+    return;
+  const long long X0 = llround((xlo + xhi) / 2);
+  const long long dmax = (long long)ceil(fmax(fabs(xlo - X0), fabs(xhi - X0))) + 4;
+  const double x0d = (g.off[k] + g.scale[k] * (double)X0) * g.unit;
+  const double C = (x0d - g.root_lo[k]) / g.cell;
+  const double B = fabs(C) + (double)dmax * R + 4;
+  int shift = 62 - (int)ceil(log2(B));
+  if (shift > 40)
+    shift = 40;
+  if (shift < 24)
+    return;
+  const double one = ldexp(1.0, shift);
+  // decode error: two roundings of |x| (<= |x0d| + dmax*u) and the subtraction of lo
+  const double mag = fabs(x0d) + (double)dmax * u + fabs(g.root_lo[k]);
+  const double errCells = (double)dmax / one + 1.0 / one + 8 * ldexp(mag, -52) / g.cell + ldexp(B, -50);
+  a.fixed[k] = 1;
+  a.shift[k] = shift;
+  a.x0[k] = X0;
+  a.dmax[k] = dmax;
+  a.rfix[k] = llround(R * one);
+  a.cfix[k] = llround(C * one);
+  a.eps[k] = (long long)ceil(16 * errCells * one) + 16;
+}
+
 int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
 {
   if (!cl || !cl->records || cl->stride < 12)
@@ -487,6 +547,8 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   }
   a.unit = g.unit;
   a.cell = g.cell;
+  for (int k = 0; k < 3; k++)
+    keyFixedPoint(g, mn[k], mx[k], k, a);
 
   int rc;
   if (cl->device_resident)
