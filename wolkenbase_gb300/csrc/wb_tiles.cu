@@ -501,6 +501,36 @@ __device__ void rowOp3(double m[3][3], double b[3], int row0, int row1, int piv)
   }
 }
 
+/* The histogram sector of a bottom point (scan.cpp:96-106): 0 inside the
+ * inner circle hypot(x, y) < rin, else 1 + (rint(atan2(y, x) * 3 / pi) mod 6).
+ * FP32 decides wherever it is at least 1e-5 (relative) away from the circle
+ * and from a sector boundary (a half-integer of atan2 * 3 / pi); the rest is
+ * evaluated in FP64 exactly as the reference writes it. */
+__device__ __forceinline__ int sectorOf(double x, double y, double rin)
+{
+  const float xf = (float)x, yf = (float)y, rf = (float)rin;
+  const float r2 = xf * xf + yf * yf, rin2 = rf * rf;
+  bool inner;
+  if (r2 < rin2 * (1 - 1e-5f))
+    inner = true;
+  else if (r2 > rin2 * (1 + 1e-5f))
+    inner = false;
+  else
+    inner = wb_hypot(x, y) < rin;
+  if (inner)
+    return 0;
+  const float v = atan2f(yf, xf) * 0.954929658551372f;   // 3 / pi
+  const float half = floorf(v) + 0.5f;
+  int sector;
+  if (fabsf(v - half) > 1e-5f * (1.f + fabsf(v)))
+    sector = (int)rintf(v);
+  else
+    sector = (int)rint(atan2(y, x) * 3 / M_PI);
+  if (sector < 0)
+    sector += 6;
+  return (sector % 6) + 1;
+}
+
 __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRes *__restrict__ res)
 {
   __shared__ double part[kTileWarps][kQ][32];
@@ -685,14 +715,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
       double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
       double uz = z - (sy * y + sx * x);
       if (uz < bottom2 + 2 * a.rad)
-      {
-        sector = (int)rint(atan2(y, x) * 3 / M_PI);
-        if (sector < 0)
-          sector += 6;
-        sector = (sector % 6) + 1;
-        if (wb_hypot(x, y) < a.rad / 2.6457513110645905905016)
-          sector = 0;
-      }
+        sector = sectorOf(x, y, a.rad / 2.6457513110645905905016);
     }
     for (int sct = 0; sct < 7; sct++)
       histo[sct] += __popc(__ballot_sync(0xffffffffu, sector == sct));
