@@ -354,6 +354,7 @@ struct ScanArgs
 };
 
 constexpr int kQ = 8;   // summed quantities: xx, yx, yy, x, y, xz, yz, z
+constexpr int kScanCache = 224;   // tile points whose coordinates stay in shared memory
 
 __device__ __forceinline__ void counterMergeGroup(double *part, uint64_t i, double g)
 {
@@ -535,6 +536,8 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
 {
   __shared__ double part[kTileWarps][kQ][32];
   __shared__ double tail[kTileWarps][kQ][8];
+  // tile-local coordinates of tiles up to kScanCache points, decoded once
+  __shared__ double cxy[kTileWarps][3][kScanCache];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const TileArgs &a = s.t;
   uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
@@ -551,6 +554,23 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
   double cx, cy;
   tileCenter(a, k, cx, cy);
   uint64_t G = M / 8;   // complete groups of eight
+  const bool cached = M <= kScanCache;
+  // coordinates of tile point i: from the cache, or decoded again
+  auto coords = [&](uint32_t i, double &x, double &y, double &z) {
+    if (cached)
+    {
+      x = cxy[w][0][i];
+      y = cxy[w][1][i];
+      z = cxy[w][2][i];
+    }
+    else
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      x = dec(a, 0, a.sx[j]) - cx;
+      y = dec(a, 1, a.sy[j]) - cy;
+      z = dec(a, 2, a.sz[j]) - 0.0;
+    }
+  };
   for (uint32_t c0 = 0; c0 < M; c0 += 32)
   {
     uint32_t i = c0 + lane;
@@ -559,6 +579,12 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
     {
       uint32_t j = s.tilePts[b0 + i];
       double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      if (cached)
+      {
+        cxy[w][0][i] = x;
+        cxy[w][1][i] = y;
+        cxy[w][2][i] = z;
+      }
       q[0] = x * x;
       q[1] = y * x;
       q[2] = y * y;
@@ -657,8 +683,8 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
     double uz = INFINITY, ut = -INFINITY;
     if (i < M)
     {
-      uint32_t j = s.tilePts[b0 + i];
-      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double x, y, z;
+      coords(i, x, y, z);
       double zz = sy * y + sx * x;
       uz = z - zz;
       ut = uz;
@@ -695,8 +721,8 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
     double v = INFINITY;
     if (i < M && i < argmin)
     {
-      uint32_t j = s.tilePts[b0 + i];
-      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double x, y, z;
+      coords(i, x, y, z);
       v = z - (sy * y + sx * x);
     }
     for (int o = 16; o; o >>= 1)
@@ -711,8 +737,8 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
     int sector = -1;
     if (i < M)
     {
-      uint32_t j = s.tilePts[b0 + i];
-      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double x, y, z;
+      coords(i, x, y, z);
       double uz = z - (sy * y + sx * x);
       if (uz < bottom2 + 2 * a.rad)
         sector = sectorOf(x, y, a.rad / 2.6457513110645905905016);
