@@ -493,8 +493,9 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   };
   // Near field: rings of single columns around the point's column, each ring
   // visited in an order that alternates sides (stride 4k-1 over its 8k
-  // columns), with the surround test after every column.
-  const int kNear = 2;
+  // columns), with the surround test after every column.  One ring (nine
+  // columns) measured fastest; the super-cell rings take over beyond it.
+  const int kNear = 1;
   for (int ring = 0; ring <= kNear && ring <= kmax && !surrounded; ring++)
   {
     if (ci + ring < 0 || ci - ring >= a.nx || cj + ring < 0 || cj - ring >= a.ny)

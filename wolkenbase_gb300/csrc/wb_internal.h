@@ -38,7 +38,9 @@ struct GridInfo
   /* super-cells: blocks of WB_SUPER x WB_SUPER columns with their own bounds */
   int snx = 0, sny = 0;
 };
-#define WB_SUPER 4
+#define WB_SUPER 3
+/* a warp tests a super-cell's columns with one lane each */
+static_assert(WB_SUPER * WB_SUPER <= 32, "WB_SUPER^2 columns must fit the lanes of a warp");
 
 struct wb_ctx
 {
