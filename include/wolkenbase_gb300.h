@@ -36,9 +36,11 @@ extern "C" {
 #define WB_EBUSY -8       /* job already running or finished (wb_cancel)     */
 #define WB_ECANCELED -9   /* job was cancelled before it ran                 */
 
-/* Classify kernel shapes: warps per block / resident blocks per SM
- * (register cap): 0 = 8/3 (default), 1 = 4/6, 2 = 4/8, 3 = 8/4, 4 = 2/12. */
-#define WB_N_SHAPES 5
+/* Classify kernel shapes: one warp per point (0-4) or one warp per group of
+ * up to 32 points of a grid column (5-7), warps per block / resident blocks
+ * per SM (register cap): 0 = 8/3, 1 = 4/6, 2 = 4/8, 3 = 8/4, 4 = 2/12,
+ * 5 = groups 8/2, 6 = groups 4/4, 7 = groups 8/3. */
+#define WB_N_SHAPES 8
 
 typedef struct wb_ctx wb_ctx;
 

@@ -47,7 +47,7 @@ class wb_tile(C.Structure):
                 ("hyperboloid_size", C.c_double), ("height", C.c_double)]
 
 
-WB_N_SHAPES = 5
+WB_N_SHAPES = 8
 
 
 class wb_tuning(C.Structure):

@@ -103,6 +103,7 @@ struct ClsArgs
   uint64_t ncell;
   const int4 *col;     /* two int4 per column: {x0, y0, x1, y1}, {zmin, begin, end, flags} */
   const int4 *gpt;     /* int4 {X, Y, Z, position | stray bit} per point, column order */
+  const uint2 *groups; /* column groups: {column, first point} */
   int snx, sny;
   const int4 *super;   /* super-cell records, the column layout */
   double zmin;
@@ -113,6 +114,9 @@ struct ClsArgs
   /* ambiguous points for the exact pass */
   uint32_t *ambList;
   uint32_t *ambCount;
+  /* points a column group handed to the one-point kernel */
+  uint32_t *deferList;
+  uint32_t *deferCount;
   const uint32_t *work;   /* exact pass: store positions to classify */
   uint32_t nwork;
   /* finishing (fused launch): records, their store positions and class bytes */
@@ -621,6 +625,353 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   }
 }
 
+
+/* ---- Column groups: one warp classifies up to 32 points of one column,
+ * one lane per point ----
+ *
+ * The points of a grid column share their neighbourhood, so the warp walks
+ * the columns around the group once: every column and super-cell is tested
+ * against the group's envelope (the highest hyperboloid apex of its points,
+ * the smallest polar radius, the column's box as the points' position), and
+ * every candidate read is tested by all lanes against their own points
+ * (candidates are staged in shared memory and broadcast).  Each lane keeps
+ * its own direction extremes in 8 bins of 45 degrees: a gap of 144 degrees
+ * cannot hide inside a bin, so the largest gap formed from the bins' extremes
+ * is the exact largest gap of the lane's directions, up to the FP32 direction
+ * error (kMargin), exactly as in the one-point kernel.  A lane stops testing
+ * once its point is proven surrounded; the group ends when every lane has or
+ * the neighbourhood is exhausted.  Envelope tests and height bounds are
+ * conservative, so a lane that ends unsurrounded has seen every point inside
+ * its hyperboloid.  Clouds whose record differences do not fit FP32 send
+ * every point to the exact pass instead. */
+constexpr int kGroupBins = 8;
+constexpr int kDefer = 6;          // undecided lanes at or below which a group hands its points over
+constexpr int kGroupColumns = 256; // columns a group reads before it hands its undecided points over
+
+struct GroupSmem
+{
+  int4 cand[32];
+  uint32_t bmin[kGroupBins][32], bmax[kGroupBins][32];
+};
+
+__device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int lane, GroupSmem &sm)
+{
+  const uint64_t col = grp.x;
+  const int4 cbox = a.col[2 * col], cr1 = a.col[2 * col + 1];
+  const uint32_t ce = (uint32_t)cr1.z;
+  const int ci0 = (int)(col % (uint64_t)a.nx), cj0 = (int)(col / (uint64_t)a.nx);
+  const float sx = a.fsx, sy = a.fsy, sz = a.fsz, s2 = a.fs2;
+  const int32_t oz = cr1.x;   // height origin of the envelope: the column's lowest point
+  {
+    const uint32_t g = grp.y;
+    const uint32_t t = g + lane;
+    bool act = false;
+    int4 me = make_int4(0, 0, 0, 0);
+    PtSetup ps{};
+    uint32_t j = 0;
+    if (t < ce)
+    {
+      me = a.gpt[t];
+      j = (uint32_t)me.w & 0x7fffffffu;
+      if (a.owner[j] >= 0)
+      {
+        act = true;
+        ps = a.setup[j];
+      }
+      else
+        a.label[j] = 0;
+    }
+    if (!__any_sync(0xffffffffu, act))
+      return;
+#ifdef WB_CLASSIFY_STATS
+    const long long tG = clock64();
+    unsigned long long gst[8] = {0};
+#endif
+    if (!a.exactInts)
+    {
+      // FP32 differences are not exact for this cloud: the exact pass decides
+      if (act)
+      {
+        a.label[j] = 2;
+        a.ambList[atomicAdd(a.ambCount, 1u)] = j;
+      }
+      return;
+    }
+    for (int b = 0; b < kGroupBins; b++)
+    {
+      sm.bmin[b][lane] = 0xffffffffu;
+      sm.bmax[b][lane] = 0;
+    }
+    unsigned occ = 0;
+    bool done = !act;
+    // The envelope of the lanes still undecided: highest apex above oz,
+    // smallest polar radius, reach in rings.  It is formed again after every
+    // column read, so it shrinks as lanes are decided (a tall point proven
+    // surrounded no longer widens the search of the low ones).
+    float apex, por2min;
+    int kmaxG, smaxG;
+    const int offG = max(abs(ps.ci - ci0), abs(ps.cj - cj0));
+    auto envelope = [&]() {
+      apex = !done ? (float)(me.z - oz) * sz + ps.czp : -INFINITY;
+      por2min = !done ? ps.por2f : INFINITY;
+      kmaxG = !done ? ps.kmax + offG : 0;
+      smaxG = !done ? ps.smax + (offG + WB_SUPER - 1) / WB_SUPER + 1 : 0;
+      for (int o = 16; o; o >>= 1)
+      {
+        apex = fmaxf(apex, __shfl_xor_sync(0xffffffffu, apex, o));
+        por2min = fminf(por2min, __shfl_xor_sync(0xffffffffu, por2min, o));
+        kmaxG = max(kmaxG, __shfl_xor_sync(0xffffffffu, kmaxG, o));
+        smaxG = max(smaxG, __shfl_xor_sync(0xffffffffu, smaxG, o));
+      }
+    };
+    envelope();
+    bool deferred = false;
+    int columnsRead = 0;
+    const float czp = ps.czp, por2 = ps.por2f;
+    // envelope test of a box {x0, y0, x1, y1} with lowest point zmin
+    auto envMeets = [&](const int4 &b, int32_t zmin) -> bool {
+      if (b.x == INT32_MAX)
+        return false;
+      float dx = (float)max(0, max(b.x - cbox.z, cbox.x - b.z)) * sx;
+      float dy = (float)max(0, max(b.y - cbox.w, cbox.y - b.w)) * sy;
+      float zd = apex - (float)(zmin - oz) * sz;
+      float r2 = s2 * (dx * dx + dy * dy);
+      float mag = zd * zd + r2 + por2min;
+      if (zd < -1e-4f * (fabsf(zd) + 1e-3f))
+        return false;
+      return zd * zd - r2 - por2min >= -(1e-4f * mag + 1e-9f);
+    };
+    // height (record units above oz) above which no point of a column can be
+    // inside any lane's hyperboloid; columns holding points outside the root
+    // cube in x or y get no bound
+    auto envZlim = [&](const int4 &b, const int4 &r1) -> int32_t {
+      if (r1.w || !(sz > 0))
+        return INT32_MAX;
+      float dx = (float)max(0, max(b.x - cbox.z, cbox.x - b.z)) * sx;
+      float dy = (float)max(0, max(b.y - cbox.w, cbox.y - b.w)) * sy;
+      float need = sqrtf(por2min + s2 * (dx * dx + dy * dy));
+      float dz = (apex - need + 1e-4f * (fabsf(apex) + need) + 1e-6f) / sz + 2.f;
+      return dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
+    };
+    // the lane's surround test from its bins
+    auto decideLane = [&](uint32_t &worst) -> bool {
+      worst = 0;
+      if (__popc(occ) < 2)
+        return false;
+      for (int b = 0; b < kGroupBins; b++)
+        if ((occ >> b) & 1)
+        {
+          unsigned rest = occ >> (b + 1);
+          int nb = rest ? b + __ffs(rest) : __ffs(occ) - 1;
+          worst = max(worst, (sm.bmin[nb][lane] - sm.bmax[b][lane]) & 0x7fffffffu);
+        }
+      return a.fp32Only ? worst < (uint32_t)WB_DEG144 : worst + 2 * kMargin < (uint32_t)WB_DEG144;
+    };
+    // reads column cc's candidates below the envelope's height bound, each
+    // tested by every lane still undecided
+    auto scanColumn = [&](uint64_t cc) {
+      WB_STAT(gst[1], 1);
+      columnsRead++;
+      const int4 box = a.col[2 * cc], r1 = a.col[2 * cc + 1];
+      const uint32_t e = (uint32_t)r1.z;
+      const int32_t zl = envZlim(box, r1);
+      bool got = false;
+      for (uint32_t t0 = (uint32_t)r1.y; t0 < e; t0 += 32)
+      {
+        int4 q = make_int4(0, 0, 0, 0);
+        bool low = false;
+        if (t0 + lane < e)
+        {
+          q = a.gpt[t0 + lane];
+          low = zl == INT32_MAX || q.z - oz <= zl;
+        }
+        unsigned lm = __ballot_sync(0xffffffffu, low);
+        if (!lm)
+          break;
+        WB_STAT(gst[2], __popc(lm));
+        WB_STAT(gst[3], __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)));
+        sm.cand[lane] = q;
+        __syncwarp();
+        while (lm)
+        {
+          const int k = __ffs(lm) - 1;
+          lm &= lm - 1;
+          if (done)
+            continue;
+          const int4 c = sm.cand[k];
+          const int32_t dxi = c.x - me.x, dyi = c.y - me.y;
+          // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
+          if (dxi == 0 && dyi == 0)
+            continue;
+          const float dx = (float)dxi * sx, dy = (float)dyi * sy;
+          const uint32_t gp = (uint32_t)c.w;
+          bool in;
+          if (gp & kStray)
+            in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
+          else
+          {
+            float dzm = (float)(me.z - c.z) * sz;
+            float zd = dzm + czp;
+            float r2 = s2 * (dx * dx + dy * dy);
+            float f = zd * zd - r2 - por2;
+            float tol = 1e-5f * (zd * zd + r2 + por2) + 1e-12f;
+            float ztol = 1e-5f * (fabsf(dzm) + fabsf(czp)) + 1e-12f;
+            if (zd > ztol && f > tol)
+              in = true;
+            else if (zd < -ztol || f < -tol)
+              in = false;
+            else if (a.fp32Only)
+              in = zd > 0 && f > 0;
+            else
+              in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
+          }
+          if (in)
+          {
+            const uint32_t u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+            const int bin = (int)(u >> 28);
+            sm.bmin[bin][lane] = min(sm.bmin[bin][lane], u);
+            sm.bmax[bin][lane] = max(sm.bmax[bin][lane], u);
+            occ |= 1u << bin;
+            got = true;
+          }
+        }
+        __syncwarp();
+      }
+      uint32_t worst;
+      if (got && !done)
+        done = decideLane(worst);
+      if (__any_sync(0xffffffffu, got))
+        envelope();
+    };
+    // When few lanes remain undecided the warp would run at a fraction of its
+    // width, and a group whose neighbourhood is very large would hold one warp
+    // while the rest of the GPU idles: in both cases the undecided points go
+    // to the one-point kernel (kDefer lanes or fewer, or more than
+    // kGroupColumns columns read).
+    auto allDone = [&]() {
+      if (__all_sync(0xffffffffu, done))
+        return true;
+      if (__popc(__ballot_sync(0xffffffffu, !done)) > kDefer && columnsRead <= kGroupColumns)
+        return false;
+      if (!done)
+      {
+        deferred = true;
+        done = true;
+        a.deferList[atomicAdd(a.deferCount, 1u)] = j;
+      }
+      return true;
+    };
+    // near field: the group's column and the ring around it
+    const int kNearG = 1;
+    for (int ring = 0; ring <= kNearG && ring <= kmaxG && !allDone(); ring++)
+    {
+      const int ncells = ring == 0 ? 1 : 8 * ring;
+      const int stride = ring == 0 ? 1 : 4 * ring - 1;
+      uint64_t c = 0;
+      bool ok = false;
+      if (lane < ncells)
+      {
+        int di, dj;
+        ringCell(ring, (lane * stride) % ncells, di, dj);
+        int i = ci0 + di, jj = cj0 + dj;
+        if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
+        {
+          c = (uint64_t)jj * a.nx + i;
+          ok = envMeets(a.col[2 * c], a.col[2 * c + 1].x);
+        }
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, ok);
+      while (mask && !allDone())
+      {
+        const int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        scanColumn(__shfl_sync(0xffffffffu, c, src));
+      }
+    }
+    // far field: rings of super-cells, then their columns outside the near field
+    const int S = WB_SUPER;
+    const int si = ci0 / S, sj = cj0 / S;
+    for (int sr = 0; sr <= smaxG && kmaxG > kNearG && !allDone(); sr++)
+    {
+      if (si + sr < 0 || si - sr >= a.snx || sj + sr < 0 || sj - sr >= a.sny)
+        continue;
+      const int nsc = sr == 0 ? 1 : 8 * sr;
+      for (int m0 = 0; m0 < nsc && !allDone(); m0 += 32)
+      {
+        const int m = m0 + lane;
+        int SI = 0, SJ = 0;
+        bool ok = false;
+        if (m < nsc)
+        {
+          int di, dj;
+          ringCell(sr, m, di, dj);
+          SI = si + di;
+          SJ = sj + dj;
+          if (SI >= 0 && SI < a.snx && SJ >= 0 && SJ < a.sny)
+          {
+            const uint64_t sc = (uint64_t)SJ * a.snx + SI;
+            ok = envMeets(a.super[2 * sc], a.super[2 * sc + 1].x);
+          }
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, ok);
+        while (mask && !allDone())
+        {
+          const int src = __ffs(mask) - 1;
+          mask &= mask - 1;
+          const int bi = __shfl_sync(0xffffffffu, SI, src) * S, bj = __shfl_sync(0xffffffffu, SJ, src) * S;
+          uint64_t c = 0;
+          bool cok = false;
+          if (lane < S * S)
+          {
+            const int i = bi + lane % S, jj = bj + lane / S;
+            if (i < a.nx && jj < a.ny && max(abs(i - ci0), abs(jj - cj0)) > kNearG)
+            {
+              c = (uint64_t)jj * a.nx + i;
+              cok = envMeets(a.col[2 * c], a.col[2 * c + 1].x);
+            }
+          }
+          unsigned cm = __ballot_sync(0xffffffffu, cok);
+          while (cm && !allDone())
+          {
+            const int cs = __ffs(cm) - 1;
+            cm &= cm - 1;
+            scanColumn(__shfl_sync(0xffffffffu, c, cs));
+          }
+        }
+      }
+    }
+#ifdef WB_CLASSIFY_STATS
+    if (lane == 0)
+    {
+      gst[0] = 1;
+      gst[4] = __popc(__ballot_sync(0xffffffffu, act));
+      gst[5] = __popc(__ballot_sync(0xffffffffu, deferred));
+      gst[6] = clock64() - tG;
+      gst[7] = smaxG;
+      for (int q = 0; q < 8; q++)
+        atomicAdd(&gClassifyStats[0][q], gst[q]);
+    }
+    else
+    {
+      __ballot_sync(0xffffffffu, act);
+      __ballot_sync(0xffffffffu, deferred);
+    }
+#endif
+    if (act && !deferred)
+    {
+      uint32_t worst = 0;
+      bool amb = false;
+      if (!done)
+      {
+        decideLane(worst);
+        amb = !a.fp32Only && __popc(occ) >= 2 && worst < (uint32_t)WB_DEG144 + 2 * kMargin;
+      }
+      a.label[j] = done ? 1 : 2;
+      if (amb)
+        a.ambList[atomicAdd(a.ambCount, 1u)] = j;
+    }
+  }
+}
 }  // namespace
 
 /* Decoding is strictly increasing in every record integer when the step
@@ -652,7 +1003,8 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   int rc;
   uint64_t nd = c->nd, n = c->n;
   if ((rc = wb_ensure(c, c->label, nd + 64)) || (rc = wb_ensure(c, c->angleT, (511 + 512 + 512) * 8)) ||
-      (rc = wb_ensure(c, c->ambiguous, nd * 4 + 64)) || (rc = wb_ensure(c, c->ptSetup, nd * sizeof(PtSetup) + 64)))
+      (rc = wb_ensure(c, c->ambiguous, nd * 4 + 64)) || (rc = wb_ensure(c, c->ptSetup, nd * sizeof(PtSetup) + 64)) ||
+      (rc = wb_ensure(c, c->deferred, nd * 4 + 64)))
     return rc;
   if (!onDevice && (rc = wb_ensure(c, c->clsDev, n + 64)))
     return rc;
@@ -699,6 +1051,7 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.ncell = c->grid.ncell;
   a.col = (const int4 *)c->cellRec.p;
   a.gpt = (const int4 *)c->gpt.p;
+  a.groups = (const uint2 *)c->groups.p;
   a.snx = c->grid.snx;
   a.sny = c->grid.sny;
   a.super = (const int4 *)c->superRec.p;
@@ -715,13 +1068,15 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.setup = (PtSetup *)c->ptSetup.p;
   a.ambList = (uint32_t *)c->ambiguous.p;
   a.ambCount = (uint32_t *)((char *)c->small.p + 448);
+  a.deferList = (uint32_t *)c->deferred.p;
+  a.deferCount = (uint32_t *)((char *)c->small.p + 452);
   a.work = nullptr;
   a.nwork = 0;
   a.n = n;
   a.nTiles = c->n_tiles;
   a.storeOf = (const uint32_t *)c->storeOf.p;
   a.cls = clsDev;
-  WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 4, c->stream));
+  WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 8, c->stream));   // ambiguous and deferred counts
   return 0;
 }
 
@@ -740,13 +1095,15 @@ namespace
 struct BatchHdr
 {
   int k, chunk;
-  unsigned long long next[2];   /* work counters of the fast and the exact pass */
+  unsigned long long next[3];   /* work counters: fast pass, deferred points, exact pass */
   uint64_t startNd[WB_BATCH_MAX + 1], startN[WB_BATCH_MAX + 1], startT[WB_BATCH_MAX + 1];
+  uint64_t startGrp[WB_BATCH_MAX + 1];   /* column groups (the column-group fast pass) */
   ClsArgs jobs[WB_BATCH_MAX];
 };
 struct BatchOut
 {
   uint64_t startAmb[WB_BATCH_MAX + 1];   /* prefix of the jobs' ambiguous counts */
+  uint64_t startDef[WB_BATCH_MAX + 1];   /* prefix of the jobs' deferred counts */
   unsigned long long ground[WB_BATCH_MAX];
 };
 
@@ -776,22 +1133,25 @@ __global__ void batchSetup(const BatchHdr *__restrict__ h)
   }
 }
 
-template <bool EXACT, int W, int MINB>
+/* MODE 0: every point of every job; 1: the points column groups deferred;
+ * 2: the ambiguous points (exact pass). */
+template <int MODE, int W, int MINB>
 __global__ void __launch_bounds__(32 * W, MINB) batchRings(BatchHdr *h, const BatchOut *o)
 {
+  constexpr bool EXACT = MODE == 2;
   __shared__ uint32_t bmin[W][kBins], bmax[W][kBins];
   __shared__ ClsArgs sa[W];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int k = h->k;
-  const uint64_t *start = EXACT ? o->startAmb : h->startNd;
+  const uint64_t *start = MODE == 2 ? o->startAmb : (MODE == 1 ? o->startDef : h->startNd);
   const uint64_t total = start[k];
-  const unsigned chunk = EXACT ? 1u : (unsigned)h->chunk;
+  const unsigned chunk = MODE == 0 ? (unsigned)h->chunk : 1u;
   uint64_t lo = 1, hi = 0;
   for (;;)
   {
     unsigned long long base = 0;
     if (lane == 0)
-      base = atomicAdd(&h->next[EXACT ? 1 : 0], (unsigned long long)chunk);
+      base = atomicAdd(&h->next[MODE], (unsigned long long)chunk);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= total)
       break;
@@ -812,22 +1172,67 @@ __global__ void __launch_bounds__(32 * W, MINB) batchRings(BatchHdr *h, const Ba
       }
       const ClsArgs &a = sa[w];
       uint64_t item = g - lo;
-      classifyPoint<EXACT>(a, EXACT ? a.ambList[item] : item, lane, bmin[w], bmax[w]);
+      classifyPoint<EXACT>(a, MODE == 2 ? a.ambList[item] : (MODE == 1 ? a.deferList[item] : item), lane, bmin[w],
+                           bmax[w]);
     }
   }
 }
 
-__global__ void batchAmbPrefix(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
+/* The fast pass by column groups: warps take chunks of groups (of all jobs)
+ * from a global counter. */
+template <int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) batchGroups(BatchHdr *h, const BatchOut *o)
+{
+  __shared__ GroupSmem gsm[W];
+  __shared__ ClsArgs sa[W];
+  (void)o;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = h->k;
+  const uint64_t *start = h->startGrp;
+  const uint64_t total = start[k];
+  const unsigned chunk = (unsigned)h->chunk;
+  uint64_t lo = 1, hi = 0;
+  for (;;)
+  {
+    unsigned long long base = 0;
+    if (lane == 0)
+      base = atomicAdd(&h->next[0], (unsigned long long)chunk);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total)
+      break;
+    uint64_t end = base + chunk < total ? base + chunk : total;
+    for (uint64_t g = base; g < end; g++)
+    {
+      if (g < lo || g >= hi)
+      {
+        int q = batchJob(start, k, g);
+        lo = start[q];
+        hi = start[q + 1];
+        __syncwarp();
+        const uint32_t *src = (const uint32_t *)&h->jobs[q];
+        uint32_t *dst = (uint32_t *)&sa[w];
+        for (int i = lane; i < (int)(sizeof(ClsArgs) / 4); i += 32)
+          dst[i] = src[i];
+        __syncwarp();
+      }
+      classifyGroup(sa[w], sa[w].groups[g - lo], lane, gsm[w]);
+    }
+  }
+}
+
+/* Prefix of the jobs' deferred (which = 0) or ambiguous (which = 1) counts. */
+__global__ void batchPrefix(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o, int which)
 {
   if (threadIdx.x || blockIdx.x)
     return;
+  uint64_t *out = which ? o->startAmb : o->startDef;
   uint64_t s = 0;
   for (int q = 0; q < h->k; q++)
   {
-    o->startAmb[q] = s;
-    s += *h->jobs[q].ambCount;
+    out[q] = s;
+    s += which ? *h->jobs[q].ambCount : *h->jobs[q].deferCount;
   }
-  o->startAmb[h->k] = s;
+  out[h->k] = s;
 }
 
 __global__ void batchZeroGround(const BatchHdr *__restrict__ h)
@@ -905,40 +1310,51 @@ struct WbBatch
   cudaStream_t capture = nullptr;
   BatchHdr *dIn = nullptr, *hIn = nullptr;
   BatchOut *dOut = nullptr, *hOut = nullptr;
-  int per[WB_N_SHAPES + 1] = {0};   /* resident blocks per SM of each ring kernel (+ exact) */
+  int per[WB_N_SHAPES + 2] = {0};   /* resident blocks per SM of each classify kernel */
   cudaGraphExec_t graphs[WB_N_SHAPES] = {nullptr};
 };
 
-const WbShape kWbShapes[WB_N_SHAPES] = {{8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}};
+const WbShape kWbShapes[WB_N_SHAPES] = {{8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}, {8, 2}, {4, 4}, {8, 3}};
 
 namespace
 {
 typedef void (*RingsFn)(BatchHdr *, const BatchOut *);
 
-/* shape WB_N_SHAPES is the exact pass */
-RingsFn ringsFn(int shape)
+/* Kernels of the fused classify: 0..WB_N_SHAPES-1 the fast pass of each
+ * shape (one point per warp, or column groups), kDeferred the one-point pass
+ * over the points column groups handed over, kExactPass the exact pass. */
+constexpr int kDeferred = WB_N_SHAPES, kExactPass = WB_N_SHAPES + 1;
+
+RingsFn ringsFn(int idx)
 {
-  // kWbShapes: about 85 or 64 registers a thread
-  switch (shape)
+  // kWbShapes: about 85 or 64 registers a thread (groups: 126 or 80)
+  switch (idx)
   {
-  case 1: return batchRings<false, 4, 6>;
-  case 2: return batchRings<false, 4, 8>;
-  case 3: return batchRings<false, 8, 4>;
-  case 4: return batchRings<false, 2, 12>;
-  case WB_N_SHAPES: return batchRings<true, 4, 6>;
-  default: return batchRings<false, 8, 3>;
+  case 1: return batchRings<0, 4, 6>;
+  case 2: return batchRings<0, 4, 8>;
+  case 3: return batchRings<0, 8, 4>;
+  case 4: return batchRings<0, 2, 12>;
+  case 5: return batchGroups<8, 2>;
+  case 6: return batchGroups<4, 4>;
+  case 7: return batchGroups<8, 3>;
+  case kDeferred: return batchRings<1, 8, 3>;
+  case kExactPass: return batchRings<2, 4, 6>;
+  default: return batchRings<0, 8, 3>;
   }
 }
 
-int ringsWarps(int shape)
+int ringsWarps(int idx)
 {
-  return shape == WB_N_SHAPES ? 4 : kWbShapes[shape].warps;
+  return idx == kExactPass ? 4 : (idx == kDeferred ? 8 : kWbShapes[idx].warps);
 }
 
 __global__ void batchAmbReset(const BatchHdr *__restrict__ h)
 {
   for (int q = threadIdx.x; q < h->k; q += blockDim.x)
+  {
     *h->jobs[q].ambCount = 0;
+    *h->jobs[q].deferCount = 0;
+  }
 }
 
 /* Persistent grid of a ring kernel: every SM filled to its occupancy
@@ -962,7 +1378,7 @@ cudaError_t ringsGrid(WbBatch *b, int shape, unsigned *grid)
  * persistent fast pass, the ambiguous prefix, the persistent exact pass,
  * ground counts, the class-byte scatter and the read-back of the per-job
  * totals (8 kernels).  With mark, stage events go on mark's stream. */
-cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned grids[2], wb_ctx *mark)
+cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned grids[3], wb_ctx *mark)
 {
   const unsigned grid = (unsigned)b->sm * 8;
   cudaError_t e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
@@ -970,10 +1386,12 @@ cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned g
     return e;
   batchSetup<<<grid, 256, 0, s>>>(b->dIn);
   ringsFn(shape)<<<grids[0], 32 * ringsWarps(shape), 0, s>>>(b->dIn, b->dOut);
+  batchPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut, 0);
+  ringsFn(kDeferred)<<<grids[1], 32 * ringsWarps(kDeferred), 0, s>>>(b->dIn, b->dOut);
   if (mark)
     wb_mark(mark, "classify");
-  batchAmbPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut);
-  ringsFn(WB_N_SHAPES)<<<grids[1], 32 * ringsWarps(WB_N_SHAPES), 0, s>>>(b->dIn, b->dOut);
+  batchPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut, 1);
+  ringsFn(kExactPass)<<<grids[2], 32 * ringsWarps(kExactPass), 0, s>>>(b->dIn, b->dOut);
   if (mark)
     wb_mark(mark, "classify_exact");
   batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
@@ -986,12 +1404,21 @@ cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned g
   return e;
 }
 
-cudaError_t captureBatch(WbBatch *b, int shape, cudaGraphExec_t *exec)
+/* The three classify grids of a shape. */
+cudaError_t batchGrids(WbBatch *b, int shape, unsigned grids[3])
 {
-  unsigned grids[2];
   cudaError_t e = ringsGrid(b, shape, &grids[0]);
   if (e == cudaSuccess)
-    e = ringsGrid(b, WB_N_SHAPES, &grids[1]);
+    e = ringsGrid(b, kDeferred, &grids[1]);
+  if (e == cudaSuccess)
+    e = ringsGrid(b, kExactPass, &grids[2]);
+  return e;
+}
+
+cudaError_t captureBatch(WbBatch *b, int shape, cudaGraphExec_t *exec)
+{
+  unsigned grids[3];
+  cudaError_t e = batchGrids(b, shape, grids);
   if (e != cudaSuccess)
     return e;
   cudaGraph_t graph = nullptr;
@@ -1021,8 +1448,8 @@ int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample
   BatchHdr *h = b->hIn;
   h->k = k;
   h->chunk = chunk < 1 ? 4 : chunk;
-  h->next[0] = h->next[1] = 0;
-  h->startNd[0] = h->startN[0] = h->startT[0] = 0;
+  h->next[0] = h->next[1] = h->next[2] = 0;
+  h->startNd[0] = h->startN[0] = h->startT[0] = h->startGrp[0] = 0;
   for (int q = 0; q < k; q++)
   {
     wb_ctx *c = jobs[q];
@@ -1038,6 +1465,10 @@ int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample
     h->startNd[q + 1] = h->startNd[q] + nd;
     h->startN[q + 1] = h->startN[q] + c->n;
     h->startT[q + 1] = h->startT[q] + c->n_tiles;
+    uint64_t ng = c->grid.nGroups;
+    if (sample && c->nd)
+      ng = (uint64_t)((double)ng * (double)(h->startNd[q + 1] - h->startNd[q]) / (double)c->nd + 0.999);
+    h->startGrp[q + 1] = h->startGrp[q] + ng;
   }
   return 0;
 }
@@ -1114,9 +1545,9 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
   if (rc)
     return rc;
   cudaSetDevice(b->device);
-  unsigned grid = 0;
+  unsigned grids[3];
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaError_t e = ringsGrid(b, shape, &grid);
+  cudaError_t e = batchGrids(b, shape, grids);
   if (e == cudaSuccess)
     e = cudaEventCreate(&e0);
   if (e == cudaSuccess)
@@ -1127,7 +1558,9 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
   {
     batchSetup<<<(unsigned)b->sm * 8, 256, 0, s>>>(b->dIn);
     cudaEventRecord(e0, s);
-    ringsFn(shape)<<<grid, 32 * ringsWarps(shape), 0, s>>>(b->dIn, b->dOut);
+    ringsFn(shape)<<<grids[0], 32 * ringsWarps(shape), 0, s>>>(b->dIn, b->dOut);
+    batchPrefix<<<1, 32, 0, s>>>(b->dIn, b->dOut, 0);
+    ringsFn(kDeferred)<<<grids[1], 32 * ringsWarps(kDeferred), 0, s>>>(b->dIn, b->dOut);
     cudaEventRecord(e1, s);
     batchAmbReset<<<1, 256, 0, s>>>(b->dIn);
     e = cudaGetLastError();
@@ -1181,7 +1614,7 @@ int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int 
     return WB_ECUDA;
   }
   if (launches)
-    *launches += 8;   /* kernel nodes of the graph */
+    *launches += 10;   /* kernel nodes of the graph */
   return 0;
 }
 
@@ -1213,11 +1646,10 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   int shape = clampShape(c->shape);
   if ((rc = fillTable(b, &c, 1, c->chunk, 0, err)))
     return wb_fail(c, rc, "wb_classify: " + err);
-  unsigned grids[2];
-  WB_CUDA(c, ringsGrid(b, shape, &grids[0]));
-  WB_CUDA(c, ringsGrid(b, WB_N_SHAPES, &grids[1]));
+  unsigned grids[3];
+  WB_CUDA(c, batchGrids(b, shape, grids));
   WB_CUDA(c, enqueueBatch(b, c->stream, shape, grids, c));
-  c->launches += 8;
+  c->launches += 10;
   ClsArgs *a = (ClsArgs *)c->clsArgs;
   if (!onDevice && c->n)
     WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDeviceToHost, c->stream));

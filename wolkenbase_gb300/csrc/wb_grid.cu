@@ -117,6 +117,29 @@ __global__ void cellFillKernel(uint64_t ncell, const uint32_t *__restrict__ star
   }
 }
 
+/* Column groups (the classify work items): a column of n points is
+ * ceil(n / 32) groups of consecutive points. */
+__global__ void groupCountKernel(uint64_t ncell, const int4 *__restrict__ rec, uint32_t *__restrict__ cnt)
+{
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int4 r1 = rec[2 * c + 1];
+    cnt[c] = ((uint32_t)(r1.z - r1.y) + 31) / 32;
+  }
+}
+
+__global__ void groupFillKernel(uint64_t ncell, const int4 *__restrict__ rec, const uint32_t *__restrict__ first,
+                                uint2 *__restrict__ groups)
+{
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (uint64_t)gridDim.x * blockDim.x)
+  {
+    int4 r1 = rec[2 * c + 1];
+    uint32_t g = first[c];
+    for (uint32_t t = (uint32_t)r1.y; t < (uint32_t)r1.z; t += 32)
+      groups[g++] = make_uint2((uint32_t)c, t);
+  }
+}
+
 /* Record-integer extent of the cloud: out[0..2] minima, out[3..5] maxima. */
 __global__ void extentKernel(uint64_t nd, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                              const int32_t *__restrict__ sz, int *__restrict__ out)
@@ -245,12 +268,29 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
     return rc;
   { superKernel<<<(unsigned)std::min<uint64_t>((nsup + 255) / 256, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(
         nx, ny, snx, sny, (const int4 *)c->cellRec.p, (int4 *)c->superRec.p); ++c->launches; }
+  // column groups: counts, their prefix, the list
+  uint32_t *gTot = (uint32_t *)((char *)c->small.p + 640);
+  if ((rc = wb_ensure(c, c->groupCnt, (ncell + 1) * 8 + 64)))
+    return rc;
+  uint32_t *gcnt = (uint32_t *)c->groupCnt.p, *gfirst = gcnt + ncell + 1;
+  { groupCountKernel<<<(unsigned)std::min<uint64_t>((ncell + 255) / 256, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        ncell, (const int4 *)c->cellRec.p, gcnt); ++c->launches; }
+  if ((rc = wb_exclusive_scan_u32(c, gcnt, gfirst, ncell, gTot)))
+    return rc;
+  // at most nd / 32 + ncell groups
+  if ((rc = wb_ensure(c, c->groups, (nd / 32 + ncell + 1) * 8 + 64)))
+    return rc;
+  { groupFillKernel<<<(unsigned)std::min<uint64_t>((ncell + 255) / 256, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        ncell, (const int4 *)c->cellRec.p, gfirst, (uint2 *)c->groups.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   unsigned long long ns = 0;
+  uint32_t ngroups = 0;
   int ext[6];
   WB_CUDA(c, cudaMemcpyAsync(&ns, dStray, 8, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaMemcpyAsync(ext, dExt, 24, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&ngroups, gTot, 4, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->grid.nGroups = ngroups;
   c->grid.nStray = ns;
   c->grid.zminInt = ext[2];
   for (int k = 0; k < 3; k++)

@@ -37,6 +37,7 @@ struct GridInfo
   int32_t imin[3] = {0, 0, 0}, imax[3] = {0, 0, 0};   /* record-integer extent of the cloud */
   /* super-cells: blocks of WB_SUPER x WB_SUPER columns with their own bounds */
   int snx = 0, sny = 0;
+  uint64_t nGroups = 0;             /* column groups of up to 32 points */
 };
 #define WB_SUPER 3
 /* a warp tests a super-cell's columns with one lane each */
@@ -69,12 +70,13 @@ struct wb_ctx
   DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
-  DevBuf label, clsDev, ambiguous, angleT;
+  DevBuf label, clsDev, ambiguous, deferred, angleT;
   /* column grid (wb_grid.cu): gpt holds one int4 {X, Y, Z, store position |
      stray bit} per point in column order; cellRec two int4 per column,
      {x0, y0, x1, y1} and {zmin, begin, end, flags}, x0 == INT32_MAX for an
      empty column; superRec the same two int4 per super-cell */
   DevBuf gKey0, gKey1, gVal0, gVal1, stray, cellStart, gpt, cellRec, superRec, ptSetup;
+  DevBuf groups, groupCnt;          /* column groups: uint2 {column, first point} of up to 32 points */
   GridInfo grid;
   /* fused fast-pass settings (wb_set_tuning; a server's autotuner picks them
      per batch): kernel shape, work chunk and points per grid column */
