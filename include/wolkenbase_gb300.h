@@ -36,10 +36,10 @@ extern "C" {
 #define WB_EBUSY -8       /* job already running or finished (wb_cancel)     */
 #define WB_ECANCELED -9   /* job was cancelled before it ran                 */
 
-/* Classify kernel shapes: one warp per point (0-4) or one warp per group of
- * up to 32 points of a grid column (5-7), warps per block / resident blocks
- * per SM (register cap): 0 = 8/3, 1 = 4/6, 2 = 4/8, 3 = 8/4, 4 = 2/12,
- * 5 = groups 8/2, 6 = groups 4/4, 7 = groups 8/3. */
+/* Classify kernel shapes: one warp per group of up to 32 points of a grid
+ * column (0-2) or one warp per point (3-7); warps per block / resident blocks
+ * per SM (register cap): 0 = groups 4/5 (default), 1 = groups 8/3,
+ * 2 = groups 8/2, 3 = 8/3, 4 = 4/6, 5 = 4/8, 6 = 8/4, 7 = 2/12. */
 #define WB_N_SHAPES 8
 
 typedef struct wb_ctx wb_ctx;
@@ -246,7 +246,7 @@ typedef struct
   int flush;             /* WB_FLUSH_EAGER or WB_FLUSH_FULL                         */
   int max_batch;         /* most jobs in one fused classify launch; 0 = 512 (max)   */
   int shape;             /* fused fast-pass kernel shape, 0..WB_N_SHAPES-1 (below)  */
-  int chunk;             /* points a warp takes per visit to the work counter; 0 = 4 */
+  int chunk;             /* groups (or points) a warp takes per visit to the work counter; 0 = 1 */
   double grid_points;    /* points per column of the neighbour grid; 0 = 64         */
   int autotune;          /* 1: on the first batch, time column densities, kernel
                             shapes and chunks on a sample and keep the fastest     */

@@ -776,64 +776,91 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       const uint32_t e = (uint32_t)r1.z;
       const int32_t zl = envZlim(box, r1);
       bool got = false;
+      // the lane's test of candidate c against its own point
+      auto testOne = [&](const int4 &c, uint32_t &u) -> bool {
+        const int32_t dxi = c.x - me.x, dyi = c.y - me.y;
+        // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
+        if (dxi == 0 && dyi == 0)
+          return false;
+        const float dx = (float)dxi * sx, dy = (float)dyi * sy;
+        const uint32_t gp = (uint32_t)c.w;
+        bool in;
+        if (gp & kStray)
+          in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
+        else
+        {
+          float dzm = (float)(me.z - c.z) * sz;
+          float zd = dzm + czp;
+          float r2 = s2 * (dx * dx + dy * dy);
+          float f = zd * zd - r2 - por2;
+          float tol = 1e-5f * (zd * zd + r2 + por2) + 1e-12f;
+          float ztol = 1e-5f * (fabsf(dzm) + fabsf(czp)) + 1e-12f;
+          if (zd > ztol && f > tol)
+            in = true;
+          else if (zd < -ztol || f < -tol)
+            in = false;
+          else if (a.fp32Only)
+            in = zd > 0 && f > 0;
+          else
+            in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
+        }
+        if (in)
+          u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+        return in;
+      };
+      auto addDir = [&](uint32_t u) {
+        const int bin = (int)(u >> 28);
+        sm.bmin[bin][lane] = min(sm.bmin[bin][lane], u);
+        sm.bmax[bin][lane] = max(sm.bmax[bin][lane], u);
+        occ |= 1u << bin;
+        got = true;
+      };
       for (uint32_t t0 = (uint32_t)r1.y; t0 < e; t0 += 32)
       {
         int4 q = make_int4(0, 0, 0, 0);
-        bool low = false;
+        bool low = false, keep = false;
         if (t0 + lane < e)
         {
           q = a.gpt[t0 + lane];
           low = zl == INT32_MAX || q.z - oz <= zl;
+          // can q be inside the hyperboloid of any undecided lane?  (its own
+          // distance to the group's column; points outside the root cube are
+          // left to the exact test)
+          keep = low;
+          if (low && !((uint32_t)q.w & kStray))
+          {
+            float ex = (float)max(0, max(q.x - cbox.z, cbox.x - q.x)) * sx;
+            float ey = (float)max(0, max(q.y - cbox.w, cbox.y - q.y)) * sy;
+            float zd = apex - (float)(q.z - oz) * sz;
+            float r2 = s2 * (ex * ex + ey * ey);
+            float mag = zd * zd + r2 + por2min;
+            keep = zd >= -1e-4f * (fabsf(zd) + 1e-3f) && zd * zd - r2 - por2min >= -(1e-4f * mag + 1e-9f);
+          }
         }
-        unsigned lm = __ballot_sync(0xffffffffu, low);
-        if (!lm)
+        if (!__any_sync(0xffffffffu, low))
           break;
+        unsigned lm = __ballot_sync(0xffffffffu, keep);
         WB_STAT(gst[2], __popc(lm));
         WB_STAT(gst[3], __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)));
         sm.cand[lane] = q;
         __syncwarp();
+        // two candidates per step: independent work for the scheduler
         while (lm)
         {
-          const int k = __ffs(lm) - 1;
+          const int k1 = __ffs(lm) - 1;
           lm &= lm - 1;
+          const int k2 = lm ? __ffs(lm) - 1 : -1;
+          if (k2 >= 0)
+            lm &= lm - 1;
           if (done)
             continue;
-          const int4 c = sm.cand[k];
-          const int32_t dxi = c.x - me.x, dyi = c.y - me.y;
-          // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
-          if (dxi == 0 && dyi == 0)
-            continue;
-          const float dx = (float)dxi * sx, dy = (float)dyi * sy;
-          const uint32_t gp = (uint32_t)c.w;
-          bool in;
-          if (gp & kStray)
-            in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
-          else
-          {
-            float dzm = (float)(me.z - c.z) * sz;
-            float zd = dzm + czp;
-            float r2 = s2 * (dx * dx + dy * dy);
-            float f = zd * zd - r2 - por2;
-            float tol = 1e-5f * (zd * zd + r2 + por2) + 1e-12f;
-            float ztol = 1e-5f * (fabsf(dzm) + fabsf(czp)) + 1e-12f;
-            if (zd > ztol && f > tol)
-              in = true;
-            else if (zd < -ztol || f < -tol)
-              in = false;
-            else if (a.fp32Only)
-              in = zd > 0 && f > 0;
-            else
-              in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
-          }
-          if (in)
-          {
-            const uint32_t u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
-            const int bin = (int)(u >> 28);
-            sm.bmin[bin][lane] = min(sm.bmin[bin][lane], u);
-            sm.bmax[bin][lane] = max(sm.bmax[bin][lane], u);
-            occ |= 1u << bin;
-            got = true;
-          }
+          uint32_t u1 = 0, u2 = 0;
+          const bool in1 = testOne(sm.cand[k1], u1);
+          const bool in2 = k2 >= 0 && testOne(sm.cand[k2], u2);
+          if (in1)
+            addDir(u1);
+          if (in2)
+            addDir(u2);
         }
         __syncwarp();
       }
@@ -1314,7 +1341,7 @@ struct WbBatch
   cudaGraphExec_t graphs[WB_N_SHAPES] = {nullptr};
 };
 
-const WbShape kWbShapes[WB_N_SHAPES] = {{8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}, {8, 2}, {4, 4}, {8, 3}};
+const WbShape kWbShapes[WB_N_SHAPES] = {{4, 5}, {8, 3}, {8, 2}, {8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}};
 
 namespace
 {
@@ -1327,19 +1354,20 @@ constexpr int kDeferred = WB_N_SHAPES, kExactPass = WB_N_SHAPES + 1;
 
 RingsFn ringsFn(int idx)
 {
-  // kWbShapes: about 85 or 64 registers a thread (groups: 126 or 80)
+  // kWbShapes 0-2: column groups (register caps of about 102, 85 and 128 a
+  // thread); 3-7: one point per warp (about 85, 85, 64, 64 and 85)
   switch (idx)
   {
-  case 1: return batchRings<0, 4, 6>;
-  case 2: return batchRings<0, 4, 8>;
-  case 3: return batchRings<0, 8, 4>;
-  case 4: return batchRings<0, 2, 12>;
-  case 5: return batchGroups<8, 2>;
-  case 6: return batchGroups<4, 4>;
-  case 7: return batchGroups<8, 3>;
+  case 1: return batchGroups<8, 3>;
+  case 2: return batchGroups<8, 2>;
+  case 3: return batchRings<0, 8, 3>;
+  case 4: return batchRings<0, 4, 6>;
+  case 5: return batchRings<0, 4, 8>;
+  case 6: return batchRings<0, 8, 4>;
+  case 7: return batchRings<0, 2, 12>;
   case kDeferred: return batchRings<1, 8, 3>;
   case kExactPass: return batchRings<2, 4, 6>;
-  default: return batchRings<0, 8, 3>;
+  default: return batchGroups<4, 5>;
   }
 }
 
@@ -1447,7 +1475,7 @@ int fillTable(WbBatch *b, wb_ctx *const *jobs, int k, int chunk, uint64_t sample
   }
   BatchHdr *h = b->hIn;
   h->k = k;
-  h->chunk = chunk < 1 ? 4 : chunk;
+  h->chunk = chunk < 1 ? 1 : chunk;
   h->next[0] = h->next[1] = h->next[2] = 0;
   h->startNd[0] = h->startN[0] = h->startT[0] = h->startGrp[0] = 0;
   for (int q = 0; q < k; q++)
@@ -1667,7 +1695,7 @@ int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int
                     int *shape, int *chunk, double *gridPoints, std::string &err)
 {
   const uint64_t sample = std::min<uint64_t>(c->nd, 2000000);
-  int sh0 = clampShape(*shape), ch0 = *chunk > 0 ? *chunk : 4;
+  int sh0 = clampShape(*shape), ch0 = *chunk > 0 ? *chunk : 1;
   double gp0 = *gridPoints > 0 ? *gridPoints : 64;
   int rc = 0;
   auto timeIt = [&](int sh, int ch) -> float {   // best of two runs
@@ -1725,7 +1753,7 @@ int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int
     }
   }
   int bestChunk = ch0;
-  static const int kChunk[] = {4, 16, 64};
+  static const int kChunk[] = {1, 4, 16};
   for (int ch : kChunk)
   {
     if (ch == ch0)

@@ -80,7 +80,7 @@ struct wb_ctx
   GridInfo grid;
   /* fused fast-pass settings (wb_set_tuning; a server's autotuner picks them
      per batch): kernel shape, work chunk and points per grid column */
-  int shape = 0, chunk = 4;
+  int shape = 0, chunk = 1;
   double grid_points = 64;
   struct WbBatch *batch = nullptr;  /* job table of the batch-of-one launch */
   double grid_bounds[4] = {0, 0, 0, 0};   /* x0, y0, x1, y1 the column grid spans */

@@ -385,7 +385,7 @@ wb_server *wb_server_open(const wb_server_config *cfg)
   if (!(s->cfg.grid_points > 0))
     s->cfg.grid_points = 64;
   if (s->cfg.chunk <= 0)
-    s->cfg.chunk = 4;
+    s->cfg.chunk = 1;
   size_t freeB = 0, totalB = 0;
   cudaMemGetInfo(&freeB, &totalB);
   s->budget = cfg->hbm_budget ? cfg->hbm_budget : (uint64_t)(freeB * 0.8);
