@@ -167,9 +167,8 @@ int wb_classify_cloud(wb_ctx *ctx, const wb_cloud *cloud, const wb_params *param
  * warp takes per visit to the work counter, and the points per column of
  * the neighbour grid (applies from the next wb_octree_build).  In
  * wb_set_tuning, a negative shape or a zero chunk/grid_points keeps the
- * current value.  wb_autotune times the candidates on the scanned cloud
- * (a sample of up to 2M points), keeps the fastest, and rebuilds the grid
- * with the chosen density. */
+ * current value.  wb_autotune times the candidates on the scanned cloud,
+ * keeps the fastest, and rebuilds the grid with the chosen density. */
 typedef struct
 {
   int shape;

@@ -107,7 +107,7 @@ def test_autotuner_picks_a_shape_and_keeps_labels(clouds_alone):
             assert np.array_equal(got[i], alone[i])
         s = srv.stats()
         assert s["tuned"] == 1 and 0 <= s["shape"] < _lib.WB_N_SHAPES
-        assert s["chunk"] in (1, 4, 16) and s["grid_points"] in (16, 24, 32, 48, 64)
+        assert s["chunk"] in (1, 2, 4, 16) and s["grid_points"] in (32, 48, 64, 96)
         assert s["tune_ms"] > 0
         got = srv.classify_batch(clouds)          # jobs prepared with the tuned column density
         for i in range(len(clouds)):
@@ -127,7 +127,7 @@ def test_classifier_tuning_keeps_labels(clouds_alone):
         clf.build(clouds[5])
         clf.scan()
         t = clf.autotune()
-        assert 0 <= t["shape"] < 8 and t["chunk"] in (1, 4, 16) and t["grid_points"] in (16, 24, 32, 48, 64)
+        assert 0 <= t["shape"] < 8 and t["chunk"] in (1, 2, 4, 16) and t["grid_points"] in (32, 48, 64, 96)
         assert np.array_equal(clf.classify(), alone[5])
         assert np.array_equal(clf.classify_cloud(clouds[0]), alone[0])
     finally:

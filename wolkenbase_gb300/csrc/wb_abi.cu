@@ -480,8 +480,9 @@ int wb_autotune(wb_ctx *c, const wb_params *p)
     return rc;
   int shape = c->shape, chunk = c->chunk;
   double gp = c->grid_points;
+  WbTuneJob job{c, p, (uint8_t *)c->clsDev.p, 1};
   if ((rc = wb_classify_stage(c, p, (uint8_t *)c->clsDev.p, 1)) ||
-      (rc = wb_autotune_job(c->batch, c, p, (uint8_t *)c->clsDev.p, 1, c->stream, &shape, &chunk, &gp, err)))
+      (rc = wb_autotune_jobs(c->batch, &job, 1, c->stream, &shape, &chunk, &gp, err)))
     return wb_fail(c, rc, "wb_autotune: " + (err.empty() ? c->err : err));
   c->shape = shape;
   c->chunk = chunk;

@@ -1687,76 +1687,95 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   return 0;
 }
 
-/* Coordinate descent over the fused fast pass's settings on one staged
- * context: column density (the grid is rebuilt for each), kernel shape, then
- * chunk, each timed over a sample of up to 2M points.  Labels do not depend
- * on any of them.  Leaves c staged with the chosen density. */
-int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, cudaStream_t s,
-                    int *shape, int *chunk, double *gridPoints, std::string &err)
+/* Search over the fused fast pass's settings on staged jobs, each setting
+ * timed (best of two) on the whole of every job given: first every column
+ * density with a group shape and a one-point shape, then the other shapes at
+ * the best density, then the chunk sizes.  The jobs' grids are rebuilt for
+ * each density and left with the chosen one.  Labels do not depend on any
+ * of the settings. */
+int wb_autotune_jobs(WbBatch *b, const WbTuneJob *jobs, int k, cudaStream_t s, int *shape, int *chunk,
+                     double *gridPoints, std::string &err)
 {
-  const uint64_t sample = std::min<uint64_t>(c->nd, 2000000);
-  int sh0 = clampShape(*shape), ch0 = *chunk > 0 ? *chunk : 1;
-  double gp0 = *gridPoints > 0 ? *gridPoints : 64;
   int rc = 0;
+  std::vector<wb_ctx *> ctxs(k);
+  for (int q = 0; q < k; q++)
+    ctxs[q] = jobs[q].c;
   auto timeIt = [&](int sh, int ch) -> float {   // best of two runs
     float best = 1e30f;
     for (int r = 0; r < 2; r++)
     {
       float ms = 0;
-      if (rc == 0 && (rc = wb_batch_time(b, &c, 1, sample, sh, ch, s, &ms, err)) == 0)
+      if (rc == 0 && (rc = wb_batch_time(b, ctxs.data(), k, 0, sh, ch, s, &ms, err)) == 0)
         best = std::min(best, ms);
     }
     return best;
   };
   auto regrid = [&](double gp) -> bool {
-    c->grid_points = gp;
-    const double *g = c->grid_bounds;
-    if (rc == 0)
+    for (int q = 0; q < k && rc == 0; q++)
+    {
+      wb_ctx *c = jobs[q].c;
+      if (c->grid_points == gp && c->clsStaged)
+        continue;
+      c->grid_points = gp;
+      const double *g = c->grid_bounds;
       rc = wb_grid_impl(c, g[0], g[1], g[2], g[3]);
-    if (rc == 0)
-      rc = wb_classify_stage(c, p, cls, onDevice);
-    if (rc == 0 && cudaStreamSynchronize(c->stream) != cudaSuccess)
-      rc = WB_ECUDA;
-    if (rc && err.empty())
-      err = c->err;
+      if (rc == 0)
+        rc = wb_classify_stage(c, jobs[q].p, jobs[q].cls, jobs[q].onDevice);
+      if (rc == 0 && cudaStreamSynchronize(c->stream) != cudaSuccess)
+        rc = WB_ECUDA;
+      if (rc && err.empty())
+        err = c->err;
+    }
     return rc == 0;
   };
-  if (c->grid_points != gp0)
-    regrid(gp0);
-  timeIt(sh0, ch0);   // warm-up
-  static const double kDensity[] = {16, 24, 32, 48, 64};
-  double bestGp = gp0;
-  float best = timeIt(sh0, ch0);
+  const int ch0 = *chunk > 0 ? *chunk : 1;
+  static const double kDensity[] = {32, 48, 64, 96};
+  static const int kProbe[] = {0, 3};   // a column-group shape and a one-point shape
+  float best = 1e30f;
+  int bestShape = clampShape(*shape), bestChunk = ch0;
+  double bestGp = *gridPoints > 0 ? *gridPoints : 64;
+  bool warm = false;
   for (double gp : kDensity)
   {
-    if (gp == gp0 || !regrid(gp))
-      continue;
-    float t = timeIt(sh0, ch0);
-    if (t < best)
+    if (!regrid(gp))
+      break;
+    if (!warm)
     {
-      best = t;
-      bestGp = gp;
+      timeIt(kProbe[0], ch0);
+      warm = true;
+    }
+    for (int sh : kProbe)
+    {
+      float t = timeIt(sh, sh < 3 ? 1 : 4);
+      if (t < best)
+      {
+        best = t;
+        bestGp = gp;
+        bestShape = sh;
+        bestChunk = sh < 3 ? 1 : 4;
+      }
     }
   }
-  if (c->grid_points != bestGp)
-    regrid(bestGp);
-  int bestShape = sh0;
+  regrid(bestGp);
+  const int probeChunk = bestChunk;
   for (int sh = 0; sh < WB_N_SHAPES; sh++)
   {
-    if (sh == sh0)
+    if (sh == kProbe[0] || sh == kProbe[1])
       continue;
-    float t = timeIt(sh, ch0);
+    float t = timeIt(sh, sh < 3 ? 1 : 4);
     if (t < best)
     {
       best = t;
       bestShape = sh;
+      bestChunk = sh < 3 ? 1 : 4;
     }
   }
-  int bestChunk = ch0;
-  static const int kChunk[] = {1, 4, 16};
+  (void)probeChunk;
+  static const int kChunk[] = {1, 2, 4, 16};
+  const int c0 = bestChunk;
   for (int ch : kChunk)
   {
-    if (ch == ch0)
+    if (ch == c0)
       continue;
     float t = timeIt(bestShape, ch);
     if (t < best)

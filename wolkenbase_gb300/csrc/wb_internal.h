@@ -165,7 +165,14 @@ extern const WbShape kWbShapes[WB_N_SHAPES];
  * cleared afterwards, so the batch can be launched normally. */
 int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int shape, int chunk, cudaStream_t s,
                   float *ms, std::string &err);
-int wb_autotune_job(WbBatch *b, wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, cudaStream_t s,
-                    int *shape, int *chunk, double *gridPoints, std::string &err);
+struct WbTuneJob
+{
+  wb_ctx *c;
+  const wb_params *p;
+  uint8_t *cls;
+  int onDevice;
+};
+int wb_autotune_jobs(WbBatch *b, const WbTuneJob *jobs, int k, cudaStream_t s, int *shape, int *chunk,
+                     double *gridPoints, std::string &err);
 
 #endif

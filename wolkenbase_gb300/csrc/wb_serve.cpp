@@ -264,18 +264,25 @@ bool flushNow(const wb_server *s)
   return s->prepBusy == 0 && (s->queue.empty() || s->headBlocked);
 }
 
-/* The autotuner (first batch, classifier thread, lock not held): tunes on
- * the batch's largest job (wb_autotune_job). */
+/* The autotuner (first batch, classifier thread, lock not held): times the
+ * settings on the batch's jobs, largest first, up to about 8M points
+ * (wb_autotune_jobs). */
 void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk, double &gridPoints)
 {
   auto t0 = std::chrono::steady_clock::now();
-  JobRec *big = batch[0];
-  for (JobRec *j : batch)
-    if (j->ctx->nd > big->ctx->nd)
-      big = j;
+  std::vector<JobRec *> order(batch);
+  std::sort(order.begin(), order.end(), [](JobRec *x, JobRec *y) { return x->ctx->nd > y->ctx->nd; });
+  std::vector<WbTuneJob> jobs;
+  uint64_t pts = 0;
+  for (JobRec *j : order)
+  {
+    if (!jobs.empty() && pts + j->ctx->nd > 8000000)
+      continue;
+    jobs.push_back(WbTuneJob{j->ctx, &j->spec.params, j->spec.cls, 0});
+    pts += j->ctx->nd;
+  }
   std::string err;
-  if (wb_autotune_job(s->batch, big->ctx, &big->spec.params, big->spec.cls, 0, s->clsStream, &shape, &chunk,
-                      &gridPoints, err))
+  if (wb_autotune_jobs(s->batch, jobs.data(), (int)jobs.size(), s->clsStream, &shape, &chunk, &gridPoints, err))
     s->err = "autotune: " + err;
   s->stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
