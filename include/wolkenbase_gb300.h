@@ -217,6 +217,11 @@ int wb_launch_count(wb_ctx *ctx, uint64_t *count);
  * points for vertex v, curvature radius r and slope s.  Synchronous. */
 int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out);
 int wb_check_hypot(const double *ab, uint64_t m, double *out);
+/* The FP32 direction of the classify filter for m record differences
+ * (dx, dy) at scales sx, sy, in the reference's angle unit (2^31 per turn,
+ * masked to 31 bits like atan2i's result); its error against atan2i bounds
+ * the filter's margin. */
+int wb_check_dir_f32(const int32_t *dxy, double sx, double sy, uint64_t m, uint32_t *out);
 int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz, uint64_t m, uint8_t *out);
 
 /* ---- Serving and batching ----

@@ -77,3 +77,27 @@ def test_hyperboloid_known_and_random(cuda_lib_path, oracle_mod):
     ref = np.array([L.wbo_hyperboloid_in(ver.ctypes.data, 0.37, 1.0, np.ascontiguousarray(p).ctypes.data)
                     for p in xyz[:20000]], dtype=np.uint8)
     assert np.array_equal(got[:20000], ref)
+
+
+@pytest.mark.parametrize("scale", [(0.001, 0.001), (0.01, 0.01), (0.00025, 0.0005)])
+def test_fp32_direction_within_margin(cuda_lib_path, scale):
+    """The classify filter's FP32 direction stays within 1000 angle units
+    (2^31 per turn) of the reference's atan2i; the filter allows 2048."""
+    rng = np.random.default_rng(7)
+    m = 400_000
+    d = rng.integers(-(1 << 20), 1 << 20, size=(m, 2)).astype(np.int32)
+    small = rng.integers(-40, 41, size=(50_000, 2)).astype(np.int32)
+    axes = np.array([[k, 0] for k in range(1, 200)] + [[0, k] for k in range(1, 200)] +
+                    [[-k, 0] for k in range(1, 200)] + [[0, -k] for k in range(1, 200)] +
+                    [[k, k] for k in range(1, 200)] + [[k, -k] for k in range(1, 200)] +
+                    [[-k, k + 1] for k in range(1, 200)], np.int32)
+    d = np.concatenate([d, small, axes])
+    d = d[(d[:, 0] != 0) | (d[:, 1] != 0)]
+    d = np.ascontiguousarray(d)
+    out = np.zeros(d.shape[0], np.uint32)
+    assert _lib().wb_check_dir_f32(d.ctypes.data, scale[0], scale[1], d.shape[0], out.ctypes.data) == 0
+    yx = np.stack([d[:, 1] * scale[1], d[:, 0] * scale[0]], axis=1)
+    ref = gpu_atan2i(yx).astype(np.int64) & 0x7fffffff
+    diff = (out.astype(np.int64) - ref) & 0x7fffffff
+    err = np.minimum(diff, (1 << 31) - diff)
+    assert err.max() < 1000, int(err.max())

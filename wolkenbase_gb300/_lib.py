@@ -104,6 +104,7 @@ SIGNATURES = {
     "wb_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "wb_check_atan2i": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_check_hypot": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_check_dir_f32": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_uint64, C.c_void_p]),
     "wb_check_hyperboloid": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),
     "wb_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(wb_tuning)]),

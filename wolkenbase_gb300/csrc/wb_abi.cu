@@ -657,6 +657,14 @@ __global__ void atanCheckKernel(const double *yx, uint64_t m, const double *tab,
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
     out[i] = wb_atan2i(yx[2 * i], yx[2 * i + 1], tab, tab + 511, tab + 1023, WB_ATAN_SCALE_HI, WB_ATAN_SCALE_LO);
 }
+__global__ void dirCheckKernel(const int32_t *d, float sx, float sy, uint64_t m, uint32_t *out)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    float dx = (float)d[2 * i] * sx, dy = (float)d[2 * i + 1] * sy;
+    out[i] = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+  }
+}
 __global__ void hypotCheckKernel(const double *ab, uint64_t m, double *out)
 {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
@@ -715,6 +723,18 @@ int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out)
   });
   cudaFree(tab);
   return rc;
+}
+
+int wb_check_dir_f32(const int32_t *dxy, double sx, double sy, uint64_t m, uint32_t *out)
+{
+  if (!m)
+    return 0;
+  if (!dxy || !out)
+    return WB_EINVAL;
+  return withDevice(m * 8, dxy, m * 4, out, [&](void *din, void *dout) {
+    dirCheckKernel<<<(unsigned)((m + 255) / 256 < 4096 ? (m + 255) / 256 : 4096), 256>>>(
+        (const int32_t *)din, (float)sx, (float)sy, m, (uint32_t *)dout);
+  });
 }
 
 int wb_check_hypot(const double *ab, uint64_t m, double *out)

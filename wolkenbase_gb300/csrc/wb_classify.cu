@@ -70,8 +70,9 @@ namespace
 constexpr int kBins = 64;
 constexpr uint32_t kStray = 0x80000000u;
 /* bound on |FP32 direction - atan2i| in angle units (2^31 per turn); the
- * FP32 direction (wb_dir_units_f32) stays below 1000 units. */
-constexpr uint32_t kMargin = 4096;
+ * FP32 direction (wb_dir_units_f32) stays below 1000 units (tested against
+ * atan2i on random and edge-case differences), so this is twice that. */
+constexpr uint32_t kMargin = 2048;
 
 /* Per-point values the warp kernel needs, formed once per point by a
  * thread-per-point kernel: double arithmetic costs 16 cycles per warp
