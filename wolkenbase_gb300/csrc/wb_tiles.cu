@@ -355,6 +355,7 @@ struct ScanArgs
 
 constexpr int kQ = 8;   // summed quantities: xx, yx, yy, x, y, xz, yz, z
 constexpr int kScanCache = 224;   // tile points whose coordinates stay in shared memory
+constexpr int kScanWarps = 6;     // tiles per block of the exact scan (one solve lane each); 41 KB of shared memory
 
 __device__ __forceinline__ void counterMergeGroup(double *part, uint64_t i, double g)
 {
@@ -386,10 +387,14 @@ __device__ __forceinline__ void counterMergeOne(double *part, uint64_t i, double
   }
 }
 
+/* Partial sums of the binary counter: a tile holds at most kFillMax (4096)
+ * points, so 16 levels cover it. */
+constexpr int kLevels = 16;
+
 __device__ double pairwiseFinish(const double *part, uint64_t n)
 {
   double s = 0;
-  for (int i = 0; i < 32; i++)
+  for (int i = 0; i < kLevels; i++)
     if ((n >> i) & 1)
       s += part[i];
   return s;
@@ -532,27 +537,25 @@ __device__ __forceinline__ int sectorOf(double x, double y, double rin)
   return (sector % 6) + 1;
 }
 
-__global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRes *__restrict__ res)
+__global__ void __launch_bounds__(32 * kScanWarps) scanKernel(ScanArgs s, TileRes *__restrict__ res)
 {
-  __shared__ double part[kTileWarps][kQ][32];
-  __shared__ double tail[kTileWarps][kQ][8];
+  __shared__ double part[kScanWarps][kQ][kLevels];
+  __shared__ double tail[kScanWarps][kQ][8];
   // tile-local coordinates of tiles up to kScanCache points, decoded once
-  __shared__ double cxy[kTileWarps][3][kScanCache];
+  __shared__ double cxy[kScanWarps][3][kScanCache];
+  // the block's solves: sums in, plane and clamped slope out
+  __shared__ double tots[kScanWarps][kQ];
+  __shared__ double planes[kScanWarps][5];
+  __shared__ uint32_t counts[kScanWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const TileArgs &a = s.t;
-  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
-  if (k >= a.T)
-    return;
-  uint32_t b0 = s.tileStart[k], M = s.tileStart[k + 1] - b0;
+  uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
+  const bool live = k < a.T;
+  uint32_t b0 = live ? s.tileStart[k] : 0, M = live ? s.tileStart[k + 1] - b0 : 0;
   TileRes r{};
-  if (M == 0)
-  {
-    if (lane == 0)
-      res[k] = r;
-    return;
-  }
-  double cx, cy;
-  tileCenter(a, k, cx, cy);
+  double cx = 0, cy = 0;
+  if (live)
+    tileCenter(a, k, cx, cy);
   uint64_t G = M / 8;   // complete groups of eight
   const bool cached = M <= kScanCache;
   // coordinates of tile point i: from the cache, or decoded again
@@ -636,13 +639,16 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
       counterMergeOne(part[w][lane], i, tail[w][lane][i - G * 8]);
   }
   __syncwarp();
-  double sx = 0, sy = 0;
+  if (lane < kQ)
+    tots[w][lane] = pairwiseFinish(part[w][lane], M);
   if (lane == 0)
+    counts[w] = M;
+  __syncthreads();
+  // one lane per tile solves the block's normal equations (matrix.cpp:262-422)
+  if (w == 0 && lane < kScanWarps && counts[lane] > 0)
   {
-    double tot[kQ];
-    for (int u = 0; u < kQ; u++)
-      tot[u] = pairwiseFinish(part[w][u], M);
-    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)M}};
+    const double *tot = tots[lane];
+    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)counts[lane]}};
     double bv[3] = {tot[5], tot[6], tot[7]};
     for (int i = 0; i < 3; i++)
     {
@@ -658,22 +664,34 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel(ScanArgs s, TileRe
       v0 = NAN;
     if (m[1][1] == 0)
       v1 = NAN;
-    r.plane[0] = v0;
-    r.plane[1] = v1;
-    r.plane[2] = m[2][2] == 0 ? NAN : bv[2];
-    sx = v0;
-    sy = v1;
-    double len = wb_hypot(sx, sy);
+    double px = v0, py = v1;
+    double len = wb_hypot(px, py);
     if (len > 1)
     {
-      sx /= len;
-      sy /= len;
+      px /= len;
+      py /= len;
     }
-    if (isnan(sx) || isnan(sy))
-      sx = sy = 0;
+    if (isnan(px) || isnan(py))
+      px = py = 0;
+    planes[lane][0] = v0;
+    planes[lane][1] = v1;
+    planes[lane][2] = m[2][2] == 0 ? NAN : bv[2];
+    planes[lane][3] = px;
+    planes[lane][4] = py;
   }
-  sx = __shfl_sync(0xffffffffu, sx, 0);
-  sy = __shfl_sync(0xffffffffu, sy, 0);
+  __syncthreads();
+  if (!live)
+    return;
+  if (M == 0)
+  {
+    if (lane == 0)
+      res[k] = r;
+    return;
+  }
+  r.plane[0] = planes[w][0];
+  r.plane[1] = planes[w][1];
+  r.plane[2] = planes[w][2];
+  const double sx = planes[w][3], sy = planes[w][4];
   // untilt: bottom (first minimum), bottom2 (running minimum before it), top
   double bottom = INFINITY, top = -INFINITY;
   uint32_t argmin = 0xffffffffu;
@@ -1237,7 +1255,7 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   if (c->precision == WB_PRECISION_FP32 && a.fast)
     { scanKernel32<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
   else
-    { scanKernel<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
+    { scanKernel<<<(unsigned)((T + kScanWarps - 1) / kScanWarps), 32 * kScanWarps, 0, c->stream>>>(s, res); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "scan");
   unsigned pb = (unsigned)std::min<uint64_t>((T + 255) / 256, (uint64_t)c->sm_count * 16);
