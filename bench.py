@@ -101,6 +101,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, device):
+    """The largest x over the ranks of the process group (x itself alone):
+    the slowest replica sets the whole job's time."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -149,6 +161,47 @@ def workload(args, rank):
            "params": {"tile_size": 1.0, "max_slope": 1.0, "thickness": 0.0, "min_hyp_size": 0.1},
            "l2": "inputs larger than L2 (int32 XYZ + leaf-ordered store >> 126 MB)"}
     return cloud, cfg
+
+
+def las_measure(clf, cloud, n, stream, device):
+    """The class split of the classified cloud as LAS point format 1 records
+    (28 bytes) resident on the device: wb_las_write_classes (the last
+    classify's bytes into the records) and wb_las_split_by_class, CUDA events
+    on the library's stream.  Algorithmic bytes of the split: every record
+    read once and written once (56 B per record)."""
+    import ctypes as C
+    import torch
+    rec = torch.zeros((n, 28), dtype=torch.uint8, device=f"cuda:{device}")
+    rec[:, 0:12] = torch.from_numpy(np.ascontiguousarray(cloud.xyz).view(np.uint8).reshape(-1, 12)).to(rec.device)
+    out = torch.empty_like(rec)
+    offsets = np.zeros(257, np.uint64)
+    L = clf.L
+
+    def write():
+        clf._check(L.wb_las_write_classes(clf.ctx, C.c_void_p(rec.data_ptr()), n, 28, 1, 1, None))
+
+    def split():
+        clf._check(L.wb_las_split_by_class(clf.ctx, C.c_void_p(rec.data_ptr()), n, 28, 1, 1,
+                                           C.c_void_p(out.data_ptr()), offsets.ctypes.data))
+
+    res = {}
+    for name, fn in (("write_classes", write), ("split_by_class", split)):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[name] = e0.elapsed_time(e1) / 3
+    peak, kind = peaks()
+    gbs = 56.0 * n / (res["split_by_class"] / 1e3) / 1e9
+    del rec, out
+    return {"records": n, "format": 1, "write_classes_ms": res["write_classes"],
+            "split_by_class_ms": res["split_by_class"], "split_achieved_GBps": gbs, "split_frac": gbs / peak,
+            "ground_records": int(offsets[3] - offsets[2]), "algorithmic_bytes_per_record": 56}
 
 
 def _gen_tile(spec):
@@ -421,11 +474,7 @@ def main():
         barrier()
     launches = clf.launch_count() - launches0
     clf.profile(False)
-    ms_total = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms_total], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ev0.elapsed_time(ev1), f"cuda:{local}")
     ms_step = ms_total / args.steps
     value = world * n / (ms_step / 1e3) / 1e6
     cls_dev = dev_cls.cpu().numpy()
@@ -446,14 +495,11 @@ def main():
     for _ in range(args.steps):
         step_host()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, f"cuda:{local}")
     e2e_value = world * n / e2e_s / 1e6
     same = bool(np.array_equal(pin_cls.numpy(), cls_dev))
 
+    las = las_measure(clf, cloud, n, stream, local) if rank == 0 else None
     info = clf.info()
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
     dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download", "classify_exact")), key=lambda k: stage_ms[k])
@@ -494,7 +540,8 @@ def main():
                      if build_ms else None, "frac": (BUILD_BYTES_PER_POINT * n / (build_ms / 1e3) / 1e9) / peak
                      if build_ms else None, "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT},
            "octree": {"leaves": info["n_leaves"], "distinct": nd, "max_depth": info["max_depth"]},
-           "labels": {"ground": int(labels[2]), "not_ground": int(labels[1]), "untouched": int(labels[0])}}
+           "labels": {"ground": int(labels[2]), "not_ground": int(labels[1]), "untouched": int(labels[0])},
+           "las": las}
     clf.close()
     del dev_xyz, dev_cls, pin_xyz, pin_cls
     torch.cuda.empty_cache()

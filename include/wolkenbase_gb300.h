@@ -224,6 +224,35 @@ int wb_check_hypot(const double *ab, uint64_t m, double *out);
 int wb_check_dir_f32(const int32_t *dxy, double sx, double sy, uint64_t m, uint32_t *out);
 int wb_check_hyperboloid(const double *v, double r, double s, const double *xyz, uint64_t m, uint8_t *out);
 
+/* ---- The steps either side of the path ---- */
+
+/* OctStore::countClasses over every block (octree.cpp:664-671, 878-881;
+ * threads.cpp:425-444): totals[c] (256 entries) = stored (distinct) points
+ * whose class byte after the last wb_classify is c. */
+int wb_class_totals(wb_ctx *ctx, uint64_t *totals);
+
+/* OctBuffer::put's overwrite of an identical point (octree.cpp:620-662):
+ * *n_dup = records a later identical point replaced; with dup_of (n entries,
+ * may be NULL), the record whose point the store kept, for every record
+ * (itself when it survived). */
+int wb_duplicates(wb_ctx *ctx, uint64_t *n_dup, uint32_t *dup_of);
+
+/* The class field LasHeader::writePoint writes (las.cpp:853-862), in place
+ * in n LAS point records of point_format 0-10: formats 0-5 keep the three
+ * flag bits above the 5-bit class, 6-10 take the whole byte.  cls NULL takes
+ * the class bytes of the last wb_classify (n must be its record count).
+ * records (and cls, when given) are device pointers if on_device. */
+int wb_las_write_classes(wb_ctx *ctx, void *records, uint64_t n, uint32_t stride, int point_format, int on_device,
+                         const uint8_t *cls);
+
+/* CloudOutput::writeFiles's grouping of the points by class
+ * (cloudoutput.cpp:187-231) on the device: out receives the n records
+ * grouped by class byte (class ascending, input order within a class);
+ * offsets (257 entries) bound each class's records.  The files themselves
+ * are the caller's.  records and out are device pointers if on_device. */
+int wb_las_split_by_class(wb_ctx *ctx, const void *records, uint64_t n, uint32_t stride, int point_format,
+                          int on_device, void *out, uint64_t *offsets);
+
 /* ---- Serving and batching ----
  *
  * No reference counterpart as an API: the reference runs one cloud at a time

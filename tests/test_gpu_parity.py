@@ -56,7 +56,7 @@ def test_octree_matches_reference(classifier, case):
     assert np.array_equal(fb, r["pleaf"].astype(np.int64))
 
 
-@pytest.mark.parametrize("case", [c for c in GOLDEN_CASES if c != "split"])
+@pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_scan_and_classify_match(classifier, oracle_mod, case):
     g = load_golden(case)
     cloud = golden_cloud(g)
@@ -67,15 +67,16 @@ def test_scan_and_classify_match(classifier, oracle_mod, case):
     for f, of in (("n_points", "n_points"), ("tree_flags", "tree_flags"), ("density", "density"),
                   ("h_scan", "h_scan"), ("hyperboloid_size", "h_final"), ("height", "height")):
         assert np.array_equal(t[f], ot[of]), f
-    # n_points does not depend on point order: equal to the reference's too
-    assert np.array_equal(t["n_points"], g["tiles"]["n_points"])
     # A record overwritten by a later duplicate (OctBuffer::put) has no class of
     # its own in the reference; the GPU reports its survivor's class for it.
     stored = g["block"] >= 0
     bad = np.nonzero((r["cls"] != o["cls"]) & stored)[0]
     assert bad.size == 0, f"{bad.size} labels differ from the oracle, e.g. {bad[:10].tolist()}"
-    diff = int(np.sum((r["cls"] != g["cls"]) & stored))
-    assert diff <= LABEL_TOL * cloud.n, f"{diff} labels differ from the reference's serial run"
+    if int(g["phases"]) >= 3:   # the reference ran scan and classify for this fixture
+        # n_points does not depend on point order: equal to the reference's too
+        assert np.array_equal(t["n_points"], g["tiles"]["n_points"])
+        diff = int(np.sum((r["cls"] != g["cls"]) & stored))
+        assert diff <= LABEL_TOL * cloud.n, f"{diff} labels differ from the reference's serial run"
     _check_duplicates_share_class(cloud, r["cls"])
 
 
@@ -88,6 +89,28 @@ def _check_duplicates_share_class(cloud, cls):
             first[k] = i
         else:
             assert cls[i] == cls[first[k]]
+
+
+def test_tiles_above_4096_points_match_oracle(classifier, oracle_mod):
+    """8000 points per square metre: tile cylinders hold more than 4096
+    points (the gather's shared-memory limit), so those tiles take the
+    unsorted-fill-and-sort path."""
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    cloud = synth.density_tile(32000, 303, density=8000.0)
+    r = _gpu_run(classifier, cloud, wb.Params())
+    assert r["tiles"]["n_points"].max() > 4096
+    o = oracle_mod.run(cloud, canonical_order=True, threads=16)
+    for f, of in (("n_points", "n_points"), ("density", "density"), ("hyperboloid_size", "h_final"),
+                  ("height", "height")):
+        assert np.array_equal(r["tiles"][f], o["tiles"][of]), f
+    # at this density some records repeat a location: the overwritten ones have
+    # no class of their own in the reference (the GPU gives them their survivor's)
+    stored = o["block"] >= 0
+    assert (~stored).sum() > 0
+    bad = np.nonzero((r["cls"] != o["cls"]) & stored)[0]
+    assert bad.size == 0, f"{bad.size} labels differ from the oracle, e.g. {bad[:10].tolist()}"
+    _check_duplicates_share_class(cloud, r["cls"])
 
 
 @pytest.mark.parametrize("seed,n", [(101, 60000), (202, 30000)])

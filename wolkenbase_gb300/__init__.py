@@ -189,6 +189,41 @@ class Classifier:
         """_lib.WB_PRECISION_EXACT (bit-exact, default) or _lib.WB_PRECISION_FP32."""
         self._check(self.L.wb_set_precision(self.ctx, int(mode)))
 
+    # -- the steps either side of the path --
+    def class_totals(self):
+        """Stored points per final class byte (OctStore::countClasses summed over blocks)."""
+        out = np.zeros(256, np.uint64)
+        self._check(self.L.wb_class_totals(self.ctx, out.ctypes.data))
+        return out
+
+    def duplicates(self, per_record=False):
+        """(records replaced by a later identical point, the kept record of every record or None)."""
+        nd = C.c_uint64(0)
+        out = np.zeros(self.info()["n_points"], np.uint32) if per_record else None
+        self._check(self.L.wb_duplicates(self.ctx, C.byref(nd), out.ctypes.data if per_record else None))
+        return nd.value, out
+
+    def las_write_classes(self, records, point_format, cls=None):
+        """Writes class bytes (default: the last classify's) into (n, stride) uint8 LAS records."""
+        records = np.ascontiguousarray(records, np.uint8)
+        n, stride = records.shape
+        ptr = None
+        if cls is not None:
+            cls = np.ascontiguousarray(cls, np.uint8)
+            ptr = cls.ctypes.data
+        self._check(self.L.wb_las_write_classes(self.ctx, records.ctypes.data, n, stride, point_format, 0, ptr))
+        return records
+
+    def las_split_by_class(self, records, point_format):
+        """(records grouped by class, input order within a class; 257 class boundaries)."""
+        records = np.ascontiguousarray(records, np.uint8)
+        n, stride = records.shape
+        out = np.empty_like(records)
+        offsets = np.zeros(257, np.uint64)
+        self._check(self.L.wb_las_split_by_class(self.ctx, records.ctypes.data, n, stride, point_format, 0,
+                                                 out.ctypes.data, offsets.ctypes.data))
+        return out, offsets
+
     # -- kernel settings (speed only; labels do not depend on them) --
     def tuning(self):
         t = _lib.wb_tuning()

@@ -111,6 +111,11 @@ SIGNATURES = {
     "wb_autotune": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
     "wb_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "wb_tile_planes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wb_class_totals": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wb_duplicates": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_void_p]),
+    "wb_las_write_classes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_void_p]),
+    "wb_las_split_by_class": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_void_p,
+                                        C.c_void_p]),
     "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
     "wb_server_close": (None, [C.c_void_p]),
     "wb_server_error": (C.c_char_p, [C.c_void_p]),

@@ -1654,6 +1654,7 @@ void wb_batch_collect(WbBatch *b, wb_ctx *const *jobs, int k)
     wb_ctx *c = jobs[q];
     c->n_ambiguous = b->hOut->startAmb[q + 1] - b->hOut->startAmb[q];
     c->n_ground = b->hOut->ground[q];
+    c->clsFinal = ((const ClsArgs *)c->clsArgs)->cls;
     c->clsStaged = false;
     c->clsHost = nullptr;
     c->stage = 3;

@@ -69,7 +69,7 @@ struct wb_ctx
   DevBuf leafFirst, leafCount, leafLevel, leafKey, leafBox;
   DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
-  DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg;
+  DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre;
   DevBuf label, clsDev, ambiguous, deferred, angleT;
   /* column grid (wb_grid.cu): gpt holds one int4 {X, Y, Z, store position |
      stray bit} per point in column order; cellRec two int4 per column,
@@ -93,6 +93,7 @@ struct wb_ctx
   alignas(16) unsigned char clsArgs[768];
   bool clsStaged = false;
   uint8_t *clsHost = nullptr;       /* host destination of the class bytes, or NULL */
+  const uint8_t *clsFinal = nullptr; /* device class bytes of the last classify (per record) */
   uint64_t n_ground = 0;
 
   /* profiling */

@@ -1,0 +1,274 @@
+/* The steps either side of the path: LAS class bytes and the class split,
+ * class totals and the duplicate report.
+ *
+ *  wb_class_totals       OctStore::countClasses over every block
+ *                        (octree.cpp:664-671, 878-881; threads.cpp:425-444)
+ *  wb_duplicates         OctBuffer::put's overwrite of an identical point
+ *                        (octree.cpp:620-662), counted as alreadyInOctree
+ *  wb_las_write_classes  the classification field LasHeader::writePoint
+ *                        writes (las.cpp:853-862): formats 0-5 keep the three
+ *                        flag bits above the 5-bit class, 6-10 the whole byte
+ *  wb_las_split_by_class CloudOutput::writeFiles's grouping of the points by
+ *                        class (cloudoutput.cpp:187-231): a stable partition
+ *                        of the records on the device; the files are the
+ *                        caller's
+ *
+ * All of it is byte movement: one pass of HBM reads and writes per kernel,
+ * records copied with the widest loads their stride allows.
+ */
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include "wb_internal.h"
+
+namespace
+{
+/* Byte offset of the class field in a LAS point record (las.cpp:747-773). */
+__host__ __device__ __forceinline__ int classOffset(int format)
+{
+  return format < 6 ? 15 : 16;
+}
+
+__device__ __forceinline__ uint8_t classOf(const uint8_t *rec, int format)
+{
+  uint8_t b = rec[classOffset(format)];
+  return format < 6 ? (uint8_t)(b & 31) : b;
+}
+
+__global__ void classTotalsKernel(uint64_t nd, const uint32_t *__restrict__ sidx, const uint8_t *__restrict__ cls,
+                                  unsigned long long *__restrict__ totals)
+{
+  __shared__ unsigned int h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    h[i] = 0;
+  __syncthreads();
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[cls[sidx[j]]], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i])
+      atomicAdd(&totals[i], (unsigned long long)h[i]);
+}
+
+__global__ void dupKernel(uint64_t n, const uint32_t *__restrict__ storeOf, const uint32_t *__restrict__ sidx,
+                          uint32_t *__restrict__ dupOf)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dupOf[i] = sidx[storeOf[i]];
+}
+
+__global__ void writeClassesKernel(uint8_t *__restrict__ rec, uint64_t n, uint32_t stride, int format,
+                                   const uint8_t *__restrict__ cls)
+{
+  const int off = classOffset(format);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint8_t *b = rec + i * stride + off;
+    *b = format < 6 ? (uint8_t)((*b & 0xe0) | (cls[i] & 31)) : cls[i];
+  }
+}
+
+/* Class of every record as a sort key, its index as the value. */
+__global__ void classKeysKernel(const uint8_t *__restrict__ rec, uint64_t n, uint32_t stride, int format,
+                                uint64_t *__restrict__ keys, uint32_t *__restrict__ idx,
+                                unsigned long long *__restrict__ hist)
+{
+  __shared__ unsigned int h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    h[i] = 0;
+  __syncthreads();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint8_t c = classOf(rec + i * stride, format);
+    keys[i] = c;
+    idx[i] = (uint32_t)i;
+    atomicAdd(&h[c], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i])
+      atomicAdd(&hist[i], (unsigned long long)h[i]);
+}
+
+/* out record k = in record perm[k], one thread per record, copied in words
+ * of the widest size the stride and both bases allow. */
+template <typename Word>
+__global__ void gatherRecordsKernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, uint64_t n,
+                                    uint32_t stride, const uint32_t *__restrict__ perm)
+{
+  const uint32_t words = stride / (uint32_t)sizeof(Word);
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const Word *src = (const Word *)(in + (uint64_t)perm[k] * stride);
+    Word *dst = (Word *)(out + k * stride);
+    for (uint32_t w = 0; w < words; w++)
+      dst[w] = src[w];
+  }
+}
+
+/* A scratch device buffer freed (stream-ordered) when it leaves scope. */
+struct TmpBuf
+{
+  wb_ctx *c;
+  DevBuf b;
+  ~TmpBuf() { wb_free_buf(c, b); }
+};
+
+unsigned gridOf(const wb_ctx *c, uint64_t n)
+{
+  return (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
+}
+}  // namespace
+
+extern "C" {
+
+int wb_class_totals(wb_ctx *c, uint64_t *totals)
+{
+  if (!c || !totals)
+    return WB_EINVAL;
+  if (c->stage < 3 || !c->clsFinal)
+    return wb_fail(c, WB_ESTATE, "wb_class_totals: classify first");
+  cudaSetDevice(c->device);
+  TmpBuf out{c, {}};
+  int rc = wb_ensure(c, out.b, 256 * 8);
+  if (rc)
+    return rc;
+  WB_CUDA(c, cudaMemsetAsync(out.b.p, 0, 256 * 8, c->stream));
+  if (c->nd)
+    { classTotalsKernel<<<gridOf(c, c->nd), 256, 0, c->stream>>>(c->nd, (const uint32_t *)c->sidx.p, c->clsFinal,
+                                                                  (unsigned long long *)out.b.p); ++c->launches; }
+  cudaError_t e = cudaMemcpyAsync(totals, out.b.p, 256 * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_class_totals: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int wb_duplicates(wb_ctx *c, uint64_t *n_dup, uint32_t *dup_of)
+{
+  if (!c || !n_dup)
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_duplicates: build the octree first");
+  *n_dup = c->n - c->nd;
+  if (!dup_of || !c->n)
+    return 0;
+  cudaSetDevice(c->device);
+  TmpBuf out{c, {}};
+  int rc = wb_ensure(c, out.b, c->n * 4);
+  if (rc)
+    return rc;
+  { dupKernel<<<gridOf(c, c->n), 256, 0, c->stream>>>(c->n, (const uint32_t *)c->storeOf.p,
+                                                       (const uint32_t *)c->sidx.p, (uint32_t *)out.b.p); ++c->launches; }
+  cudaError_t e = cudaMemcpyAsync(dup_of, out.b.p, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_duplicates: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int wb_las_write_classes(wb_ctx *c, void *records, uint64_t n, uint32_t stride, int point_format, int on_device,
+                         const uint8_t *cls)
+{
+  if (!c || (n && !records))
+    return WB_EINVAL;
+  if (point_format < 0 || point_format > 10 || stride < (uint32_t)classOffset(point_format) + 1)
+    return wb_fail(c, WB_EINVAL, "wb_las_write_classes: point format 0-10 and a stride that holds its class field");
+  if (!cls && (c->stage < 3 || !c->clsFinal || n != c->n))
+    return wb_fail(c, WB_ESTATE, "wb_las_write_classes: no class bytes of a classified cloud of n records");
+  if (!n)
+    return 0;
+  cudaSetDevice(c->device);
+  int rc;
+  TmpBuf rbuf{c, {}}, cbuf{c, {}};
+  uint8_t *drec = (uint8_t *)records;
+  const uint8_t *dcls = cls ? cls : c->clsFinal;
+  if (!on_device)
+  {
+    if ((rc = wb_ensure(c, rbuf.b, n * stride)))
+      return rc;
+    drec = (uint8_t *)rbuf.b.p;
+    WB_CUDA(c, cudaMemcpyAsync(drec, records, n * stride, cudaMemcpyHostToDevice, c->stream));
+    if (cls)
+    {
+      if ((rc = wb_ensure(c, cbuf.b, n)))
+        return rc;
+      WB_CUDA(c, cudaMemcpyAsync(cbuf.b.p, cls, n, cudaMemcpyHostToDevice, c->stream));
+      dcls = (const uint8_t *)cbuf.b.p;
+    }
+  }
+  { writeClassesKernel<<<gridOf(c, n), 256, 0, c->stream>>>(drec, n, stride, point_format, dcls); ++c->launches; }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !on_device)
+    e = cudaMemcpyAsync(records, drec, n * stride, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_las_write_classes: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t stride, int point_format,
+                          int on_device, void *out, uint64_t *offsets)
+{
+  if (!c || !offsets || (n && (!records || !out)))
+    return WB_EINVAL;
+  if (point_format < 0 || point_format > 10 || stride < (uint32_t)classOffset(point_format) + 1)
+    return wb_fail(c, WB_EINVAL, "wb_las_split_by_class: point format 0-10 and a stride that holds its class field");
+  if (n >= 0xffffffffull)
+    return wb_fail(c, WB_EINVAL, "wb_las_split_by_class: at most 2^32-1 records");
+  memset(offsets, 0, 257 * sizeof(uint64_t));
+  if (!n)
+    return 0;
+  cudaSetDevice(c->device);
+  int rc;
+  TmpBuf rin{c, {}}, rout{c, {}}, hist{c, {}};
+  const uint8_t *din = (const uint8_t *)records;
+  uint8_t *dout = (uint8_t *)out;
+  if (!on_device)
+  {
+    if ((rc = wb_ensure(c, rin.b, n * stride)) || (rc = wb_ensure(c, rout.b, n * stride)))
+      return rc;
+    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, records, n * stride, cudaMemcpyHostToDevice, c->stream));
+    din = (const uint8_t *)rin.b.p;
+    dout = (uint8_t *)rout.b.p;
+  }
+  if ((rc = wb_ensure(c, hist.b, 256 * 8)) || (rc = wb_ensure(c, c->key0, n * 8)) ||
+      (rc = wb_ensure(c, c->key1, n * 8)) || (rc = wb_ensure(c, c->idx0, n * 4)) || (rc = wb_ensure(c, c->idx1, n * 4)))
+    return rc;
+  uint64_t *keys = (uint64_t *)c->key0.p;
+  uint32_t *idx = (uint32_t *)c->idx0.p;
+  WB_CUDA(c, cudaMemsetAsync(hist.b.p, 0, 256 * 8, c->stream));
+  { classKeysKernel<<<gridOf(c, n), 256, 0, c->stream>>>(din, n, stride, point_format, keys, idx,
+                                                         (unsigned long long *)hist.b.p); ++c->launches; }
+  // one stable pass of the 8-bit digit: records keep their order within a class
+  if ((rc = wb_radix_sort_pairs(c, keys, idx, (uint64_t *)c->key1.p, (uint32_t *)c->idx1.p, n, 0, 8)))
+    return rc;
+  if (stride % 16 == 0 && ((uintptr_t)din % 16 == 0) && ((uintptr_t)dout % 16 == 0))
+    { gatherRecordsKernel<uint4><<<gridOf(c, n), 256, 0, c->stream>>>(din, dout, n, stride, idx); ++c->launches; }
+  else if (stride % 8 == 0 && ((uintptr_t)din % 8 == 0) && ((uintptr_t)dout % 8 == 0))
+    { gatherRecordsKernel<uint2><<<gridOf(c, n), 256, 0, c->stream>>>(din, dout, n, stride, idx); ++c->launches; }
+  else if (stride % 4 == 0 && ((uintptr_t)din % 4 == 0) && ((uintptr_t)dout % 4 == 0))
+    { gatherRecordsKernel<uint32_t><<<gridOf(c, n), 256, 0, c->stream>>>(din, dout, n, stride, idx); ++c->launches; }
+  else
+    { gatherRecordsKernel<uint8_t><<<gridOf(c, n), 256, 0, c->stream>>>(din, dout, n, stride, idx); ++c->launches; }
+  uint64_t h[256];
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h, hist.b.p, sizeof h, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && !on_device)
+    e = cudaMemcpyAsync(out, dout, n * stride, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_las_split_by_class: ") + cudaGetErrorString(e));
+  for (int k = 0; k < 256; k++)
+    offsets[k + 1] = offsets[k] + h[k];
+  return 0;
+}
+
+}  // extern "C"

@@ -144,6 +144,43 @@ __device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const int4 &box,
   return dx * dx + dy * dy <= r * r;
 }
 
+/* Entries of the huge tiles as sort keys: (huge tile rank << 32) | store
+ * position, huge tile h owning entries [pre[h], pre[h+1]). */
+__global__ void hugeKeysKernel(uint32_t nh, const uint32_t *__restrict__ hugeList, const uint32_t *__restrict__ tileStart,
+                               const uint64_t *__restrict__ pre, const uint32_t *__restrict__ tilePts,
+                               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+  const uint64_t total = pre[nh];
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t lo = 0, hi = nh;
+    while (hi - lo > 1)
+    {
+      uint32_t mid = (lo + hi) >> 1;
+      if (pre[mid] <= e)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    uint32_t base = tileStart[hugeList[lo]];
+    keys[e] = ((uint64_t)lo << 32) | tilePts[base + (e - pre[lo])];
+    vals[e] = 0;
+  }
+}
+
+__global__ void hugeBackKernel(uint32_t nh, const uint32_t *__restrict__ hugeList, const uint32_t *__restrict__ tileStart,
+                               const uint64_t *__restrict__ pre, const uint64_t *__restrict__ keys,
+                               uint32_t *__restrict__ tilePts)
+{
+  const uint64_t total = pre[nh];
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t h = (uint32_t)(keys[e] >> 32);
+    uint32_t base = tileStart[hugeList[h]];
+    tilePts[base + (e - pre[h])] = (uint32_t)keys[e];
+  }
+}
+
 /* Pass 1: one warp per tile counts the tile's points. */
 __global__ void __launch_bounds__(32 * kTileWarps) gridCount(TileArgs a, GridDev gd, uint32_t *__restrict__ tileN)
 {
@@ -267,11 +304,14 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
   }
 }
 
-/* The block-wide fill for the tiles gridFillWarp listed (up to kFillMax points). */
+/* The block-wide fill for the tiles gridFillWarp listed: sorted in shared
+ * memory up to kFillMax points; larger tiles are written unsorted, listed in
+ * hugeList (*overflow counts them) and sorted by sortHugeTiles. */
 __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd, const uint32_t *__restrict__ tileStart,
                                                          uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
                                                          int *__restrict__ overflow, const uint32_t *__restrict__ bigList,
-                                                         const uint32_t *__restrict__ bigCount)
+                                                         const uint32_t *__restrict__ bigCount,
+                                                         uint32_t *__restrict__ hugeList)
 {
   __shared__ uint32_t buf[kFillMax];
   __shared__ uint32_t cnt;
@@ -279,14 +319,14 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
   {
   uint64_t k = bigList[bi];
   uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
-  if (M > kFillMax)
-  {
-    if (threadIdx.x == 0)
-      atomicExch(overflow, 1);
-    continue;
-  }
+  const bool huge = M > kFillMax;
   if (threadIdx.x == 0)
+  {
     cnt = 0;
+    // tiles above kFillMax points are written unsorted and sorted afterwards
+    if (huge)
+      hugeList[atomicAdd(overflow, 1)] = (uint32_t)k;
+  }
   __syncthreads();
   TileFrame f = tileFrame(a, gd, k);
   for (int j = f.j0; j <= f.j1; j++)
@@ -304,12 +344,22 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
         if (cylMember(a, gd, f, gp, p.x, p.y))
         {
           uint32_t slot = atomicAdd(&cnt, 1u);
-          if (slot < kFillMax)
+          if (huge)
+          {
+            if (slot < M)
+            {
+              tilePts[base + slot] = gp & 0x7fffffffu;
+              atomicMax(&owner[gp & 0x7fffffffu], (int32_t)k);
+            }
+          }
+          else if (slot < kFillMax)
             buf[slot] = gp & 0x7fffffffu;
         }
       }
     }
   __syncthreads();
+  if (huge)
+    continue;
   int P = 1;
   while (P < (int)M)
     P <<= 1;
@@ -387,9 +437,9 @@ __device__ __forceinline__ void counterMergeOne(double *part, uint64_t i, double
   }
 }
 
-/* Partial sums of the binary counter: a tile holds at most kFillMax (4096)
- * points, so 16 levels cover it. */
-constexpr int kLevels = 16;
+/* Partial sums of the binary counter: 24 levels cover tiles of up to 2^26
+ * points. */
+constexpr int kLevels = 24;
 
 __device__ double pairwiseFinish(const double *part, uint64_t n)
 {
@@ -1185,6 +1235,45 @@ static TileArgs tileArgs(wb_ctx *c)
   return a;
 }
 
+/* Puts the points of tiles above kFillMax points in store order (the order
+ * OctStore::pointsIn returns), all such tiles in one radix sort. */
+static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
+{
+  std::vector<uint32_t> list(nh), first(nh), last(nh);
+  std::vector<uint64_t> pre(nh + 1, 0);
+  WB_CUDA(c, cudaMemcpyAsync(list.data(), c->tileHuge.p, nh * 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t h = 0; h < nh; h++)
+  {
+    WB_CUDA(c, cudaMemcpyAsync(&first[h], tileStart + list[h], 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(&last[h], tileStart + list[h] + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t h = 0; h < nh; h++)
+    pre[h + 1] = pre[h] + (last[h] - first[h]);
+  const uint64_t total = pre[nh];
+  int rc;
+  if ((rc = wb_ensure(c, c->hugePre, (nh + 1) * 8 + 64)) || (rc = wb_ensure(c, c->key0, total * 8 + 64)) ||
+      (rc = wb_ensure(c, c->key1, total * 8 + 64)) || (rc = wb_ensure(c, c->idx0, total * 4 + 64)) ||
+      (rc = wb_ensure(c, c->idx1, total * 4 + 64)))
+    return rc;
+  WB_CUDA(c, cudaMemcpyAsync(c->hugePre.p, pre.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  uint64_t *keys = (uint64_t *)c->key0.p;
+  uint32_t *vals = (uint32_t *)c->idx0.p;
+  unsigned g = (unsigned)std::min<uint64_t>((total + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
+  { hugeKeysKernel<<<g, 256, 0, c->stream>>>(nh, (const uint32_t *)c->tileHuge.p, tileStart, (const uint64_t *)c->hugePre.p,
+                                             (const uint32_t *)c->tilePts.p, keys, vals); ++c->launches; }
+  int bits = 1;
+  while ((1ull << bits) < nh)
+    bits++;
+  if ((rc = wb_radix_sort_pairs(c, keys, vals, (uint64_t *)c->key1.p, (uint32_t *)c->idx1.p, total, 0, 32 + bits)))
+    return rc;
+  { hugeBackKernel<<<g, 256, 0, c->stream>>>(nh, (const uint32_t *)c->tileHuge.p, tileStart, (const uint64_t *)c->hugePre.p,
+                                             keys, (uint32_t *)c->tilePts.p); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  return 0;
+}
+
 int wb_scan_impl(wb_ctx *c, const wb_params *p)
 {
   if (c->stage < 1)
@@ -1237,14 +1326,17 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 16, c->stream));
   { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
                                                            (uint32_t *)c->tileNg.p, dBig); ++c->launches; }
+  if ((rc = wb_ensure(c, c->tileHuge, T * 4 + 64)))
+    return rc;
   { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
-                                                                   dOvf, (const uint32_t *)c->tileNg.p, dBig); ++c->launches; }
+                                                                   dOvf, (const uint32_t *)c->tileNg.p, dBig,
+                                                                   (uint32_t *)c->tileHuge.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
-  int ovf = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&ovf, dOvf, 4, cudaMemcpyDeviceToHost, c->stream));
+  int nHuge = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&nHuge, dOvf, 4, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (ovf)
-    return wb_fail(c, WB_EINVAL, "wb_scan_tiles: a tile cylinder holds more than 4096 points; use a smaller tile_size");
+  if (nHuge && (rc = sortHugeTiles(c, (uint32_t)nHuge, tileStart)))
+    return rc;
   wb_mark(c, "tile_gather");
   ScanArgs s;
   s.t = a;
