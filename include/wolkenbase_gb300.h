@@ -253,6 +253,15 @@ int wb_las_write_classes(wb_ctx *ctx, void *records, uint64_t n, uint32_t stride
 int wb_las_split_by_class(wb_ctx *ctx, const void *records, uint64_t n, uint32_t stride, int point_format,
                           int on_device, void *out, uint64_t *offsets);
 
+/* OctStore::hiLoPointsIn and countPointsIn (octree.cpp:1244-1293) for every
+ * pixel of a w x h view, each pixel a Column (shape.cpp:245-254) of the given
+ * side centred at (x0 + i*side, y0 + j*side), as WolkenCanvas::pixelColorRead
+ * (wolkencanvas.cpp:91-106) asks them one at a time.  count (w*h, may be
+ * NULL): stored points in the column; lo/hi (w*h doubles each, may be NULL):
+ * their lowest and highest elevation, INFINITY/-INFINITY when empty.
+ * Pixel p = j*w + i. */
+int wb_preview(wb_ctx *ctx, double x0, double y0, double side, int w, int h, uint64_t *count, double *lo, double *hi);
+
 /* ---- Serving and batching ----
  *
  * No reference counterpart as an API: the reference runs one cloud at a time

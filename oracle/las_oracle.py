@@ -14,6 +14,8 @@ versions; the product package never imports it.
                   blocks (threads.cpp:425-444): one count per stored point.
   survivors       OctBuffer::put (octree.cpp:620-662) keeps the last point read
                   at an exact location: for each record, the record kept.
+  preview         OctStore::hiLoPointsIn / countPointsIn (octree.cpp:1244-1293) for
+                  each pixel Column (shape.cpp:251-254) of a view.
 """
 from __future__ import annotations
 
@@ -65,3 +67,26 @@ def survivors(xyz):
 def class_totals(stored_records, cls):
     """Counts of the final class bytes of the stored (surviving) records."""
     return np.bincount(cls[stored_records].astype(np.int64), minlength=256).astype(np.uint64)
+
+
+def preview(points, x0, y0, side, w, h):
+    """points: (m, 3) decoded stored points.  Returns count, lo, hi per pixel (h, w)."""
+    cnt = np.zeros((h, w), np.uint64)
+    lo = np.full((h, w), np.inf)
+    hi = np.full((h, w), -np.inf)
+    half = side / 2
+    px, py, pz = points[:, 0], points[:, 1], points[:, 2]
+    fi = np.rint((px - x0) / side).astype(np.int64)
+    fj = np.rint((py - y0) / side).astype(np.int64)
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            i = fi + di
+            j = fj + dj
+            ok = (i >= 0) & (i < w) & (j >= 0) & (j < h)
+            cx = x0 + i * side
+            cy = y0 + j * side
+            ok &= (np.abs(cx - px) <= half) & (np.abs(cy - py) <= half)
+            np.add.at(cnt, (j[ok], i[ok]), 1)
+            np.minimum.at(lo, (j[ok], i[ok]), pz[ok])
+            np.maximum.at(hi, (j[ok], i[ok]), pz[ok])
+    return cnt, lo, hi

@@ -67,3 +67,20 @@ def test_class_totals_and_duplicates(classifier, name):
     surv = LO.survivors(cloud.xyz)
     assert ndup == int(np.count_nonzero(surv != np.arange(cloud.n)))
     assert np.array_equal(kept.astype(np.int64), surv)
+
+
+@pytest.mark.parametrize("side", [0.5, 0.37, 2.0])
+def test_preview_matches_restatement(classifier, side):
+    from oracle import las_oracle as LO
+    from wolkenbase_gb300 import synth
+    cloud = synth.density_tile(80_000, 41)
+    classifier.build(cloud)
+    stored = classifier.store_order().astype(np.int64)
+    pts = cloud.decoded()[stored]
+    x0, y0 = float(pts[:, 0].min()) - 1.0, float(pts[:, 1].min()) + 0.25
+    w, h = 70, 41
+    cnt, lo, hi = classifier.preview(x0, y0, side, w, h)
+    rc, rl, rh = LO.preview(pts, x0, y0, side, w, h)
+    assert np.array_equal(cnt, rc)
+    assert np.array_equal(lo, rl) and np.array_equal(hi, rh)
+    assert cnt.sum() > 0 and (cnt == 0).any()

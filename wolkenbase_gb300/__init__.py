@@ -224,6 +224,15 @@ class Classifier:
                                                  out.ctypes.data, offsets.ctypes.data))
         return out, offsets
 
+    def preview(self, x0, y0, side, w, h):
+        """Per pixel of a w x h view (pixel (i, j) centred at x0 + i*side, y0 + j*side):
+        (count, lowest, highest elevation) of the stored points in its column."""
+        cnt = np.zeros((h, w), np.uint64)
+        lo = np.zeros((h, w))
+        hi = np.zeros((h, w))
+        self._check(self.L.wb_preview(self.ctx, x0, y0, side, w, h, cnt.ctypes.data, lo.ctypes.data, hi.ctypes.data))
+        return cnt, lo, hi
+
     # -- kernel settings (speed only; labels do not depend on them) --
     def tuning(self):
         t = _lib.wb_tuning()

@@ -116,6 +116,8 @@ SIGNATURES = {
     "wb_las_write_classes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_void_p]),
     "wb_las_split_by_class": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_void_p,
                                         C.c_void_p]),
+    "wb_preview": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                             C.c_void_p]),
     "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
     "wb_server_close": (None, [C.c_void_p]),
     "wb_server_error": (C.c_char_p, [C.c_void_p]),

@@ -12,6 +12,8 @@
  *                        class (cloudoutput.cpp:187-231): a stable partition
  *                        of the records on the device; the files are the
  *                        caller's
+ *  wb_preview            OctStore::hiLoPointsIn / countPointsIn over the
+ *                        pixel columns of a view (octree.cpp:1244-1293)
  *
  * All of it is byte movement: one pass of HBM reads and writes per kernel,
  * records copied with the widest loads their stride allows.
@@ -21,6 +23,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <vector>
 #include "wb_internal.h"
 
 namespace
@@ -272,3 +275,120 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
 }
 
 }  // extern "C"
+
+/* ---- Preview queries: OctStore::hiLoPointsIn and countPointsIn (octree.cpp:1244-1293) over
+ * the pixels of a view, each pixel a Column (shape.cpp:245-254: an infinitely tall square
+ * prism, |cx - x| <= side/2 and |cy - y| <= side/2, both in double) ----
+ *
+ * WolkenCanvas::pixelColorRead (wolkencanvas.cpp:91-106) asks one pixel at a time; here every
+ * stored point visits the pixels whose column can hold it (its nearest pixel centre and, on a
+ * boundary, the neighbours), tests them with the reference's comparison, and updates the
+ * pixel's count and lowest and highest record Z (decoding is monotone in Z, so the extreme
+ * integers decode to the extreme elevations). */
+namespace
+{
+struct ViewArgs
+{
+  double x0, y0, side;   /* centre of pixel (0, 0) and the pixel size */
+  int w, h;
+  double off[3], scale[3], unit;
+};
+
+__global__ void previewKernel(ViewArgs v, uint64_t nd, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
+                              const int32_t *__restrict__ sz, unsigned long long *__restrict__ count,
+                              int *__restrict__ zlo, int *__restrict__ zhi)
+{
+  const double half = v.side / 2;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const double px = (v.off[0] + v.scale[0] * (double)sx[j]) * v.unit;
+    const double py = (v.off[1] + v.scale[1] * (double)sy[j]) * v.unit;
+    const double fi = rint((px - v.x0) / v.side), fj = rint((py - v.y0) / v.side);
+    if (!(fi > -2 && fi < v.w + 1 && fj > -2 && fj < v.h + 1))
+      continue;
+    const int i0 = (int)fi, j0 = (int)fj;
+    for (int dj = -1; dj <= 1; dj++)
+      for (int di = -1; di <= 1; di++)
+      {
+        const int i = i0 + di, jj = j0 + dj;
+        if (i < 0 || i >= v.w || jj < 0 || jj >= v.h)
+          continue;
+        const double cx = v.x0 + i * v.side, cy = v.y0 + jj * v.side;
+        if (fabs(cx - px) <= half && fabs(cy - py) <= half)
+        {
+          const uint64_t pix = (uint64_t)jj * v.w + i;
+          atomicAdd(&count[pix], 1ull);
+          atomicMin(&zlo[pix], sz[j]);
+          atomicMax(&zhi[pix], sz[j]);
+        }
+      }
+  }
+}
+
+__global__ void previewInit(uint64_t npix, unsigned long long *count, int *zlo, int *zhi)
+{
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (uint64_t)gridDim.x * blockDim.x)
+  {
+    count[p] = 0;
+    zlo[p] = INT32_MAX;
+    zhi[p] = INT32_MIN;
+  }
+}
+}  // namespace
+
+extern "C" int wb_preview(wb_ctx *c, double x0, double y0, double side, int w, int h, uint64_t *count, double *lo,
+                          double *hi)
+{
+  if (!c || w <= 0 || h <= 0 || !(side > 0))
+    return WB_EINVAL;
+  if (c->stage < 1)
+    return wb_fail(c, WB_ESTATE, "wb_preview: build the octree first");
+  if (!(c->g.scale[2] * c->g.unit > 0))
+    return wb_fail(c, WB_EINVAL, "wb_preview: needs a positive z scale (elevation increasing in Z)");
+  cudaSetDevice(c->device);
+  const uint64_t npix = (uint64_t)w * h;
+  TmpBuf cnt{c, {}}, zl{c, {}}, zh{c, {}};
+  int rc;
+  if ((rc = wb_ensure(c, cnt.b, npix * 8)) || (rc = wb_ensure(c, zl.b, npix * 4)) || (rc = wb_ensure(c, zh.b, npix * 4)))
+    return rc;
+  ViewArgs v;
+  v.x0 = x0;
+  v.y0 = y0;
+  v.side = side;
+  v.w = w;
+  v.h = h;
+  for (int k = 0; k < 3; k++)
+  {
+    v.off[k] = c->g.off[k];
+    v.scale[k] = c->g.scale[k];
+  }
+  v.unit = c->g.unit;
+  { previewInit<<<gridOf(c, npix), 256, 0, c->stream>>>(npix, (unsigned long long *)cnt.b.p, (int *)zl.b.p,
+                                                        (int *)zh.b.p); ++c->launches; }
+  if (c->nd)
+    { previewKernel<<<gridOf(c, c->nd), 256, 0, c->stream>>>(v, c->nd, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
+                                                              (const int32_t *)c->sz.p, (unsigned long long *)cnt.b.p,
+                                                              (int *)zl.b.p, (int *)zh.b.p); ++c->launches; }
+  std::vector<int> zlo(npix), zhi(npix);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && count)
+    e = cudaMemcpyAsync(count, cnt.b.p, npix * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(zlo.data(), zl.b.p, npix * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(zhi.data(), zh.b.p, npix * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess)
+    return wb_fail(c, WB_ECUDA, std::string("wb_preview: ") + cudaGetErrorString(e));
+  const WbGeom &g = c->g;
+  for (uint64_t p = 0; p < npix; p++)
+  {
+    // hiLoPointsIn returns (INFINITY, -INFINITY) for an empty shape
+    if (lo)
+      lo[p] = zlo[p] == INT32_MAX ? INFINITY : (g.off[2] + g.scale[2] * (double)zlo[p]) * g.unit;
+    if (hi)
+      hi[p] = zhi[p] == INT32_MIN ? -INFINITY : (g.off[2] + g.scale[2] * (double)zhi[p]) * g.unit;
+  }
+  return 0;
+}
