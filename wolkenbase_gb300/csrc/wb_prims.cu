@@ -86,8 +86,8 @@ __global__ void totalOf(const uint32_t *in, const uint32_t *ex, uint64_t n, uint
 /* ---------------- radix sort ---------------- */
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortPerLane = 16;
-constexpr int kSortTile = kSortThreads * kSortPerLane;   // 4096
+constexpr int kSortPerLane = 8;
+constexpr int kSortTile = kSortThreads * kSortPerLane;   // 2048
 
 __global__ void __launch_bounds__(kSortThreads) digitCounts(const uint64_t *__restrict__ keys, uint64_t n,
                                                            int shift, uint32_t *__restrict__ counts,
@@ -109,6 +109,10 @@ __global__ void __launch_bounds__(kSortThreads) digitCounts(const uint64_t *__re
     counts[(uint64_t)d * numTiles + blockIdx.x] = h[d];
 }
 
+/* One stable pass of an 8-bit digit over a tile of kSortTile pairs: warps rank
+ * their keys per digit (match_any), the tile is put in digit order in shared
+ * memory, and consecutive threads then write consecutive positions of each
+ * digit's run, so the global writes coalesce. */
 __global__ void __launch_bounds__(kSortThreads) digitScatter(const uint64_t *__restrict__ keys,
                                                             const uint32_t *__restrict__ vals, uint64_t n,
                                                             int shift, const uint32_t *__restrict__ offsets,
@@ -116,11 +120,16 @@ __global__ void __launch_bounds__(kSortThreads) digitScatter(const uint64_t *__r
                                                             uint32_t *__restrict__ valsOut)
 {
   __shared__ uint32_t wcount[kSortWarps][256];
+  __shared__ uint32_t localStart[256], globalStart[256];
+  __shared__ uint64_t skeys[kSortTile];
+  __shared__ uint32_t svals[kSortTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads)
     (&wcount[0][0])[i] = 0;
   __syncthreads();
-  uint64_t wbase = (uint64_t)blockIdx.x * kSortTile + (uint64_t)warp * (kSortPerLane * 32);
+  const uint64_t tbase = (uint64_t)blockIdx.x * kSortTile;
+  const uint32_t tileN = (uint32_t)(n - tbase < (uint64_t)kSortTile ? n - tbase : (uint64_t)kSortTile);
+  uint64_t wbase = tbase + (uint64_t)warp * (kSortPerLane * 32);
   uint64_t k8[kSortPerLane];
   uint32_t v8[kSortPerLane];
   uint32_t rank[kSortPerLane];
@@ -143,15 +152,44 @@ __global__ void __launch_bounds__(kSortThreads) digitScatter(const uint64_t *__r
     __syncwarp();
   }
   __syncthreads();
-  // exclusive prefix over warps for every digit
+  // per digit: exclusive prefix over warps, the tile's total, and where the
+  // digit's run starts in the tile and in the output
   for (int d = threadIdx.x; d < 256; d += kSortThreads)
   {
-    uint32_t run = offsets[(uint64_t)d * numTiles + blockIdx.x];
+    uint32_t run = 0;
     for (int w = 0; w < kSortWarps; w++)
     {
       uint32_t c = wcount[w][d];
       wcount[w][d] = run;
       run += c;
+    }
+    localStart[d] = run;   // the digit's count for now
+    globalStart[d] = offsets[(uint64_t)d * numTiles + blockIdx.x];
+  }
+  __syncthreads();
+  if (warp == 0)
+  {
+    // exclusive prefix of the 256 digit counts, 8 per lane
+    uint32_t c[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      c[q] = localStart[lane * 8 + q];
+      sum += c[q];
+    }
+    uint32_t inc = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o)
+        inc += v;
+    }
+    uint32_t run = inc - sum;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      localStart[lane * 8 + q] = run;
+      run += c[q];
     }
   }
   __syncthreads();
@@ -162,10 +200,19 @@ __global__ void __launch_bounds__(kSortThreads) digitScatter(const uint64_t *__r
     if (i < n)
     {
       uint32_t d = (uint32_t)((k8[s] >> shift) & 255);
-      uint32_t pos = wcount[warp][d] + rank[s];
-      keysOut[pos] = k8[s];
-      valsOut[pos] = v8[s];
+      uint32_t lp = localStart[d] + wcount[warp][d] + rank[s];
+      skeys[lp] = k8[s];
+      svals[lp] = v8[s];
     }
+  }
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < tileN; t += kSortThreads)
+  {
+    uint64_t key = skeys[t];
+    uint32_t d = (uint32_t)((key >> shift) & 255);
+    uint32_t pos = globalStart[d] + (t - localStart[d]);
+    keysOut[pos] = key;
+    valsOut[pos] = svals[t];
   }
 }
 
