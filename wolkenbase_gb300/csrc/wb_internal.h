@@ -56,7 +56,7 @@ struct wb_ctx
 
   /* state */
   int stage = 0;                    /* 0 empty, 1 built, 2 scanned, 3 classified */
-  uint64_t n = 0, nd = 0, n_leaves = 0, n_nodes = 0, n_tiles = 0, n_pairs = 0;
+  uint64_t n = 0, nd = 0, n_leaves = 0, n_nodes = 0, n_tiles = 0;
   uint32_t max_depth = 0;
   uint64_t n_ambiguous = 0;         /* points the exact classify pass re-ran */
   WbGeom g{};

@@ -9,8 +9,9 @@
  * sequence as the reference's and the plane fit, the untilt and the
  * "second lowest" point come out identical.
  *
- * Pass 1 counts each tile's points, pass 2 writes them (a CSR: tileStart,
- * tilePts) and records for every point the last tile in flowsnake order that
+ * Pass 1 bounds each tile's points by the columns its cylinder meets (room
+ * at tileStart[k]), pass 2 gathers them (tilePts from tileStart[k], tileN[k]
+ * points) and records for every point the last tile in flowsnake order that
  * contains it (owner), which is the tile whose classification survives.
  */
 #include <cuda_runtime.h>
@@ -182,36 +183,25 @@ __global__ void hugeBackKernel(uint32_t nh, const uint32_t *__restrict__ hugeLis
 }
 
 /* Pass 1: one warp per tile counts the tile's points. */
-__global__ void __launch_bounds__(32 * kTileWarps) gridCount(TileArgs a, GridDev gd, uint32_t *__restrict__ tileN)
+/* Room for each tile's points: the points of the grid columns its cylinder
+ * meets (an upper bound of the tile's count), one thread per tile.  The fill
+ * passes write a tile's points from tileStart[k] on and its count to tileN. */
+__global__ void gridBound(TileArgs a, GridDev gd, uint32_t *__restrict__ bound)
 {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
-  if (k >= a.T)
-    return;
-  TileFrame f = tileFrame(a, gd, k);
-  uint32_t found = 0;
-  for (int j = f.j0; j <= f.j1; j++)
-    for (int i = f.i0; i <= f.i1; i++)
-    {
-      uint64_t c = (uint64_t)j * gd.nx + i;
-      int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
-      uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
-      if (b == e || !cellMeetsCyl(a, box, f.cx, f.cy))
-        continue;
-      for (uint32_t t0 = b; t0 < e; t0 += 32)
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    TileFrame f = tileFrame(a, gd, k);
+    uint32_t room = 0;
+    for (int j = f.j0; j <= f.j1; j++)
+      for (int i = f.i0; i <= f.i1; i++)
       {
-        uint32_t t = t0 + lane;
-        bool in = false;
-        if (t < e)
-        {
-          int4 p = gd.gpt[t];
-          in = cylMember(a, gd, f, (uint32_t)p.w, p.x, p.y);
-        }
-        found += __popc(__ballot_sync(0xffffffffu, in));
+        uint64_t c = (uint64_t)j * gd.nx + i;
+        int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
+        if (r1.y != r1.z && cellMeetsCyl(a, box, f.cx, f.cy))
+          room += (uint32_t)(r1.z - r1.y);
       }
-    }
-  if (lane == 0)
-    tileN[k] = found;
+    bound[k] = room;
+  }
 }
 
 constexpr int kFillThreads = 256;
@@ -225,6 +215,7 @@ constexpr int kWarpFill = 1024;
  * Tiles above kWarpFill points are listed for the block-wide version. */
 __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, GridDev gd,
                                                                 const uint32_t *__restrict__ tileStart,
+                                                                uint32_t *__restrict__ tileN,
                                                                 uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
                                                                 uint32_t *__restrict__ bigList, uint32_t *__restrict__ bigCount)
 {
@@ -233,13 +224,11 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
   uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
   if (k >= a.T)
     return;
-  uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
-  if (M == 0)
-    return;
-  if (M > kWarpFill)
+  const uint32_t base = tileStart[k];
+  if (tileStart[k + 1] == base)
   {
     if (lane == 0)
-      bigList[atomicAdd(bigCount, 1u)] = (uint32_t)k;
+      tileN[k] = 0;
     return;
   }
   uint32_t *b = buf[w];
@@ -271,6 +260,18 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
         n += __popc(m);
       }
     }
+  const uint32_t M = n;
+  if (lane == 0)
+    tileN[k] = M;
+  if (M == 0)
+    return;
+  if (M > kWarpFill)
+  {
+    // too many for the warp's buffer: the block-wide fill gathers it again
+    if (lane == 0)
+      bigList[atomicAdd(bigCount, 1u)] = (uint32_t)k;
+    return;
+  }
   int P = 32;
   while (P < (int)M)
     P <<= 1;
@@ -308,6 +309,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
  * memory up to kFillMax points; larger tiles are written unsorted, listed in
  * hugeList (*overflow counts them) and sorted by sortHugeTiles. */
 __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd, const uint32_t *__restrict__ tileStart,
+                                                         const uint32_t *__restrict__ tileN,
                                                          uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
                                                          int *__restrict__ overflow, const uint32_t *__restrict__ bigList,
                                                          const uint32_t *__restrict__ bigCount,
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
   for (uint32_t bi = blockIdx.x; bi < *bigCount; bi += gridDim.x)
   {
   uint64_t k = bigList[bi];
-  uint32_t base = tileStart[k], M = tileStart[k + 1] - base;
+  uint32_t base = tileStart[k], M = tileN[k];
   const bool huge = M > kFillMax;
   if (threadIdx.x == 0)
   {
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
 struct ScanArgs
 {
   TileArgs t;
-  const uint32_t *tileStart, *tilePts;
+  const uint32_t *tileStart, *tileN, *tilePts;   /* tile k: tilePts[tileStart[k] ...], tileN[k] points */
   double minH;
 };
 
@@ -601,7 +603,7 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanKernel(ScanArgs s, TileRe
   const TileArgs &a = s.t;
   uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
   const bool live = k < a.T;
-  uint32_t b0 = live ? s.tileStart[k] : 0, M = live ? s.tileStart[k + 1] - b0 : 0;
+  uint32_t b0 = live ? s.tileStart[k] : 0, M = live ? s.tileN[k] : 0;
   TileRes r{};
   double cx = 0, cy = 0;
   if (live)
@@ -862,7 +864,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
   uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
   if (k >= a.T)
     return;
-  uint32_t b0 = s.tileStart[k], M = s.tileStart[k + 1] - b0;
+  uint32_t b0 = s.tileStart[k], M = s.tileN[k];
   TileRes r{};
   if (M == 0)
   {
@@ -1239,18 +1241,16 @@ static TileArgs tileArgs(wb_ctx *c)
  * OctStore::pointsIn returns), all such tiles in one radix sort. */
 static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
 {
-  std::vector<uint32_t> list(nh), first(nh), last(nh);
+  std::vector<uint32_t> list(nh), last(nh);
   std::vector<uint64_t> pre(nh + 1, 0);
   WB_CUDA(c, cudaMemcpyAsync(list.data(), c->tileHuge.p, nh * 4, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint32_t *tileN = (const uint32_t *)c->tileN.p;
   for (uint32_t h = 0; h < nh; h++)
-  {
-    WB_CUDA(c, cudaMemcpyAsync(&first[h], tileStart + list[h], 4, cudaMemcpyDeviceToHost, c->stream));
-    WB_CUDA(c, cudaMemcpyAsync(&last[h], tileStart + list[h] + 1, 4, cudaMemcpyDeviceToHost, c->stream));
-  }
+    WB_CUDA(c, cudaMemcpyAsync(&last[h], tileN + list[h], 4, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   for (uint32_t h = 0; h < nh; h++)
-    pre[h + 1] = pre[h] + (last[h] - first[h]);
+    pre[h + 1] = pre[h] + last[h];
   const uint64_t total = pre[nh];
   int rc;
   if ((rc = wb_ensure(c, c->hugePre, (nh + 1) * 8 + 64)) || (rc = wb_ensure(c, c->key0, total * 8 + 64)) ||
@@ -1305,31 +1305,33 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   uint32_t *tileN = (uint32_t *)c->tileN.p, *tileStart = (uint32_t *)c->tileStart.p;
   int32_t *owner = (int32_t *)c->owner.p;
   unsigned blocks = (unsigned)((T + kTileWarps - 1) / kTileWarps);
-  { gridCount<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileN); ++c->launches; }
+  // room per tile (tileNg holds the bounds until the fill reuses it as its list)
+  if ((rc = wb_ensure(c, c->tileNg, T * 4 + 64)))
+    return rc;
+  uint32_t *bound = (uint32_t *)c->tileNg.p;
+  { gridBound<<<(unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32), 128, 0, c->stream>>>(
+        a, gd, bound); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
-  if ((rc = wb_exclusive_scan_u32(c, tileN, tileStart, T, dTot)))
+  if ((rc = wb_exclusive_scan_u32(c, bound, tileStart, T, dTot)))
     return rc;
   WB_CUDA(c, cudaMemcpyAsync(tileStart + T, dTot, 4, cudaMemcpyDeviceToDevice, c->stream));
-  uint32_t M = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&M, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  uint32_t room = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&room, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->n_pairs = M;
-  if ((rc = wb_ensure(c, c->tilePts, (uint64_t)M * 4 + 64)))
+  if ((rc = wb_ensure(c, c->tilePts, (uint64_t)room * 4 + 64)))
     return rc;
   { fillOwner<<<(unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(owner, nd); ++c->launches; }
   int *dOvf = (int *)((char *)c->small.p + 384);
   uint32_t *dBig = (uint32_t *)((char *)c->small.p + 392);
-  if ((rc = wb_ensure(c, c->tileNg, T * 4 + 64)))
-    return rc;
-  // overflow flag and big-tile count (bytes 384..395 of the scratch block)
+  // huge-tile count and big-tile count (bytes 384..395 of the scratch block)
   WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 16, c->stream));
-  { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
+  { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, tileN, (uint32_t *)c->tilePts.p, owner,
                                                            (uint32_t *)c->tileNg.p, dBig); ++c->launches; }
   if ((rc = wb_ensure(c, c->tileHuge, T * 4 + 64)))
     return rc;
-  { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, (uint32_t *)c->tilePts.p, owner,
-                                                                   dOvf, (const uint32_t *)c->tileNg.p, dBig,
+  { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, tileN, (uint32_t *)c->tilePts.p,
+                                                                   owner, dOvf, (const uint32_t *)c->tileNg.p, dBig,
                                                                    (uint32_t *)c->tileHuge.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   int nHuge = 0;
@@ -1341,6 +1343,7 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   ScanArgs s;
   s.t = a;
   s.tileStart = tileStart;
+  s.tileN = tileN;
   s.tilePts = (const uint32_t *)c->tilePts.p;
   s.minH = p->min_hyp_size;
   TileRes *res = (TileRes *)c->tileRes.p;
