@@ -518,8 +518,9 @@ def main():
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes": alg_bytes, "avg_ms": stage_ms[dom]}
+    # the octree build proper (sizeFit + put of every point); the column grid is this path's own index
     build_ms = sum(v for k, v in stage_ms.items() if k in ("decode_key", "sort", "dedup", "leaves", "leaf_order",
-                                                         "point_map", "nodes", "grid"))
+                                                         "point_map", "nodes"))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

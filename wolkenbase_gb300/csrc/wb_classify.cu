@@ -9,18 +9,22 @@
  * function of the neighbour set alone: 1 (not ground) if it surrounds p, else 2.
  * The neighbour set is what OctStore::pointsIn returns for the hyperboloid.
  *
- * One warp classifies one point.  It walks rings of grid columns outward from
- * the point, so directions from every side arrive early, and stops as soon as
- * the directions seen surround the point.  Per column it first checks whether
- * the column's lowest point could be inside the hyperboloid at the column's
- * nearest distance.  Each candidate is tested in FP32 in a frame centred on p
+ * Two kernels walk the same neighbourhood.  The column-group kernel
+ * (classifyGroup, the fast pass) gives one warp to up to 32 points of one
+ * grid column and shares the walk between them; the one-point kernel
+ * (classifyPoint) gives one warp to one point and serves the points a group
+ * hands over, and the exact pass.  Both walk rings of grid columns outward
+ * from the point, so directions from every side arrive early, and stop as soon
+ * as the directions seen surround the point.  Per column they first check
+ * whether the column's lowest point could be inside the hyperboloid at the
+ * column's nearest distance.  Each candidate is tested in FP32 in a frame centred on p
  * (integer record differences times the scale); the few whose FP32 value lies
  * within 1e-5 of the boundary, and points outside the octree root cube (which
  * the reference treats through their leaf's cube), are tested exactly in
  * FP64 as the reference computes it.  Directions are FP32 arctangents
  * (wb_dir_units_f32, error below 1000 units) in the reference's integer angle
- * unit; 64 bins keep each bin's extremes, and the largest circular gap
- * follows from them.  With the direction error bounded by kMargin units, a
+ * unit; bins (64 in the one-point kernel, 8 per lane in the group kernel) keep
+ * their extremes, and the largest circular gap follows from them.  With the direction error bounded by kMargin units, a
  * gap estimate below 144 degrees - 2*kMargin proves "surrounded" and one
  * above 144 degrees + 2*kMargin proves the opposite;
  * anything between is re-run by the exact kernel with the reference's own
