@@ -267,7 +267,8 @@ bool flushNow(const wb_server *s)
 /* The autotuner (first batch, classifier thread, lock not held): times the
  * settings on the batch's jobs, largest first, up to about 8M points
  * (wb_autotune_jobs). */
-void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk, double &gridPoints)
+double autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk, double &gridPoints,
+                std::string &err)
 {
   auto t0 = std::chrono::steady_clock::now();
   std::vector<JobRec *> order(batch);
@@ -281,10 +282,9 @@ void autotune(wb_server *s, std::vector<JobRec *> &batch, int &shape, int &chunk
     jobs.push_back(WbTuneJob{j->ctx, &j->spec.params, j->spec.cls, 0});
     pts += j->ctx->nd;
   }
-  std::string err;
-  if (wb_autotune_jobs(s->batch, jobs.data(), (int)jobs.size(), s->clsStream, &shape, &chunk, &gridPoints, err))
-    s->err = "autotune: " + err;
-  s->stats.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (wb_autotune_jobs(s->batch, jobs.data(), (int)jobs.size(), s->clsStream, &shape, &chunk, &gridPoints, err) == 0)
+    err.clear();
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 void classifyLoop(wb_server *s)
@@ -320,24 +320,27 @@ void classifyLoop(wb_server *s)
     {
       int shape = s->cfg.shape, chunk = s->cfg.chunk;
       double gp = s->cfg.grid_points;
-      autotune(s, batch, shape, chunk, gp);
+      std::string terr;
+      double ms = autotune(s, batch, shape, chunk, gp, terr);
       std::lock_guard<std::mutex> g(s->m);
       s->cfg.shape = shape;
       s->cfg.chunk = chunk;
       s->cfg.grid_points = gp;
       s->stats.tuned = 1;
+      s->stats.tune_ms = ms;
+      if (!terr.empty())
+        s->err = "autotune: " + terr;
     }
     uint64_t launches = 0;
     if (rc == 0)
       rc = wb_batch_launch(s->batch, ctxs.data(), k, s->clsStream, s->cfg.shape, s->cfg.chunk, &launches, err);
-    if (rc == 0)
+    // wait even after a failed launch: the jobs' contexts go back to the pool
+    // and must not be reused while work that reads them may still run
+    cudaError_t e = cudaStreamSynchronize(s->clsStream);
+    if (rc == 0 && e != cudaSuccess)
     {
-      cudaError_t e = cudaStreamSynchronize(s->clsStream);
-      if (e != cudaSuccess)
-      {
-        rc = WB_ECUDA;
-        err = std::string("fused classify: ") + cudaGetErrorString(e);
-      }
+      rc = WB_ECUDA;
+      err = std::string("fused classify: ") + cudaGetErrorString(e);
     }
     if (rc == 0)
       wb_batch_collect(s->batch, ctxs.data(), k);
