@@ -332,6 +332,9 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   if (EXACT)
     hx = exactHyp(a, (uint32_t)j);
   bool surrounded = false, ambiguous = false;
+  // FP32 membership (exact: its band goes to FP64) and height bounds wherever
+  // 32-bit record differences are exact; FP32 directions only in the fast pass
+  const bool fp32Member = a.exactInts;
   const bool fast = !EXACT && a.exactInts;
   // Directions are kept as exact per-bin extremes in shared memory plus a
   // 64-bit occupancy mask in registers (uniform across the warp).
@@ -347,7 +350,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   // the point.  Columns holding points outside the root cube in x or y get no
   // bound (their blocks' cubes decide for them).
   auto colZlim = [&](const int4 &box, const int4 &r1) -> int32_t {
-    if (!fast || r1.w || !(h.sz > 0))
+    if (!fp32Member || r1.w || !(h.sz > 0))
       return INT32_MAX;
     float xl = (float)(box.x - h.qx) * h.sx, xh = (float)(box.z - h.qx) * h.sx;
     float yl = (float)(box.y - h.qy) * h.sy, yh = (float)(box.w - h.qy) * h.sy;
@@ -362,7 +365,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     bool in = false;
     const int32_t qx = pt.x, qy = pt.y, qz = pt.z;
     const uint32_t gp = (uint32_t)pt.w;
-    if (fast)
+    if (fp32Member)
     {
       int32_t dxi = qx - h.qx, dyi = qy - h.qy;
       // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
@@ -388,8 +391,15 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           else
             in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
         }
-        if (in)
+        if (in && fast)
           u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
+        else if (in)
+        {
+          // the exact pass: the reference's integer direction of the decoded points
+          double x = decA(a, 0, qx), y = decA(a, 1, qy);
+          u = (uint32_t)wb_atan2i(y - hx.py, x - hx.px, a.tanT, a.sinT, a.cosT, WB_ATAN_SCALE_HI,
+                                  WB_ATAN_SCALE_LO) & 0x7fffffffu;
+        }
       }
     }
     else
