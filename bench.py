@@ -164,11 +164,14 @@ def workload(args, rank):
 
 
 def las_measure(clf, cloud, n, stream, device):
-    """The class split of the classified cloud as LAS point format 1 records
-    (28 bytes) resident on the device: wb_las_write_classes (the last
-    classify's bytes into the records) and wb_las_split_by_class, CUDA events
-    on the library's stream.  Algorithmic bytes of the split: every record
-    read once and written once (56 B per record)."""
+    """The steps either side of the path on the classified cloud as LAS point
+    format 1 records (28 bytes) resident on the device, CUDA events on the
+    library's stream: wb_las_write_classes (the last classify's bytes into the
+    records), wb_las_split_by_class, wb_las_decode (every LasPoint field) and
+    wb_las_write_output (the class-split writer).  Algorithmic bytes: split 56 B
+    per record (read once, written once); decode 90 B per record (28 read, 62
+    written as field arrays); writer 61 B per stored point (record read, record
+    written, store index and class byte read)."""
     import ctypes as C
     import torch
     rec = torch.zeros((n, 28), dtype=torch.uint8, device=f"cuda:{device}")
@@ -184,8 +187,37 @@ def las_measure(clf, cloud, n, stream, device):
         clf._check(L.wb_las_split_by_class(clf.ctx, C.c_void_p(rec.data_ptr()), n, 28, 1, 1,
                                            C.c_void_p(out.data_ptr()), offsets.ctypes.data))
 
+    # LasHeader::readPoint of every record into device arrays of every LasPoint field
+    from wolkenbase_gb300 import _lib
+    dev = rec.device
+    tdt = {C.c_double: torch.float64, C.c_uint16: torch.int16, C.c_uint8: torch.uint8, C.c_int32: torch.int32}
+    fields = {name: torch.empty(n, dtype=tdt[t], device=dev) for name, t in _lib.LAS_POINT_FIELDS}
+    pts = _lib.wb_las_points(**{name: t.data_ptr() for name, t in fields.items()})
+    d = cloud.decoded()
+    cs = _lib.wb_cloud()
+    cs.records, cs.n, cs.stride, cs.device_resident = rec.data_ptr(), n, 28, 1
+    cs.scale[:], cs.offset[:], cs.unit = cloud.scale, cloud.offset, cloud.unit
+
+    def decode():
+        clf._check(L.wb_las_decode(clf.ctx, C.byref(cs), 1, C.byref(pts)))
+
+    # CloudOutput::writeFiles as the GUI runs it (separate classes, 10M points
+    # per file: wolkencanvas.cpp:619), records in and files out on the device
+    import wolkenbase_gb300 as wb
+    o = wb.LasOutput(point_format=1, separate_classes=True, points_per_file=10_000_000, unit=cloud.unit,
+                     min_cor=tuple(d.min(axis=0)), max_cor=tuple(d.max(axis=0)), scale=(0.001, 0.001, 0.001),
+                     creation_day=1, creation_year=2026).c()
+    nd = clf.info()["n_distinct"]
+    fout = torch.empty((nd, 28), dtype=torch.uint8, device=dev)
+    files = (_lib.wb_las_file * 64)()
+    nfiles = C.c_int(0)
+
+    def writer():
+        clf._check(L.wb_las_write_output(clf.ctx, C.byref(cs), 1, None, C.byref(o), C.c_void_p(fout.data_ptr()), 1,
+                                          files, 64, C.byref(nfiles)))
+
     res = {}
-    for name, fn in (("write_classes", write), ("split_by_class", split)):
+    for name, fn in (("write_classes", write), ("split_by_class", split), ("decode", decode), ("writer", writer)):
         fn()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -198,10 +230,17 @@ def las_measure(clf, cloud, n, stream, device):
         res[name] = e0.elapsed_time(e1) / 3
     peak, kind = peaks()
     gbs = 56.0 * n / (res["split_by_class"] / 1e3) / 1e9
-    del rec, out
+    dec_gbs = 90.0 * n / (res["decode"] / 1e3) / 1e9
+    wr_gbs = 61.0 * nd / (res["writer"] / 1e3) / 1e9
+    del rec, out, fields, fout
     return {"records": n, "format": 1, "write_classes_ms": res["write_classes"],
             "split_by_class_ms": res["split_by_class"], "split_achieved_GBps": gbs, "split_frac": gbs / peak,
-            "ground_records": int(offsets[3] - offsets[2]), "algorithmic_bytes_per_record": 56}
+            "ground_records": int(offsets[3] - offsets[2]), "algorithmic_bytes_per_record": 56,
+            "decode_ms": res["decode"], "decode_GBps": dec_gbs, "decode_frac": dec_gbs / peak,
+            "decode_bytes_per_record": 90,
+            "writer_ms": res["writer"], "writer_GBps": wr_gbs, "writer_frac": wr_gbs / peak,
+            "writer_bytes_per_point": 61, "writer_files": nfiles.value,
+            "writer_workload": "format 1 in and out, separate classes, 10M points per file, device-resident"}
 
 
 def _gen_tile(spec):

@@ -35,6 +35,7 @@ extern "C" {
 #define WB_ENOTFOUND -7   /* no such job / entry                             */
 #define WB_EBUSY -8       /* job already running or finished (wb_cancel)     */
 #define WB_ECANCELED -9   /* job was cancelled before it ran                 */
+#define WB_EIO -10        /* a file could not be written                    */
 
 /* Classify kernel shapes: one warp per group of up to 32 points of a grid
  * column (0-2) or one warp per point (3-7); warps per block / resident blocks
@@ -261,6 +262,102 @@ int wb_las_split_by_class(wb_ctx *ctx, const void *records, uint64_t n, uint32_t
  * their lowest and highest elevation, INFINITY/-INFINITY when empty.
  * Pixel p = j*w + i. */
 int wb_preview(wb_ctx *ctx, double x0, double y0, double side, int w, int h, uint64_t *count, double *lo, double *hi);
+
+/* ---- LAS records: full decode and the class-split writer ---- */
+
+/* Record length of LAS point formats 0-10 (las.cpp:38); 0 for others. */
+int wb_las_point_length(int point_format);
+
+/* The fields of a LasPoint (las.h:53-78) as LasHeader::readPoint fills them
+ * (las.cpp:735-820), one array per field, indexed by record.  Any pointer
+ * may be NULL (field not wanted).  Fields a format lacks read as LasPoint's
+ * defaults (las.cpp:121-132): 0.  scan_angle is in 2^31 units per turn
+ * (degtobin, angle.cpp:229-243). */
+typedef struct
+{
+  double *x, *y, *z;               /* (offset + scale*X) * unit, las.cpp:808 */
+  uint16_t *intensity, *return_num, *n_returns;
+  uint8_t *scan_direction, *edge_line;
+  uint16_t *classification, *class_flags, *scanner_channel, *user_data;
+  int32_t *scan_angle;
+  uint16_t *point_source;
+  double *gps_time;
+  uint16_t *red, *green, *blue, *nir;
+} wb_las_points;
+
+/* readPoint for every record of cloud (formats 0-10; stride >= the format's
+ * record length).  The arrays are device pointers if cloud->device_resident,
+ * else host pointers. */
+int wb_las_decode(wb_ctx *ctx, const wb_cloud *cloud, int point_format, const wb_las_points *out);
+
+/* What CloudOutput is told before openFiles (wolkencanvas.cpp:614-622,
+ * cloudoutput.h). */
+typedef struct
+{
+  int32_t point_format;        /* CloudOutput::pointFormat (wb_las_join_point_format)  */
+  int32_t separate_classes;    /* one set of files per class (SI_EXTRACT)             */
+  int32_t n_input_files;       /* > 1: system identifier MERGE                         */
+  int32_t creation_day;        /* day of year (1-366) and year written in the headers; */
+  int32_t creation_year;       /* 0 = today (UTC), as LasHeader::openWrite does        */
+  int32_t pad;
+  uint64_t points_per_file;    /* CloudOutput::pointsPerFile; 0 = one file per set     */
+  double unit;                 /* CloudOutput::unit, metres per file unit              */
+  double min_cor[3], max_cor[3];   /* CloudOutput::minCor/maxCor, metres                */
+  double scale[3];             /* CloudOutput::scale (wb_las_combine_scales), metres   */
+  const char *software;        /* header software name; NULL = "Wolkenbase 0.1.2~alpha" */
+} wb_las_output;
+
+/* One output file: its place in the set, its records in the output buffer
+ * and the header figures LasHeader accumulates while writing (las.cpp:636-673,
+ * 822-903). */
+typedef struct
+{
+  int32_t class_id;            /* class of the set; 0 when classes are not separated */
+  int32_t index;               /* file number within its set                          */
+  int32_t name_digits;         /* digits of that number in the file name              */
+  int32_t point_format;
+  uint64_t first;              /* first record of the file in the output buffer       */
+  uint64_t n_points[16];       /* [0] records, [r] records of return number r         */
+  double scale[3], offset[3];  /* LasHeader::setScale, file units                     */
+  double min[3], max[3];       /* of the written coordinates, file units (+-INFINITY if empty) */
+} wb_las_file;
+
+/* joinPointFormat (las.cpp:103-118): the smallest format whose features
+ * hold every input format's. */
+int wb_las_join_point_format(const int *formats, int n);
+
+/* combineScales (las.cpp:906-944): per axis, the scale that fits every input
+ * file's scale and offset (manygcd, manygcd.cpp:44-74).  scales and offsets
+ * are n x 3 (metres: LasHeader::getScale/getOffset); out receives 3. */
+int wb_las_combine_scales(const double *scales, const double *offsets, int n, double *out);
+
+/* CloudOutput::openFiles + writeFiles (cloudoutput.cpp:116-231) on the
+ * device: every stored point of the classified cloud is read from its record
+ * (the surviving record of a duplicated location), given its class byte and
+ * written with LasHeader::writePoint (las.cpp:822-904) into the file of its
+ * class, files balanced by points_per_file over the octree's blocks.
+ * cls: class byte per record (NULL = those of the last wb_classify), on the
+ * side of the records.  out receives the files' records back to back
+ * (n_distinct x wb_las_point_length(opt->point_format) bytes; device pointer
+ * if out_on_device).  files (max_files entries) receive each file;
+ * *n_files their count, also when max_files is too small (WB_EINVAL). */
+int wb_las_write_output(wb_ctx *ctx, const wb_cloud *cloud, int in_format, const uint8_t *cls,
+                        const wb_las_output *opt, void *out, int out_on_device, wb_las_file *files, int max_files,
+                        int *n_files);
+
+/* LasHeader::writeHeader (las.cpp:540-595) of one output file: 375 bytes of
+ * a LAS 1.4 header.  Fields the reference leaves unset (source id, global
+ * encoding, GUID, start of waveform data) are written as 0. */
+int wb_las_header_bytes(const wb_las_output *opt, const wb_las_file *file, uint8_t *header);
+
+/* The name CloudOutput::openFiles gives a file (cloudoutput.cpp:146-185):
+ * base-class[-NN].las, or base[-NN].las when classes are not separated. */
+int wb_las_file_name(const wb_las_output *opt, const wb_las_file *file, const char *base, char *buf, size_t cap);
+
+/* wb_las_write_output, then every file written to disk under its name
+ * (header + records), as writeFiles + closeFiles (cloudoutput.cpp:187-245). */
+int wb_las_write_files(wb_ctx *ctx, const wb_cloud *cloud, int in_format, const uint8_t *cls,
+                       const wb_las_output *opt, const char *base, wb_las_file *files, int max_files, int *n_files);
 
 /* ---- Serving and batching ----
  *

@@ -22,6 +22,15 @@
  *   wb_ref quadrant OUT               sin/cos(int) of 0, 90, 180, 270 degrees
  *   wb_ref flowsnake IDX OUT          toFlowsnake(n) for n in [loLim,hiLim]
  *   wb_ref lsq IN OUT                 linearLeastSquares on n x 3 systems
+ *   wb_ref lasrw IN OUT FMT UNIT SX SY SZ X0 Y0 Z0 X1 Y1 Z1 CLS FIELDS SYSID
+ *                                     LasHeader::readPoint of every record of
+ *                                     the LAS file IN (fields -> FIELDS), class
+ *                                     byte from CLS, writePoint into OUT opened
+ *                                     as CloudOutput::openFiles opens a file
+ *                                     (openWrite, setUnit, setScale, setVersion
+ *                                     1.4, setPointFormat), then writeHeader
+ *   wb_ref combine N S0x S0y S0z O0x O0y O0z ...   combineScales per axis
+ *   wb_ref join F0 F1 ...             joinPointFormat
  */
 #include <cstdio>
 #include <cstdlib>
@@ -44,6 +53,8 @@
 #include "boundrect.h"
 #include "leastsquares.h"
 #include "manysum.h"
+#include "las.h"
+#include <new>
 
 using namespace std;
 
@@ -344,6 +355,99 @@ static int runLsq(int argc, char **argv)
   return 0;
 }
 
+double combine1Scale(vector<double> &scales, vector<double> &offsets);
+
+/* A LasHeader built in zeroed memory, so that the fields its constructor and
+ * openWrite leave unset (source id, encoding, GUID, start of waveform data)
+ * read as 0 in the header written. */
+static LasHeader *zeroedHeader()
+{
+  void *mem = aligned_alloc(alignof(LasHeader), (sizeof(LasHeader) + alignof(LasHeader) - 1) / alignof(LasHeader) *
+                                                    alignof(LasHeader));
+  memset(mem, 0, sizeof(LasHeader));
+  return new (mem) LasHeader;
+}
+
+static int runLasRW(int argc, char **argv)
+{
+  if (argc < 18) die("lasrw IN OUT FMT UNIT SX SY SZ X0 Y0 Z0 X1 Y1 Z1 CLS FIELDS SYSID");
+  double unit = atof(argv[5]);
+  xyz scale(atof(argv[6]), atof(argv[7]), atof(argv[8]));
+  xyz lo(atof(argv[9]), atof(argv[10]), atof(argv[11])), hi(atof(argv[12]), atof(argv[13]), atof(argv[14]));
+  LasHeader *in = zeroedHeader(), *out = zeroedHeader();
+  in->setUnit(unit);
+  in->openRead(argv[2]);
+  size_t n = in->numberPoints();
+  vector<unsigned char> cls(n);
+  FILE *c = fopen(argv[15], "rb");
+  if (!c || fread(cls.data(), 1, n, c) != n) die("classes");
+  fclose(c);
+  out->openWrite(argv[3], atoi(argv[17]));
+  out->setUnit(unit);
+  out->setScale(lo, hi, scale);
+  out->setVersion(1, 4);
+  out->setPointFormat(atoi(argv[4]));
+  FILE *f = fopen(argv[16], "wb");
+  for (size_t i = 0; i < n; i++)
+  {
+    LasPoint p = in->readPoint(i);
+    double xyzv[3] = {p.location.getx(), p.location.gety(), p.location.getz()};
+    uint8_t sd = p.scanDirection, el = p.edgeLine;
+    int32_t ang = p.scanAngle;
+    fwrite(xyzv, 8, 3, f);
+    fwrite(&p.intensity, 2, 1, f);
+    fwrite(&p.returnNum, 2, 1, f);
+    fwrite(&p.nReturns, 2, 1, f);
+    fwrite(&sd, 1, 1, f);
+    fwrite(&el, 1, 1, f);
+    fwrite(&p.classification, 2, 1, f);
+    fwrite(&p.classificationFlags, 2, 1, f);
+    fwrite(&p.scannerChannel, 2, 1, f);
+    fwrite(&p.userData, 2, 1, f);
+    fwrite(&ang, 4, 1, f);
+    fwrite(&p.pointSource, 2, 1, f);
+    fwrite(&p.gpsTime, 8, 1, f);
+    fwrite(&p.red, 2, 1, f);
+    fwrite(&p.green, 2, 1, f);
+    fwrite(&p.blue, 2, 1, f);
+    fwrite(&p.nir, 2, 1, f);
+    p.classification = cls[i];
+    out->writePoint(p);
+  }
+  fclose(f);
+  out->writeHeader();
+  out->close();
+  in->close();
+  return 0;
+}
+
+static int runCombine(int argc, char **argv)
+{
+  if (argc < 3) die("combine N S O ...");
+  int n = atoi(argv[2]);
+  if (argc < 3 + 6 * n) die("combine: 6 numbers per file");
+  for (int k = 0; k < 3; k++)
+  {
+    vector<double> s, o;
+    for (int i = 0; i < n; i++)
+    {
+      s.push_back(atof(argv[3 + 6 * i + k]));
+      o.push_back(atof(argv[3 + 6 * i + 3 + k]));
+    }
+    printf("%.17g\n", combine1Scale(s, o));
+  }
+  return 0;
+}
+
+static int runJoin(int argc, char **argv)
+{
+  vector<int> f;
+  for (int i = 2; i < argc; i++)
+    f.push_back(atoi(argv[i]));
+  printf("%d\n", joinPointFormat(f));
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc < 2) die("mode required");
@@ -354,6 +458,9 @@ int main(int argc, char **argv)
   if (mode == "quadrant") return runQuadrant(argc, argv);
   if (mode == "flowsnake") return runFlowsnake(argc, argv);
   if (mode == "lsq") return runLsq(argc, argv);
+  if (mode == "lasrw") return runLasRW(argc, argv);
+  if (mode == "combine") return runCombine(argc, argv);
+  if (mode == "join") return runJoin(argc, argv);
   die("unknown mode");
   return 2;
 }

@@ -20,6 +20,9 @@ def _structs():
         "wb_job": _lib.wb_job,
         "wb_job_status": _lib.wb_job_status,
         "wb_server_stats": _lib.wb_server_stats,
+        "wb_las_points": _lib.wb_las_points,
+        "wb_las_output": _lib.wb_las_output,
+        "wb_las_file": _lib.wb_las_file,
     }
 
 

@@ -26,7 +26,8 @@ import numpy as np
 from . import _lib
 from ._lib import wb_cloud, wb_octree_stats, wb_params, wb_tile
 
-__all__ = ["Params", "Classifier", "Server", "WolkenbaseError", "cloud_struct"]
+__all__ = ["Params", "Classifier", "Server", "WolkenbaseError", "cloud_struct", "LasOutput", "las_point_length",
+           "join_point_format", "combine_scales", "las_header_bytes", "las_file_name"]
 
 
 class WolkenbaseError(RuntimeError):
@@ -233,6 +234,64 @@ class Classifier:
         self._check(self.L.wb_preview(self.ctx, x0, y0, side, w, h, cnt.ctypes.data, lo.ctypes.data, hi.ctypes.data))
         return cnt, lo, hi
 
+    # -- LAS records: full decode and the class-split writer --
+    def las_decode(self, records, point_format, scale, offset, unit=1.0, fields=None):
+        """LasHeader::readPoint of every (n, stride) uint8 record: a dict of one
+        array per LasPoint field (all fields, or those named in fields)."""
+        records = np.ascontiguousarray(records, np.uint8)
+        n, stride = records.shape
+        cs = cloud_struct(records, n, stride, scale, offset, unit, (0, 0, 0), (0, 0, 0))
+        names = [f for f, _ in _lib.LAS_POINT_FIELDS if fields is None or f in fields]
+        out = {f: np.zeros(n, np.dtype(t)) for f, t in _lib.LAS_POINT_FIELDS if f in names}
+        pts = _lib.wb_las_points(**{f: out[f].ctypes.data for f in names})
+        self._check(self.L.wb_las_decode(self.ctx, C.byref(cs), point_format, C.byref(pts)))
+        return out
+
+    def las_write_output(self, records, in_format, scale, offset, unit, output, cls=None):
+        """CloudOutput::writeFiles on the device for the built (and classified)
+        cloud whose (n, stride) records are given: (records of every file back
+        to back as (n_distinct, length) uint8, list of file dicts)."""
+        records = np.ascontiguousarray(records, np.uint8)
+        n, stride = records.shape
+        cs = cloud_struct(records, n, stride, scale, offset, unit, (0, 0, 0), (0, 0, 0))
+        o = output.c()
+        length = self.L.wb_las_point_length(o.point_format)
+        out = np.zeros((self.info()["n_distinct"], length), np.uint8)
+        cptr = None
+        if cls is not None:
+            cls = np.ascontiguousarray(cls, np.uint8)
+            cptr = cls.ctypes.data
+        nf = C.c_int(0)
+        rc = self.L.wb_las_write_output(self.ctx, C.byref(cs), in_format, cptr, C.byref(o), out.ctypes.data, 0,
+                                        None, 0, C.byref(nf))
+        files = (_lib.wb_las_file * max(1, nf.value))()
+        if rc == _lib.WB_EINVAL and nf.value:
+            rc = self.L.wb_las_write_output(self.ctx, C.byref(cs), in_format, cptr, C.byref(o), out.ctypes.data, 0,
+                                            files, nf.value, C.byref(nf))
+        self._check(rc)
+        return out, [_las_file_dict(files[i]) for i in range(nf.value)], files
+
+    def las_write_files(self, records, in_format, scale, offset, unit, output, base, cls=None, max_files=4096):
+        """Writes the class files (header + records) under base; returns the file dicts with their names."""
+        records = np.ascontiguousarray(records, np.uint8)
+        n, stride = records.shape
+        cs = cloud_struct(records, n, stride, scale, offset, unit, (0, 0, 0), (0, 0, 0))
+        o = output.c()
+        cptr = None
+        if cls is not None:
+            cls = np.ascontiguousarray(cls, np.uint8)
+            cptr = cls.ctypes.data
+        files = (_lib.wb_las_file * max_files)()
+        nf = C.c_int(0)
+        self._check(self.L.wb_las_write_files(self.ctx, C.byref(cs), in_format, cptr, C.byref(o), base.encode(),
+                                              files, max_files, C.byref(nf)))
+        res = []
+        for i in range(nf.value):
+            d = _las_file_dict(files[i])
+            d["name"] = las_file_name(output, files[i], base)
+            res.append(d)
+        return res
+
     # -- kernel settings (speed only; labels do not depend on them) --
     def tuning(self):
         t = _lib.wb_tuning()
@@ -264,6 +323,81 @@ class Classifier:
         ms = (C.c_float * 64)()
         self._check(self.L.wb_stage_times(self.ctx, names, ms, 64, C.byref(cnt)))
         return [(names[i].decode(), ms[i]) for i in range(cnt.value)]
+
+
+@dataclasses.dataclass
+class LasOutput:
+    """What CloudOutput is told before openFiles (wolkencanvas.cpp:614-622)."""
+    point_format: int = 6
+    separate_classes: bool = True
+    n_input_files: int = 1
+    points_per_file: int = 0
+    unit: float = 1.0
+    min_cor: tuple = (0.0, 0.0, 0.0)
+    max_cor: tuple = (0.0, 0.0, 0.0)
+    scale: tuple = (0.0, 0.0, 0.0)
+    creation_day: int = 0
+    creation_year: int = 0
+    software: str = None
+
+    def c(self):
+        o = _lib.wb_las_output()
+        o.point_format = self.point_format
+        o.separate_classes = 1 if self.separate_classes else 0
+        o.n_input_files = self.n_input_files
+        o.creation_day = self.creation_day
+        o.creation_year = self.creation_year
+        o.points_per_file = self.points_per_file
+        o.unit = self.unit
+        o.min_cor[:] = self.min_cor
+        o.max_cor[:] = self.max_cor
+        o.scale[:] = self.scale
+        o.software = self.software.encode() if self.software is not None else None
+        return o
+
+
+def _las_file_dict(f):
+    return {"class_id": f.class_id, "index": f.index, "name_digits": f.name_digits, "point_format": f.point_format,
+            "first": f.first, "n_points": list(f.n_points), "scale": tuple(f.scale), "offset": tuple(f.offset),
+            "min": tuple(f.min), "max": tuple(f.max)}
+
+
+def las_point_length(point_format):
+    return _lib.load().wb_las_point_length(point_format)
+
+
+def join_point_format(formats):
+    """joinPointFormat (las.cpp:103-118)."""
+    arr = (C.c_int * max(1, len(formats)))(*formats)
+    return _lib.load().wb_las_join_point_format(arr, len(formats))
+
+
+def combine_scales(scales, offsets):
+    """combineScales (las.cpp:925-944) of n files' (scale, offset) triples in metres."""
+    s = np.ascontiguousarray(scales, np.float64).reshape(-1, 3)
+    o = np.ascontiguousarray(offsets, np.float64).reshape(-1, 3)
+    out = np.zeros(3)
+    rc = _lib.load().wb_las_combine_scales(s.ctypes.data, o.ctypes.data, s.shape[0], out.ctypes.data)
+    if rc:
+        raise WolkenbaseError(rc, "wb_las_combine_scales")
+    return tuple(out)
+
+
+def las_header_bytes(output, file):
+    """LasHeader::writeHeader of one output file (a wb_las_file): 375 bytes."""
+    h = np.zeros(375, np.uint8)
+    rc = _lib.load().wb_las_header_bytes(C.byref(output.c()), C.byref(file), h.ctypes.data)
+    if rc:
+        raise WolkenbaseError(rc, "wb_las_header_bytes")
+    return h
+
+
+def las_file_name(output, file, base):
+    buf = C.create_string_buffer(4096)
+    rc = _lib.load().wb_las_file_name(C.byref(output.c()), C.byref(file), base.encode(), buf, 4096)
+    if rc:
+        raise WolkenbaseError(rc, "wb_las_file_name")
+    return buf.value.decode()
 
 
 class Server:

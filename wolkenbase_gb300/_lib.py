@@ -12,10 +12,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libwolkenbase_gb300.so")
 
 WB_OK, WB_EINVAL, WB_ENOMEM, WB_ECUDA, WB_EDEPTH, WB_ESTATE, WB_ETIMEDOUT, WB_ENOTFOUND = 0, -1, -2, -3, -4, -5, -6, -7
-WB_EBUSY, WB_ECANCELED = -8, -9
+WB_EBUSY, WB_ECANCELED, WB_EIO = -8, -9, -10
 ERROR_NAMES = {WB_EINVAL: "WB_EINVAL", WB_ENOMEM: "WB_ENOMEM", WB_ECUDA: "WB_ECUDA", WB_EDEPTH: "WB_EDEPTH",
                WB_ESTATE: "WB_ESTATE", WB_ETIMEDOUT: "WB_ETIMEDOUT", WB_ENOTFOUND: "WB_ENOTFOUND",
-               WB_EBUSY: "WB_EBUSY", WB_ECANCELED: "WB_ECANCELED"}
+               WB_EBUSY: "WB_EBUSY", WB_ECANCELED: "WB_ECANCELED", WB_EIO: "WB_EIO"}
 
 WB_FLUSH_EAGER, WB_FLUSH_FULL = 0, 1
 WB_PRECISION_EXACT, WB_PRECISION_FP32 = 0, 1
@@ -81,6 +81,32 @@ class wb_server_stats(C.Structure):
                 ("grid_points", C.c_double), ("tune_ms", C.c_double)]
 
 
+LAS_POINT_FIELDS = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("intensity", C.c_uint16),
+                    ("return_num", C.c_uint16), ("n_returns", C.c_uint16), ("scan_direction", C.c_uint8),
+                    ("edge_line", C.c_uint8), ("classification", C.c_uint16), ("class_flags", C.c_uint16),
+                    ("scanner_channel", C.c_uint16), ("user_data", C.c_uint16), ("scan_angle", C.c_int32),
+                    ("point_source", C.c_uint16), ("gps_time", C.c_double), ("red", C.c_uint16),
+                    ("green", C.c_uint16), ("blue", C.c_uint16), ("nir", C.c_uint16)]
+
+
+class wb_las_points(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name, _ in LAS_POINT_FIELDS]
+
+
+class wb_las_output(C.Structure):
+    _fields_ = [("point_format", C.c_int32), ("separate_classes", C.c_int32), ("n_input_files", C.c_int32),
+                ("creation_day", C.c_int32), ("creation_year", C.c_int32), ("pad", C.c_int32),
+                ("points_per_file", C.c_uint64), ("unit", C.c_double), ("min_cor", C.c_double * 3),
+                ("max_cor", C.c_double * 3), ("scale", C.c_double * 3), ("software", C.c_char_p)]
+
+
+class wb_las_file(C.Structure):
+    _fields_ = [("class_id", C.c_int32), ("index", C.c_int32), ("name_digits", C.c_int32),
+                ("point_format", C.c_int32), ("first", C.c_uint64), ("n_points", C.c_uint64 * 16),
+                ("scale", C.c_double * 3), ("offset", C.c_double * 3), ("min", C.c_double * 3),
+                ("max", C.c_double * 3)]
+
+
 # name -> (restype, argtypes); every symbol include/wolkenbase_gb300.h declares
 SIGNATURES = {
     "wb_open": (C.c_void_p, [C.c_int, C.c_size_t]),
@@ -118,6 +144,17 @@ SIGNATURES = {
                                         C.c_void_p]),
     "wb_preview": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                              C.c_void_p]),
+    "wb_las_point_length": (C.c_int, [C.c_int]),
+    "wb_las_decode": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud), C.c_int, C.POINTER(wb_las_points)]),
+    "wb_las_join_point_format": (C.c_int, [C.c_void_p, C.c_int]),
+    "wb_las_combine_scales": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "wb_las_write_output": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud), C.c_int, C.c_void_p, C.POINTER(wb_las_output),
+                                      C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "wb_las_header_bytes": (C.c_int, [C.POINTER(wb_las_output), C.POINTER(wb_las_file), C.c_void_p]),
+    "wb_las_file_name": (C.c_int, [C.POINTER(wb_las_output), C.POINTER(wb_las_file), C.c_char_p, C.c_char_p,
+                                   C.c_size_t]),
+    "wb_las_write_files": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud), C.c_int, C.c_void_p, C.POINTER(wb_las_output),
+                                     C.c_char_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "wb_server_open": (C.c_void_p, [C.POINTER(wb_server_config)]),
     "wb_server_close": (None, [C.c_void_p]),
     "wb_server_error": (C.c_char_p, [C.c_void_p]),
