@@ -243,6 +243,44 @@ def las_measure(clf, cloud, n, stream, device):
             "writer_workload": "format 1 in and out, separate classes, 10M points per file, device-resident"}
 
 
+def paging_measure(cloud, params, want_cls, device, args):
+    """The same cloud through wb_classify_cloud on a context whose HBM budget
+    holds about a third of its working set, paging on (buffers beyond the
+    budget in pinned host memory, used in place over the CPU link): Mpts/s with
+    host buffers in and out, the bytes placed on each side, and whether the
+    labels equal the unpaged run's."""
+    import ctypes as C
+    import torch
+    import wolkenbase_gb300 as wb
+    n = cloud.n
+    budget = int(n * 100)
+    clf = wb.Classifier(device, hbm_budget=budget)
+    try:
+        clf.set_paging(int(n * 400))
+    except wb.WolkenbaseError as e:
+        clf.close()
+        return {"unavailable": str(e)}
+    pin_xyz = torch.from_numpy(np.ascontiguousarray(cloud.xyz)).pin_memory()
+    pin_cls = torch.zeros(n, dtype=torch.uint8).pin_memory()
+    cs = wb.cloud_struct(pin_xyz.data_ptr(), n, 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+
+    def step():
+        clf._check(clf.L.wb_classify_cloud(clf.ctx, C.byref(cs), C.byref(params.c()), C.c_void_p(pin_cls.data_ptr())))
+
+    step()
+    reps = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        step()
+    dt = (time.perf_counter() - t0) / reps
+    st = clf.paging_stats()
+    same = bool(np.array_equal(pin_cls.numpy(), want_cls))
+    clf.close()
+    return {"workload": "the plain workload, HBM budget 100 B per point, host memory up to 400 B per point",
+            "hbm_budget": budget, "value": n / dt / 1e6, "unit": UNIT, "host_peak_bytes": st["host_peak"],
+            "device_bytes": st["device_bytes"], "same_labels": same}
+
+
 def _gen_tile(spec):
     from wolkenbase_gb300 import synth
     kind, n, seed, frac = spec
@@ -539,6 +577,7 @@ def main():
     same = bool(np.array_equal(pin_cls.numpy(), cls_dev))
 
     las = las_measure(clf, cloud, n, stream, local) if rank == 0 else None
+    paging = paging_measure(cloud, params, cls_dev, local, args) if rank == 0 and not args.no_forms else None
     info = clf.info()
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
     dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download", "classify_exact")), key=lambda k: stage_ms[k])
@@ -581,7 +620,7 @@ def main():
                      if build_ms else None, "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT},
            "octree": {"leaves": info["n_leaves"], "distinct": nd, "max_depth": info["max_depth"]},
            "labels": {"ground": int(labels[2]), "not_ground": int(labels[1]), "untouched": int(labels[0])},
-           "las": las}
+           "las": las, "paging": paging}
     clf.close()
     del dev_xyz, dev_cls, pin_xyz, pin_cls
     torch.cuda.empty_cache()

@@ -105,6 +105,21 @@ const char *wb_last_error(const wb_ctx *ctx);
 int wb_set_stream(wb_ctx *ctx, void *cuda_stream);
 int wb_synchronize(wb_ctx *ctx);
 
+/* Paging for clouds above the HBM budget (the reference pages octree blocks
+ * to store.oct through an LRU cache under lowRam back-pressure:
+ * octree.cpp:427-559, 1017-1147; threads.cpp:227-228).  Here buffers that do
+ * not fit the context's HBM budget are placed in pinned host memory -- on
+ * GB300 the Grace LPDDR5X behind NVLink-C2C -- and the kernels use them in
+ * place; a cloud whose working set is above the budget puts its sequential
+ * scratch buffers (sort ping-pong, record upload, tile lists) there first so
+ * that HBM keeps what the classify reads at random.  host_budget: bytes of
+ * host memory the context may pin (0 = off, the default: over-budget
+ * allocations fail with WB_ENOMEM).  Needs a device that uses host memory in
+ * place with native atomics (WB_EINVAL otherwise). */
+int wb_set_paging(wb_ctx *ctx, size_t host_budget);
+/* Host bytes held now and at most, and device bytes held now. */
+int wb_paging_stats(wb_ctx *ctx, uint64_t *host_bytes, uint64_t *host_peak, uint64_t *device_bytes);
+
 /* Octree::sizeFit + OctStore::put for every record + OctStore::split
  * (octree.cpp:268-347, 620-662, 849-876, 1295-1338).  Leaf cubes and the
  * point->leaf map equal the reference's; leaves are numbered in depth-first

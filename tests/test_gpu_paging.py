@@ -1,0 +1,49 @@
+"""Paging: a cloud whose working set is about three times the context's HBM
+budget is classified with the buffers beyond the budget in pinned host memory
+(used in place by the kernels), and the labels equal the unbudgeted run's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_paged_run_equals_resident_run():
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    cloud = synth.density_tile(1_500_000, 61)
+    clf = wb.Classifier(0)
+    want = clf.classify_cloud(cloud)
+    want_tiles = clf.tiles()
+    clf.close()
+    budget = 100 * cloud.n
+    tight = wb.Classifier(0, hbm_budget=budget)
+    try:
+        with pytest.raises(wb.WolkenbaseError) as e:
+            tight.classify_cloud(cloud)          # paging off: over budget
+        assert e.value.code == _lib.WB_ENOMEM
+        tight.set_paging(2 << 30)
+        got = tight.classify_cloud(cloud)
+        st = tight.paging_stats()
+        assert st["host_peak"] > 0 and st["device_bytes"] <= budget
+        assert np.array_equal(got, want)
+        assert np.array_equal(tight.tiles(), want_tiles)
+        # classes of the paged run feed the LAS steps the same way
+        assert tight.class_totals()[2] == np.count_nonzero(want[tight.store_order().astype(np.int64)] == 2)
+        tight.set_paging(0)
+    finally:
+        tight.close()
+
+
+def test_paging_host_budget_is_respected():
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    cloud = synth.density_tile(600_000, 62)
+    clf = wb.Classifier(0, hbm_budget=60 * cloud.n)
+    try:
+        clf.set_paging(16 << 20)                  # far too little host memory as well
+        with pytest.raises(wb.WolkenbaseError) as e:
+            clf.classify_cloud(cloud)
+        assert e.value.code == _lib.WB_ENOMEM
+        assert clf.paging_stats()["host_peak"] <= 16 << 20
+    finally:
+        clf.close()

@@ -186,6 +186,15 @@ class Classifier:
         self._check(self.L.wb_tile_planes(self.ctx, out.ctypes.data, T))
         return out
 
+    def set_paging(self, host_budget):
+        """Lets buffers beyond the HBM budget live in pinned host memory (0 turns it off)."""
+        self._check(self.L.wb_set_paging(self.ctx, int(host_budget)))
+
+    def paging_stats(self):
+        h, p, d = C.c_uint64(0), C.c_uint64(0), C.c_uint64(0)
+        self._check(self.L.wb_paging_stats(self.ctx, C.byref(h), C.byref(p), C.byref(d)))
+        return {"host_bytes": h.value, "host_peak": p.value, "device_bytes": d.value}
+
     def set_precision(self, mode):
         """_lib.WB_PRECISION_EXACT (bit-exact, default) or _lib.WB_PRECISION_FP32."""
         self._check(self.L.wb_set_precision(self.ctx, int(mode)))

@@ -114,6 +114,8 @@ SIGNATURES = {
     "wb_last_error": (C.c_char_p, [C.c_void_p]),
     "wb_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wb_synchronize": (C.c_int, [C.c_void_p]),
+    "wb_set_paging": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "wb_paging_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "wb_octree_build": (C.c_int, [C.c_void_p, C.POINTER(wb_cloud)]),
     "wb_octree_info": (C.c_int, [C.c_void_p, C.POINTER(wb_octree_stats)]),
     "wb_octree_leaves": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

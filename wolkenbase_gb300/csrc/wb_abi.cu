@@ -2,6 +2,7 @@
  * Each entry point's counterpart in the reference is named in
  * include/wolkenbase_gb300.h. */
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -25,13 +26,48 @@ int wb_fail(wb_ctx *c, int code, const std::string &msg)
 /* Buffers are stream-ordered allocations on the context's stream: growing
  * one frees the old block after the work queued before it, and neither call
  * waits for other streams (several contexts share a GPU in a server). */
+/* Buffers a pass reads or writes in order (sort ping-pong, scratch, the
+ * record upload, the tile lists): with paging, a cloud above the budget keeps
+ * them in host memory first, so that HBM holds what classify reads at random. */
+static bool coldBuffer(const wb_ctx *c, const DevBuf &b)
+{
+  const DevBuf *cold[] = {&c->rec, &c->key0, &c->key1, &c->idx0, &c->idx1, &c->tmp32, &c->tmp32b,
+                          &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->tilePts, &c->survivorOf, &c->pointLeaf};
+  for (const DevBuf *x : cold)
+    if (x == &b)
+      return true;
+  return false;
+}
+
+static const size_t kSpillMin = 1 << 20;   /* smaller scratch buffers stay in HBM while the budget allows */
+
 int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes)
 {
   if (bytes <= b.cap)
     return 0;
   size_t want = bytes + bytes / 8 + 256;
-  if (c->budget && c->used - b.cap + want > c->budget)
-    return wb_fail(c, WB_ENOMEM, "device memory budget exceeded (" + std::to_string(c->used - b.cap + want) +
+  const size_t devHeld = b.host ? 0 : b.cap, hostHeld = b.host ? b.cap : 0;
+  const bool over = c->budget && c->used - devHeld + want > c->budget;
+  const bool cold = c->spill_cold && want >= kSpillMin && coldBuffer(c, b);
+  if ((over || cold) && c->host_budget && c->host_used - hostHeld + want <= c->host_budget)
+  {
+    wb_free_buf(c, b);
+    cudaError_t e = cudaHostAlloc(&b.p, want, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e == cudaSuccess)
+    {
+      b.host = true;
+      b.cap = want;
+      c->host_used += want;
+      c->host_peak = std::max(c->host_peak, c->host_used);
+      return 0;
+    }
+    b.p = nullptr;
+    cudaGetLastError();
+    if (over)
+      return wb_fail(c, WB_ENOMEM, std::string("cudaHostAlloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
+  }
+  if (over)
+    return wb_fail(c, WB_ENOMEM, "device memory budget exceeded (" + std::to_string(c->used - devHeld + want) +
                                      " > " + std::to_string(c->budget) + " bytes)");
   wb_free_buf(c, b);
   cudaError_t e = cudaMallocAsync(&b.p, want, c->stream);
@@ -50,10 +86,21 @@ void wb_free_buf(wb_ctx *c, DevBuf &b)
 {
   if (!b.p)
     return;
-  cudaFreeAsync(b.p, c->stream);
-  c->used -= b.cap;
+  if (b.host)
+  {
+    // kernels may still use it: host memory has no stream-ordered free
+    cudaStreamSynchronize(c->stream);
+    cudaFreeHost(b.p);
+    c->host_used -= b.cap;
+  }
+  else
+  {
+    cudaFreeAsync(b.p, c->stream);
+    c->used -= b.cap;
+  }
   b.p = nullptr;
   b.cap = 0;
+  b.host = false;
 }
 
 void wb_mark(wb_ctx *c, const char *name)
@@ -231,6 +278,36 @@ int wb_stage_times(wb_ctx *c, const char **names, float *ms, uint32_t capacity, 
   return 0;
 }
 
+int wb_set_paging(wb_ctx *c, size_t host_budget)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (host_budget)
+  {
+    int mapped = 0, atomics = 0;
+    cudaDeviceGetAttribute(&mapped, cudaDevAttrCanMapHostMemory, c->device);
+    cudaDeviceGetAttribute(&atomics, cudaDevAttrHostNativeAtomicSupported, c->device);
+    if (!mapped || !atomics)
+      return wb_fail(c, WB_EINVAL, "wb_set_paging: the device cannot use host memory in place with atomics "
+                                   "(needs a coherent CPU link such as NVLink-C2C)");
+  }
+  c->host_budget = host_budget;
+  return 0;
+}
+
+int wb_paging_stats(wb_ctx *c, uint64_t *host_bytes, uint64_t *host_peak, uint64_t *device_bytes)
+{
+  if (!c)
+    return WB_EINVAL;
+  if (host_bytes)
+    *host_bytes = c->host_used;
+  if (host_peak)
+    *host_peak = c->host_peak;
+  if (device_bytes)
+    *device_bytes = c->used;
+  return 0;
+}
+
 int wb_octree_build(wb_ctx *c, const wb_cloud *cloud)
 {
   if (!c || !cloud)
@@ -282,12 +359,12 @@ int wb_octree_leaves(wb_ctx *c, double *cs, uint32_t *first, uint32_t *count)
     return 0;
   std::vector<uint64_t> key(L);
   std::vector<uint8_t> lev(L);
-  WB_CUDA(c, cudaMemcpyAsync(key.data(), c->leafKey.p, L * 8, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(lev.data(), c->leafLevel.p, L, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(key.data(), c->leafKey.p, L * 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(lev.data(), c->leafLevel.p, L, cudaMemcpyDefault, c->stream));
   if (first)
-    WB_CUDA(c, cudaMemcpyAsync(first, c->leafFirst.p, L * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(first, c->leafFirst.p, L * 4, cudaMemcpyDefault, c->stream));
   if (count)
-    WB_CUDA(c, cudaMemcpyAsync(count, c->leafCount.p, L * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(count, c->leafCount.p, L * 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   if (cs)
     for (uint64_t l = 0; l < L; l++)
@@ -319,7 +396,7 @@ int wb_octree_point_leaf(wb_ctx *c, uint32_t *out)
     return wb_fail(c, WB_ESTATE, "wb_octree_point_leaf: no octree built");
   if (c->n)
   {
-    WB_CUDA(c, cudaMemcpyAsync(out, c->pointLeaf.p, c->n * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(out, c->pointLeaf.p, c->n * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   return 0;
@@ -333,7 +410,7 @@ int wb_octree_store_order(wb_ctx *c, uint32_t *out)
     return wb_fail(c, WB_ESTATE, "wb_octree_store_order: no octree built");
   if (c->nd)
   {
-    WB_CUDA(c, cudaMemcpyAsync(out, c->sidx.p, c->nd * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(out, c->sidx.p, c->nd * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   return 0;
@@ -373,7 +450,7 @@ int wb_tiles(wb_ctx *c, wb_tile *out, uint64_t capacity, uint64_t *count)
   if (capacity < T)
     return wb_fail(c, WB_EINVAL, "wb_tiles: capacity below the tile count");
   std::vector<TileRes> r(T);
-  WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   for (uint64_t k = 0; k < T; k++)
   {
@@ -446,7 +523,7 @@ int wb_tile_planes(wb_ctx *c, double *abc, uint64_t capacity)
   cudaSetDevice(c->device);
   std::vector<TileRes> r(T);
   if (T)
-    WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   for (uint64_t k = 0; k < T; k++)
     for (int i = 0; i < 3; i++)
@@ -611,11 +688,11 @@ extern "C" int wb_octree_find_block_static(wb_ctx *c, const double *xyz, uint64_
     r.lo[k] = c->g.root_lo[k];
   r.side = c->g.root_side;
   r.cell = c->g.cell;
-  WB_CUDA(c, cudaMemcpyAsync(s.in, xyz, m * 24, cudaMemcpyHostToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(s.in, xyz, m * 24, cudaMemcpyDefault, c->stream));
   { findBlockKernel<<<(unsigned)std::min<uint64_t>((m + 255) / 256, 4096), 256, 0, c->stream>>>(
         s.in, m, r, (const uint64_t *)c->leafKey.p, (const uint8_t *)c->leafLevel.p, c->n_leaves, s.out); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
-  WB_CUDA(c, cudaMemcpyAsync(leaf, s.out, m * 8, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(leaf, s.out, m * 8, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -636,11 +713,11 @@ int wb_find_block_impl(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf)
     r.lo[k] = c->g.root_lo[k];
   r.side = c->g.root_side;
   r.cell = c->g.cell;
-  cudaMemcpyAsync(in.p, xyz, m * 24, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(in.p, xyz, m * 24, cudaMemcpyDefault, c->stream);
   { findBlockKernel<<<(unsigned)std::min<uint64_t>((m + 255) / 256, 4096), 256, 0, c->stream>>>(
       (const double *)in.p, m, r, (const uint64_t *)c->leafKey.p, (const uint8_t *)c->leafLevel.p, c->n_leaves,
       (int64_t *)out.p); ++c->launches; }
-  cudaMemcpyAsync(leaf, out.p, m * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(leaf, out.p, m * 8, cudaMemcpyDefault, c->stream);
   wb_free_buf(c, in);
   wb_free_buf(c, out);
   cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -691,12 +768,12 @@ int withDevice(size_t inBytes, const void *in, size_t outBytes, void *out, F lau
     return WB_ENOMEM;
   }
   int rc = 0;
-  if (cudaMemcpy(din, in, inBytes, cudaMemcpyHostToDevice) != cudaSuccess)
+  if (cudaMemcpy(din, in, inBytes, cudaMemcpyDefault) != cudaSuccess)
     rc = WB_ECUDA;
   if (!rc)
   {
     launch(din, dout);
-    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, outBytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, outBytes, cudaMemcpyDefault) != cudaSuccess)
       rc = WB_ECUDA;
   }
   cudaFree(din);
@@ -715,9 +792,9 @@ int wb_check_atan2i(const double *yx, uint64_t m, int32_t *out)
   double *tab = nullptr;
   if (cudaMalloc(&tab, 1535 * 8) != cudaSuccess)
     return WB_ENOMEM;
-  cudaMemcpy(tab, kWbTan, 511 * 8, cudaMemcpyHostToDevice);
-  cudaMemcpy(tab + 511, kWbSin, 512 * 8, cudaMemcpyHostToDevice);
-  cudaMemcpy(tab + 1023, kWbCos, 512 * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(tab, kWbTan, 511 * 8, cudaMemcpyDefault);
+  cudaMemcpy(tab + 511, kWbSin, 512 * 8, cudaMemcpyDefault);
+  cudaMemcpy(tab + 1023, kWbCos, 512 * 8, cudaMemcpyDefault);
   int rc = withDevice(m * 16, yx, m * 4, out, [&](void *din, void *dout) {
     atanCheckKernel<<<(unsigned)((m + 255) / 256 < 4096 ? (m + 255) / 256 : 4096), 256>>>((const double *)din, m, tab,
                                                                                          (int32_t *)dout);

@@ -513,6 +513,10 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if (cl->n > 0xfffffff0ull)
     return wb_fail(c, WB_EINVAL, "wb_octree_build: at most 2^32-16 points per cloud");
   uint64_t n = cl->n;
+  // with paging, a cloud whose working set (about 300 B per point plus the
+  // records) is above the HBM budget keeps its scratch buffers in host memory
+  c->spill_cold = c->host_budget && c->budget &&
+                  n * (300ull + (cl->device_resident ? 0 : cl->stride)) > c->budget;
   WbGeom &g = c->g;
   for (int a = 0; a < 3; a++)
   {
@@ -557,7 +561,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   {
     if ((rc = wb_ensure(c, c->rec, n * (uint64_t)cl->stride)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(c->rec.p, cl->records, n * (uint64_t)cl->stride, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->rec.p, cl->records, n * (uint64_t)cl->stride, cudaMemcpyDefault, c->stream));
     a.rec = (const uint8_t *)c->rec.p;
   }
   wb_mark(c, "upload");
@@ -596,7 +600,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if ((rc = wb_exclusive_scan_u32(c, surv, rank, n, dTot)))
     return rc;
   uint32_t ndh = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&ndh, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&ndh, dTot, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   uint64_t nd = ndh;
   c->nd = nd;
@@ -626,8 +630,8 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
     return rc;
   uint32_t Lh = 0;
   int errh = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&Lh, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(&errh, dErr, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&Lh, dTot, 4, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&errh, dErr, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   if (errh)
     return wb_fail(c, WB_EDEPTH, "wb_octree_build: more than 537 distinct points in a cell 21 levels below the root");
@@ -657,7 +661,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   { pointLeafKernel<<<gridFor(c, n), 256, 0, c->stream>>>(n, storeOf, leafId, (uint32_t *)c->pointLeaf.p); ++c->launches; }
   { maxLevelKernel<<<gridFor(c, L), 256, 0, c->stream>>>(L, leafLev, dMax); ++c->launches; }
   int maxLev = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&maxLev, dMax, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&maxLev, dMax, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   c->max_depth = (uint32_t)maxLev;
   wb_mark(c, "point_map");
@@ -673,7 +677,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if ((rc = wb_exclusive_scan_u32(c, flag, flagEx, LD, dTot)))
     return rc;
   uint32_t Nh = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&Nh, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&Nh, dTot, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   uint64_t N = Nh;
   c->n_nodes = N;

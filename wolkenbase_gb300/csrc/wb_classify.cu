@@ -1051,12 +1051,12 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   if (!onDevice && (rc = wb_ensure(c, c->clsDev, n + 64)))
     return rc;
   double *tab = (double *)c->angleT.p;
-  WB_CUDA(c, cudaMemcpyAsync(tab, kWbTan, 511 * 8, cudaMemcpyHostToDevice, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(tab + 511, kWbSin, 512 * 8, cudaMemcpyHostToDevice, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(tab + 1023, kWbCos, 512 * 8, cudaMemcpyHostToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(tab, kWbTan, 511 * 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(tab + 511, kWbSin, 512 * 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(tab + 1023, kWbCos, 512 * 8, cudaMemcpyDefault, c->stream));
   uint8_t *clsDev = onDevice ? cls : (uint8_t *)c->clsDev.p;
   if (!onDevice && n)
-    WB_CUDA(c, cudaMemcpyAsync(clsDev, cls, n, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(clsDev, cls, n, cudaMemcpyDefault, c->stream));
   wb_mark(c, "cls_upload");
   a.nd = nd;
   const WbGeom &g = c->g;
@@ -1424,7 +1424,7 @@ cudaError_t ringsGrid(WbBatch *b, int shape, unsigned *grid)
 cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned grids[3], wb_ctx *mark)
 {
   const unsigned grid = (unsigned)b->sm * 8;
-  cudaError_t e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyDefault, s);
   if (e != cudaSuccess)
     return e;
   batchSetup<<<grid, 256, 0, s>>>(b->dIn);
@@ -1441,7 +1441,7 @@ cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned g
   batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
   batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
   batchScatter<<<grid, 256, 0, s>>>(b->dIn);
-  e = cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDeviceToHost, s);
+  e = cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDefault, s);
   if (e == cudaSuccess)
     e = cudaGetLastError();
   return e;
@@ -1596,7 +1596,7 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
   if (e == cudaSuccess)
     e = cudaEventCreate(&e1);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(b->dIn, b->hIn, sizeof(BatchHdr), cudaMemcpyDefault, s);
   if (e == cudaSuccess)
   {
     batchSetup<<<(unsigned)b->sm * 8, 256, 0, s>>>(b->dIn);
@@ -1649,7 +1649,7 @@ int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int 
     wb_ctx *c = jobs[q];
     ClsArgs *a = (ClsArgs *)c->clsArgs;
     if (c->clsHost && c->n)
-      e = cudaMemcpyAsync(c->clsHost, a->cls, c->n, cudaMemcpyDeviceToHost, s);
+      e = cudaMemcpyAsync(c->clsHost, a->cls, c->n, cudaMemcpyDefault, s);
   }
   if (e != cudaSuccess)
   {
@@ -1696,7 +1696,7 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   c->launches += 10;
   ClsArgs *a = (ClsArgs *)c->clsArgs;
   if (!onDevice && c->n)
-    WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDefault, c->stream));
   wb_mark(c, "cls_download");
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   wb_batch_collect(b, &c, 1);

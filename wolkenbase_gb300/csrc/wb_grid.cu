@@ -242,7 +242,7 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   int *dExt = (int *)((char *)c->small.p + 512);
   static const int kExtInit[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};
   WB_CUDA(c, cudaMemsetAsync(dStray, 0, 8, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(dExt, kExtInit, 24, cudaMemcpyHostToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(dExt, kExtInit, 24, cudaMemcpyDefault, c->stream));
   unsigned blocks = (unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
   uint64_t *key = (uint64_t *)c->gKey0.p;
   uint32_t *val = (uint32_t *)c->gVal0.p;
@@ -286,9 +286,9 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   unsigned long long ns = 0;
   uint32_t ngroups = 0;
   int ext[6];
-  WB_CUDA(c, cudaMemcpyAsync(&ns, dStray, 8, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(ext, dExt, 24, cudaMemcpyDeviceToHost, c->stream));
-  WB_CUDA(c, cudaMemcpyAsync(&ngroups, gTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&ns, dStray, 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(ext, dExt, 24, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&ngroups, gTot, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   c->grid.nGroups = ngroups;
   c->grid.nStray = ns;

@@ -14,6 +14,7 @@ struct DevBuf
 {
   void *p = nullptr;
   size_t cap = 0;
+  bool host = false;   /* pinned host memory the kernels use in place (paging) */
 };
 
 struct WbGeom
@@ -50,6 +51,10 @@ struct wb_ctx
   bool own_stream = false;
   size_t budget = 0;
   std::atomic<size_t> used{0};      /* device bytes held (read by a server's scheduler) */
+  /* paging (wb_set_paging): buffers beyond the HBM budget in pinned host memory */
+  size_t host_budget = 0;
+  size_t host_used = 0, host_peak = 0;
+  bool spill_cold = false;          /* this cloud needs more than the budget: scratch buffers go to the host */
   std::string err;
   int sm_count = 0;
   uint64_t launches = 0;            /* kernels launched by this context */

@@ -142,7 +142,7 @@ int wb_class_totals(wb_ctx *c, uint64_t *totals)
   if (c->nd)
     { classTotalsKernel<<<gridOf(c, c->nd), 256, 0, c->stream>>>(c->nd, (const uint32_t *)c->sidx.p, c->clsFinal,
                                                                   (unsigned long long *)out.b.p); ++c->launches; }
-  cudaError_t e = cudaMemcpyAsync(totals, out.b.p, 256 * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaMemcpyAsync(totals, out.b.p, 256 * 8, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
@@ -166,7 +166,7 @@ int wb_duplicates(wb_ctx *c, uint64_t *n_dup, uint32_t *dup_of)
     return rc;
   { dupKernel<<<gridOf(c, c->n), 256, 0, c->stream>>>(c->n, (const uint32_t *)c->storeOf.p,
                                                        (const uint32_t *)c->sidx.p, (uint32_t *)out.b.p); ++c->launches; }
-  cudaError_t e = cudaMemcpyAsync(dup_of, out.b.p, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaMemcpyAsync(dup_of, out.b.p, c->n * 4, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
@@ -195,19 +195,19 @@ int wb_las_write_classes(wb_ctx *c, void *records, uint64_t n, uint32_t stride, 
     if ((rc = wb_ensure(c, rbuf.b, n * stride)))
       return rc;
     drec = (uint8_t *)rbuf.b.p;
-    WB_CUDA(c, cudaMemcpyAsync(drec, records, n * stride, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(drec, records, n * stride, cudaMemcpyDefault, c->stream));
     if (cls)
     {
       if ((rc = wb_ensure(c, cbuf.b, n)))
         return rc;
-      WB_CUDA(c, cudaMemcpyAsync(cbuf.b.p, cls, n, cudaMemcpyHostToDevice, c->stream));
+      WB_CUDA(c, cudaMemcpyAsync(cbuf.b.p, cls, n, cudaMemcpyDefault, c->stream));
       dcls = (const uint8_t *)cbuf.b.p;
     }
   }
   { writeClassesKernel<<<gridOf(c, n), 256, 0, c->stream>>>(drec, n, stride, point_format, dcls); ++c->launches; }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !on_device)
-    e = cudaMemcpyAsync(records, drec, n * stride, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(records, drec, n * stride, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
@@ -236,7 +236,7 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
   {
     if ((rc = wb_ensure(c, rin.b, n * stride)) || (rc = wb_ensure(c, rout.b, n * stride)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, records, n * stride, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, records, n * stride, cudaMemcpyDefault, c->stream));
     din = (const uint8_t *)rin.b.p;
     dout = (uint8_t *)rout.b.p;
   }
@@ -262,9 +262,9 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
   uint64_t h[256];
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(h, hist.b.p, sizeof h, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(h, hist.b.p, sizeof h, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess && !on_device)
-    e = cudaMemcpyAsync(out, dout, n * stride, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(out, dout, n * stride, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
@@ -372,11 +372,11 @@ extern "C" int wb_preview(wb_ctx *c, double x0, double y0, double side, int w, i
   std::vector<int> zlo(npix), zhi(npix);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && count)
-    e = cudaMemcpyAsync(count, cnt.b.p, npix * 8, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(count, cnt.b.p, npix * 8, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(zlo.data(), zl.b.p, npix * 4, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(zlo.data(), zl.b.p, npix * 4, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(zhi.data(), zh.b.p, npix * 4, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(zhi.data(), zh.b.p, npix * 4, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)

@@ -799,7 +799,7 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
   {
     if ((rc = wb_ensure(c, rin.b, n * cloud->stride)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, cloud->records, n * cloud->stride, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, cloud->records, n * cloud->stride, cudaMemcpyDefault, c->stream));
     a.rec = (const uint8_t *)rin.b.p;
     // device arrays for the wanted fields, carved from one buffer
     struct F
@@ -838,7 +838,7 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
     cudaError_t e = cudaGetLastError();
     for (F &f : fs)
       if (f.host && e == cudaSuccess)
-        e = cudaMemcpyAsync(f.host, *f.dev, n * f.size, cudaMemcpyDeviceToHost, c->stream);
+        e = cudaMemcpyAsync(f.host, *f.dev, n * f.size, cudaMemcpyDefault, c->stream);
     if (e == cudaSuccess)
       e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess)
@@ -900,7 +900,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   {
     if ((rc = wb_ensure(c, rin.b, n * cloud->stride)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, cloud->records, n * cloud->stride, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(rin.b.p, cloud->records, n * cloud->stride, cudaMemcpyDefault, c->stream));
     a.rec = (const uint8_t *)rin.b.p;
   }
   else
@@ -914,7 +914,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   {
     if ((rc = wb_ensure(c, cin.b, n + 16)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(cin.b.p, cls, n, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(cin.b.p, cls, n, cudaMemcpyDefault, c->stream));
     a.cls = (const uint8_t *)cin.b.p;
   }
   a.sidx = (const uint32_t *)c->sidx.p;
@@ -929,7 +929,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   if (nd)
     { storedTotals<<<gridOf(c, nd), kBlock, 0, c->stream>>>(nd, a.sidx, a.cls, (unsigned long long *)tot.b.p); ++c->launches; }
   uint64_t T[256];
-  WB_CUDA(c, cudaMemcpyAsync(T, tot.b.p, sizeof T, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(T, tot.b.p, sizeof T, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
 
   Plan P = planFiles(T, opt);
@@ -949,7 +949,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
       return rc;
     WB_CUDA(c, cudaMemsetAsync(counts.b.p, 0, L * S * 4, c->stream));
     { setCountKernel<<<gridOf(c, L * 32, 8), kBlock, 0, c->stream>>>(a, (uint32_t *)counts.b.p); ++c->launches; }
-    WB_CUDA(c, cudaMemcpyAsync(cnt.data(), counts.b.p, L * S * 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(cnt.data(), counts.b.p, L * S * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
   }
 
@@ -1001,8 +1001,8 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   {
     if ((rc = wb_ensure(c, bases.b, L * S * 8)) || (rc = wb_ensure(c, fileOf.b, L * S * 4)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(bases.b.p, base.data(), L * S * 8, cudaMemcpyHostToDevice, c->stream));
-    WB_CUDA(c, cudaMemcpyAsync(fileOf.b.p, fof.data(), L * S * 4, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(bases.b.p, base.data(), L * S * 8, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(fileOf.b.p, fof.data(), L * S * 4, cudaMemcpyDefault, c->stream));
     a.base = (unsigned long long *)bases.b.p;
     a.fileOf = (const uint32_t *)fileOf.b.p;
     const size_t slots = 2 * (size_t)kBlock * kSlotWords * 4;
@@ -1021,9 +1021,9 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   std::vector<FileStat> fs(P.nFiles + 1);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(fs.data(), a.stats, sizeof(FileStat) * (P.nFiles + 1), cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(fs.data(), a.stats, sizeof(FileStat) * (P.nFiles + 1), cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess && !out_on_device && outBytes)
-    e = cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)

@@ -280,7 +280,7 @@ int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *k
   WB_CUDA(c, cudaMemsetAsync(dOr, 0, 8, c->stream));
   { keySpread<<<c->sm_count * 4, 256, 0, c->stream>>>(keys, n, dOr); ++c->launches; }
   unsigned long long spread = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&spread, dOr, 8, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&spread, dOr, 8, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   int numTiles = (int)((n + kSortTile - 1) / kSortTile);
   size_t cntBytes = (size_t)numTiles * 256 * sizeof(uint32_t);

@@ -1179,9 +1179,9 @@ static int uploadTiles(wb_ctx *c)
     if ((rc = wb_ensure(c, c->tileEx, T * 4 + 64)) || (rc = wb_ensure(c, c->tileEy, T * 4 + 64)) ||
         (rc = wb_ensure(c, c->tileLookup, look.size() * 4 + 64)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(c->tileEx.p, c->flowHostEx.data(), T * 4, cudaMemcpyHostToDevice, c->stream));
-    WB_CUDA(c, cudaMemcpyAsync(c->tileEy.p, c->flowHostEy.data(), T * 4, cudaMemcpyHostToDevice, c->stream));
-    WB_CUDA(c, cudaMemcpyAsync(c->tileLookup.p, look.data(), look.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->tileEx.p, c->flowHostEx.data(), T * 4, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->tileEy.p, c->flowHostEy.data(), T * 4, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(c->tileLookup.p, look.data(), look.size() * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
     c->flowIdxCached = g.snake_idx;
   }
@@ -1243,11 +1243,11 @@ static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
 {
   std::vector<uint32_t> list(nh), last(nh);
   std::vector<uint64_t> pre(nh + 1, 0);
-  WB_CUDA(c, cudaMemcpyAsync(list.data(), c->tileHuge.p, nh * 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(list.data(), c->tileHuge.p, nh * 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   const uint32_t *tileN = (const uint32_t *)c->tileN.p;
   for (uint32_t h = 0; h < nh; h++)
-    WB_CUDA(c, cudaMemcpyAsync(&last[h], tileN + list[h], 4, cudaMemcpyDeviceToHost, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(&last[h], tileN + list[h], 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   for (uint32_t h = 0; h < nh; h++)
     pre[h + 1] = pre[h] + last[h];
@@ -1257,7 +1257,7 @@ static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
       (rc = wb_ensure(c, c->key1, total * 8 + 64)) || (rc = wb_ensure(c, c->idx0, total * 4 + 64)) ||
       (rc = wb_ensure(c, c->idx1, total * 4 + 64)))
     return rc;
-  WB_CUDA(c, cudaMemcpyAsync(c->hugePre.p, pre.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(c->hugePre.p, pre.data(), (nh + 1) * 8, cudaMemcpyDefault, c->stream));
   uint64_t *keys = (uint64_t *)c->key0.p;
   uint32_t *vals = (uint32_t *)c->idx0.p;
   unsigned g = (unsigned)std::min<uint64_t>((total + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
@@ -1315,9 +1315,9 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
   if ((rc = wb_exclusive_scan_u32(c, bound, tileStart, T, dTot)))
     return rc;
-  WB_CUDA(c, cudaMemcpyAsync(tileStart + T, dTot, 4, cudaMemcpyDeviceToDevice, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(tileStart + T, dTot, 4, cudaMemcpyDefault, c->stream));
   uint32_t room = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&room, dTot, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&room, dTot, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   if ((rc = wb_ensure(c, c->tilePts, (uint64_t)room * 4 + 64)))
     return rc;
@@ -1335,7 +1335,7 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
                                                                    (uint32_t *)c->tileHuge.p); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   int nHuge = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&nHuge, dOvf, 4, cudaMemcpyDeviceToHost, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(&nHuge, dOvf, 4, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   if (nHuge && (rc = sortHugeTiles(c, (uint32_t)nHuge, tileStart)))
     return rc;
