@@ -90,6 +90,7 @@ struct wb_ctx
   struct WbBatch *batch = nullptr;  /* job table of the batch-of-one launch */
   double grid_bounds[4] = {0, 0, 0, 0};   /* x0, y0, x1, y1 the column grid spans */
   DevBuf flowCache;
+  DevBuf lasAngles;                 /* scan-angle tables of the LAS decode and writer */
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
   int flowIdxCached = -1;
   int lookupX0 = 0, lookupY0 = 0, lookupW = 0, lookupH = 0;

@@ -87,6 +87,7 @@ struct LasPt
 {
   double x, y, z, gps;
   int32_t angle;
+  uint32_t angleRaw;   /* the record's scan-angle byte or short */
   uint16_t intensity, ret, nret, cls, flags, chan, user, src, r, g, b, nir;
   bool sdir, edge;
 };
@@ -132,9 +133,23 @@ __device__ __forceinline__ uint64_t lrintBits(double v)
   return (uint64_t)__double2ll_rn(v);
 }
 
-/* rottobin / degtobin / bintodeg (angle.cpp:199-243): 2^31 units per turn,
- * the fraction of a turn folded into [-1, 1) with modf. */
-__device__ __forceinline__ int32_t degToBin(double deg)
+/* Scan angles.  A record holds a signed byte of degrees (formats 0-5) or a
+ * signed short of 0.006 degrees (6-10); readPoint turns it into 2^31 units
+ * per turn with degtobin, and writePoint back with lrint(bintodeg(...)) or
+ * lrint(bintodeg(...)/0.006) (angle.cpp:199-243, las.cpp:758, 772, 857, 866).
+ * Both are functions of the record's value alone, so they are tabulated once
+ * per context on the host (double arithmetic as the reference's, no FMA) and
+ * the kernels look them up instead of running FP64 divisions. */
+struct AngleTabs
+{
+  const int32_t *bin8, *bin16;      /* degtobin of each byte / short value   */
+  const uint8_t *deg8of8, *deg8of16; /* written byte (formats 0-5) of each value */
+  const uint16_t *deg16of8, *deg16of16; /* written short (formats 6-10) of each value */
+};
+
+constexpr size_t kAngleBytes = 256 * 4 + 65536 * 4 + 256 + 65536 + 256 * 2 + 65536 * 2;
+
+int32_t hostDegToBin(double deg)
 {
   double ip;
   double f = 2 * modf(deg / 360 / 2, &ip);
@@ -142,11 +157,51 @@ __device__ __forceinline__ int32_t degToBin(double deg)
     f -= 2;
   if (f < -1)
     f += 2;
-  return (int32_t)(uint32_t)lrintBits(2147483648. * f);
+  return (int32_t)(uint32_t)(uint64_t)(int64_t)llrint(2147483648. * f);
 }
-__device__ __forceinline__ double binToDeg(int32_t a)
+
+double hostBinToDeg(int32_t a)
 {
   return a / 2147483648. * 360;
+}
+
+/* Builds (once per context) and returns the device tables. */
+int angleTables(wb_ctx *c, AngleTabs &t)
+{
+  const bool ready = c->lasAngles.p && c->lasAngles.cap >= kAngleBytes;
+  int rc = wb_ensure(c, c->lasAngles, kAngleBytes);
+  if (rc)
+    return rc;
+  uint8_t *base = (uint8_t *)c->lasAngles.p;
+  t.bin8 = (const int32_t *)base;
+  t.bin16 = t.bin8 + 256;
+  t.deg16of8 = (const uint16_t *)(t.bin16 + 65536);
+  t.deg16of16 = t.deg16of8 + 256;
+  t.deg8of8 = (const uint8_t *)(t.deg16of16 + 65536);
+  t.deg8of16 = t.deg8of8 + 256;
+  if (ready)
+    return 0;
+  std::vector<uint8_t> h(kAngleBytes);
+  int32_t *bin8 = (int32_t *)h.data(), *bin16 = bin8 + 256;
+  uint16_t *d16of8 = (uint16_t *)(bin16 + 65536), *d16of16 = d16of8 + 256;
+  uint8_t *d8of8 = (uint8_t *)(d16of16 + 65536), *d8of16 = d8of8 + 256;
+  for (int v = 0; v < 256; v++)
+    bin8[v] = hostDegToBin((double)(int8_t)v);
+  for (int v = 0; v < 65536; v++)
+    bin16[v] = hostDegToBin((double)(int16_t)v * 0.006);
+  for (int v = 0; v < 256; v++)
+  {
+    d8of8[v] = (uint8_t)llrint(hostBinToDeg(bin8[v]));
+    d16of8[v] = (uint16_t)llrint(hostBinToDeg(bin8[v]) / 0.006);
+  }
+  for (int v = 0; v < 65536; v++)
+  {
+    d8of16[v] = (uint8_t)llrint(hostBinToDeg(bin16[v]));
+    d16of16[v] = (uint16_t)llrint(hostBinToDeg(bin16[v]) / 0.006);
+  }
+  WB_CUDA(c, cudaMemcpyAsync(base, h.data(), kAngleBytes, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return 0;
 }
 
 /* Copies the first len bytes of a record into a shared-memory slot; words
@@ -180,12 +235,19 @@ __device__ __forceinline__ void storeRecord(uint8_t *dst, const uint8_t *slot, i
 }
 
 /* LasHeader::readPoint (las.cpp:735-820) from a record in shared memory. */
-__device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layout &L, const Decode &d, LasPt &p)
+__device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layout &L, const Decode &d,
+                                            const AngleTabs &at, LasPt &p)
 {
   const int32_t X = (int32_t)rd32(s, 0), Y = (int32_t)rd32(s, 4), Z = (int32_t)rd32(s, 8);
-  p.x = (d.off[0] + d.scale[0] * (double)X) * d.unit;
-  p.y = (d.off[1] + d.scale[1] * (double)Y) * d.unit;
-  p.z = (d.off[2] + d.scale[2] * (double)Z) * d.unit;
+  p.x = d.off[0] + d.scale[0] * (double)X;
+  p.y = d.off[1] + d.scale[1] * (double)Y;
+  p.z = d.off[2] + d.scale[2] * (double)Z;
+  if (d.unit != 1)   // x * 1 == x: the product only where it can change the value
+  {
+    p.x *= d.unit;
+    p.y *= d.unit;
+    p.z *= d.unit;
+  }
   p.intensity = (uint16_t)rd16(s, 12);
   if (f < 6)
   {
@@ -197,7 +259,8 @@ __device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layou
     p.flags = (c >> 5) & 7;
     p.cls = c & 31;
     p.chan = 0;
-    p.angle = degToBin((double)(int8_t)s[16]);
+    p.angleRaw = s[16];
+    p.angle = __ldg(at.bin8 + p.angleRaw);
     p.user = s[17];
     p.src = (uint16_t)rd16(s, 18);
   }
@@ -212,7 +275,8 @@ __device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layou
     p.edge = (u >> 7) & 1;
     p.cls = s[16];
     p.user = s[17];
-    p.angle = degToBin((double)(int16_t)rd16(s, 18) * 0.006);
+    p.angleRaw = rd16(s, 18);
+    p.angle = __ldg(at.bin16 + p.angleRaw);
     p.src = (uint16_t)rd16(s, 20);
   }
   p.gps = L.gps >= 0 ? __longlong_as_double((long long)rd64(s, L.gps)) : 0.0;
@@ -235,12 +299,15 @@ struct Encode
 /* The record integer writePoint computes (las.cpp:827-829). */
 __device__ __forceinline__ int32_t quantise(double v, double unit, double off, double scale)
 {
-  return (int32_t)(uint32_t)lrintBits((v / unit - off) / scale);
+  if (unit != 1)   // v / 1 == v
+    v = v / unit;
+  return (int32_t)(uint32_t)lrintBits((v - off) / scale);
 }
 
 /* LasHeader::writePoint (las.cpp:822-904) into a shared-memory slot; the
  * waveform part is written as zeros (the reference's build without WAVEFORM). */
-__device__ __forceinline__ void encodeRecord(uint8_t *o, int f, const Layout &L, const LasPt &p, const int32_t *q)
+__device__ __forceinline__ void encodeRecord(uint8_t *o, int f, const Layout &L, const LasPt &p, const int32_t *q,
+                                             bool in16, const AngleTabs &t)
 {
   wr32(o, 0, (uint32_t)q[0]);
   wr32(o, 4, (uint32_t)q[1]);
@@ -250,7 +317,7 @@ __device__ __forceinline__ void encodeRecord(uint8_t *o, int f, const Layout &L,
   {
     o[14] = (uint8_t)((p.ret & 7) + ((p.nret & 7) << 3) + ((p.sdir & 1) << 6) + ((p.edge & 1) << 7));
     o[15] = (uint8_t)((p.cls & 31) + ((p.flags & 7) << 5));
-    o[16] = (uint8_t)lrintBits(binToDeg(p.angle));
+    o[16] = __ldg((in16 ? t.deg8of16 : t.deg8of8) + p.angleRaw);
     o[17] = (uint8_t)p.user;
     wr16(o, 18, p.src);
   }
@@ -260,7 +327,7 @@ __device__ __forceinline__ void encodeRecord(uint8_t *o, int f, const Layout &L,
     o[15] = (uint8_t)((p.flags & 15) + ((p.chan & 3) << 4) + ((p.sdir & 1) << 6) + ((p.edge & 1) << 7));
     o[16] = (uint8_t)p.cls;
     o[17] = (uint8_t)p.user;
-    wr16(o, 18, (uint32_t)lrintBits(binToDeg(p.angle) / 0.006));
+    wr16(o, 18, __ldg((in16 ? t.deg16of16 : t.deg16of8) + p.angleRaw));
     wr16(o, 20, p.src);
   }
   if (L.gps >= 0)
@@ -286,41 +353,78 @@ struct DecodeArgs
   uint64_t n;
   uint32_t stride;
   int fmt;
-  bool words;
+  bool words, vec16;
   Decode d;
+  AngleTabs t;
   wb_las_points o;
 };
 
+/* One warp per 32 consecutive records: when the records start on a 16-byte
+ * boundary and a record is at most kStageStride bytes, the warp copies its 32
+ * records into shared memory with coalesced 16-byte loads and each lane parses
+ * its own record there; otherwise each lane loads its record into its slot. */
+constexpr int kStageStride = 80;
+
 __global__ void __launch_bounds__(kBlock) decodeKernel(const DecodeArgs a)
 {
+  __shared__ __align__(16) uint8_t stage[kBlock / 32][32 * kStageStride];
   __shared__ uint32_t slots[kBlock * kSlotWords];
-  uint8_t *s = (uint8_t *)(slots + threadIdx.x * kSlotWords);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Layout L = layoutOf(a.fmt);
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x)
+  const bool staged = a.vec16 && a.stride <= (uint32_t)kStageStride;
+  const uint64_t chunks = (a.n + 31) / 32;
+  for (uint64_t ch = (uint64_t)blockIdx.x * (kBlock / 32) + warp; ch < chunks; ch += (uint64_t)gridDim.x * (kBlock / 32))
   {
-    loadRecord(s, a.rec + i * a.stride, L.len, a.words);
-    LasPt p;
-    parseRecord(s, a.fmt, L, a.d, p);
-    const wb_las_points &o = a.o;
-    if (o.x) o.x[i] = p.x;
-    if (o.y) o.y[i] = p.y;
-    if (o.z) o.z[i] = p.z;
-    if (o.intensity) o.intensity[i] = p.intensity;
-    if (o.return_num) o.return_num[i] = p.ret;
-    if (o.n_returns) o.n_returns[i] = p.nret;
-    if (o.scan_direction) o.scan_direction[i] = p.sdir;
-    if (o.edge_line) o.edge_line[i] = p.edge;
-    if (o.classification) o.classification[i] = p.cls;
-    if (o.class_flags) o.class_flags[i] = p.flags;
-    if (o.scanner_channel) o.scanner_channel[i] = p.chan;
-    if (o.user_data) o.user_data[i] = p.user;
-    if (o.scan_angle) o.scan_angle[i] = p.angle;
-    if (o.point_source) o.point_source[i] = p.src;
-    if (o.gps_time) o.gps_time[i] = p.gps;
-    if (o.red) o.red[i] = p.r;
-    if (o.green) o.green[i] = p.g;
-    if (o.blue) o.blue[i] = p.b;
-    if (o.nir) o.nir[i] = p.nir;
+    const uint64_t i0 = ch * 32, i = i0 + lane;
+    const uint8_t *s;
+    if (staged)
+    {
+      // 32 records of a multiple-of-32 stride start on a 16-byte boundary
+      const uint64_t start = i0 * a.stride;
+      const uint32_t bytes = (uint32_t)((min(i0 + 32, a.n) - i0) * a.stride);
+      const uint4 *src = (const uint4 *)(a.rec + start);
+      uint4 *dst = (uint4 *)stage[warp];
+      const uint32_t vecs = bytes >> 4;
+      for (uint32_t v = lane; v < vecs; v += 32)
+        dst[v] = __ldg(src + v);
+      for (uint32_t b = (vecs << 4) + lane; b < bytes; b += 32)
+        stage[warp][b] = __ldg(a.rec + start + b);
+      __syncwarp();
+      s = stage[warp] + lane * a.stride;
+    }
+    else
+    {
+      uint8_t *slot = (uint8_t *)(slots + threadIdx.x * kSlotWords);
+      if (i < a.n)
+        loadRecord(slot, a.rec + i * a.stride, L.len, a.words);
+      s = slot;
+    }
+    if (i < a.n)
+    {
+      LasPt p;
+      parseRecord(s, a.fmt, L, a.d, a.t, p);
+      const wb_las_points &o = a.o;
+      if (o.x) o.x[i] = p.x;
+      if (o.y) o.y[i] = p.y;
+      if (o.z) o.z[i] = p.z;
+      if (o.intensity) o.intensity[i] = p.intensity;
+      if (o.return_num) o.return_num[i] = p.ret;
+      if (o.n_returns) o.n_returns[i] = p.nret;
+      if (o.scan_direction) o.scan_direction[i] = p.sdir;
+      if (o.edge_line) o.edge_line[i] = p.edge;
+      if (o.classification) o.classification[i] = p.cls;
+      if (o.class_flags) o.class_flags[i] = p.flags;
+      if (o.scanner_channel) o.scanner_channel[i] = p.chan;
+      if (o.user_data) o.user_data[i] = p.user;
+      if (o.scan_angle) o.scan_angle[i] = p.angle;
+      if (o.point_source) o.point_source[i] = p.src;
+      if (o.gps_time) o.gps_time[i] = p.gps;
+      if (o.red) o.red[i] = p.r;
+      if (o.green) o.green[i] = p.g;
+      if (o.blue) o.blue[i] = p.b;
+      if (o.nir) o.nir[i] = p.nir;
+    }
+    __syncwarp();
   }
 }
 
@@ -344,6 +448,7 @@ struct WriteArgs
   int outWidth;                  /* widest store the output records allow: 4, 2 or 1 */
   Decode d;
   Encode e;
+  AngleTabs t;
   uint8_t *out;
   uint64_t nLeaves;
   const uint32_t *leafFirst, *leafCount, *sidx;
@@ -422,13 +527,13 @@ __global__ void __launch_bounds__(kBlock) writeKernel(const WriteArgs a)
         const uint32_t s = a.setOf[cl];
         loadRecord(si, a.rec + (uint64_t)idx * a.stride, Li.len, a.inWords);
         LasPt p;
-        parseRecord(si, a.inFmt, Li, a.d, p);
+        parseRecord(si, a.inFmt, Li, a.d, a.t, p);
         p.cls = cl;
         int32_t q[3];
         q[0] = quantise(p.x, a.e.unit, a.e.off[0], a.e.scale[0]);
         q[1] = quantise(p.y, a.e.unit, a.e.off[1], a.e.scale[1]);
         q[2] = quantise(p.z, a.e.unit, a.e.off[2], a.e.scale[2]);
-        encodeRecord(so, a.outFmt, Lo, p, q);
+        encodeRecord(so, a.outFmt, Lo, p, q, a.inFmt >= 6, a.t);
         // the block's points of one set go to one file, in store order
         const unsigned gm = __match_any_sync(act, s);
         const int leader = __ffs(gm) - 1;
@@ -790,64 +895,67 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
   }
   a.d.unit = cloud->unit;
   TmpBuf rin{c, {}}, fields{c, {}};
-  if (cloud->device_resident)
+  const bool host = !cloud->device_resident;
+  a.rec = (const uint8_t *)cloud->records;
+  a.o = *out;
+  // with host records and arrays: the records go up, the wanted fields come
+  // back from device arrays carved out of one buffer
+  struct Field
   {
-    a.rec = (const uint8_t *)cloud->records;
-    a.o = *out;
-  }
-  else
+    void *host;
+    void **dev;
+    size_t size;
+  };
+  wb_las_points &o = a.o;
+  Field fs[] = {{out->x, (void **)&o.x, 8},
+                {out->y, (void **)&o.y, 8},
+                {out->z, (void **)&o.z, 8},
+                {out->intensity, (void **)&o.intensity, 2},
+                {out->return_num, (void **)&o.return_num, 2},
+                {out->n_returns, (void **)&o.n_returns, 2},
+                {out->scan_direction, (void **)&o.scan_direction, 1},
+                {out->edge_line, (void **)&o.edge_line, 1},
+                {out->classification, (void **)&o.classification, 2},
+                {out->class_flags, (void **)&o.class_flags, 2},
+                {out->scanner_channel, (void **)&o.scanner_channel, 2},
+                {out->user_data, (void **)&o.user_data, 2},
+                {out->scan_angle, (void **)&o.scan_angle, 4},
+                {out->point_source, (void **)&o.point_source, 2},
+                {out->gps_time, (void **)&o.gps_time, 8},
+                {out->red, (void **)&o.red, 2},
+                {out->green, (void **)&o.green, 2},
+                {out->blue, (void **)&o.blue, 2},
+                {out->nir, (void **)&o.nir, 2}};
+  if (host)
   {
     if ((rc = wb_ensure(c, rin.b, n * cloud->stride)))
       return rc;
     WB_CUDA(c, cudaMemcpyAsync(rin.b.p, cloud->records, n * cloud->stride, cudaMemcpyDefault, c->stream));
     a.rec = (const uint8_t *)rin.b.p;
-    // device arrays for the wanted fields, carved from one buffer
-    struct F
-    {
-      void *host;
-      void **dev;
-      size_t size;
-    };
-    wb_las_points &o = a.o;
-    o = *out;
-    F fs[] = {{out->x, (void **)&o.x, 8},          {out->y, (void **)&o.y, 8},
-              {out->z, (void **)&o.z, 8},          {out->intensity, (void **)&o.intensity, 2},
-              {out->return_num, (void **)&o.return_num, 2}, {out->n_returns, (void **)&o.n_returns, 2},
-              {out->scan_direction, (void **)&o.scan_direction, 1}, {out->edge_line, (void **)&o.edge_line, 1},
-              {out->classification, (void **)&o.classification, 2}, {out->class_flags, (void **)&o.class_flags, 2},
-              {out->scanner_channel, (void **)&o.scanner_channel, 2}, {out->user_data, (void **)&o.user_data, 2},
-              {out->scan_angle, (void **)&o.scan_angle, 4}, {out->point_source, (void **)&o.point_source, 2},
-              {out->gps_time, (void **)&o.gps_time, 8}, {out->red, (void **)&o.red, 2},
-              {out->green, (void **)&o.green, 2},  {out->blue, (void **)&o.blue, 2},
-              {out->nir, (void **)&o.nir, 2}};
     size_t total = 0;
-    for (F &f : fs)
+    for (Field &f : fs)
       if (f.host)
         total += (n * f.size + 255) & ~(size_t)255;
     if (total && (rc = wb_ensure(c, fields.b, total)))
       return rc;
     size_t at = 0;
-    for (F &f : fs)
+    for (Field &f : fs)
       if (f.host)
       {
         *f.dev = (uint8_t *)fields.b.p + at;
         at += (n * f.size + 255) & ~(size_t)255;
       }
-    a.words = ((uintptr_t)a.rec % 4 == 0) && (a.stride % 4 == 0);
-    { decodeKernel<<<gridOf(c, n), kBlock, 0, c->stream>>>(a); ++c->launches; }
-    cudaError_t e = cudaGetLastError();
-    for (F &f : fs)
-      if (f.host && e == cudaSuccess)
-        e = cudaMemcpyAsync(f.host, *f.dev, n * f.size, cudaMemcpyDefault, c->stream);
-    if (e == cudaSuccess)
-      e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess)
-      return wb_fail(c, WB_ECUDA, std::string("wb_las_decode: ") + cudaGetErrorString(e));
-    return 0;
   }
+  if ((rc = angleTables(c, a.t)))
+    return rc;
   a.words = ((uintptr_t)a.rec % 4 == 0) && (a.stride % 4 == 0);
+  a.vec16 = (uintptr_t)a.rec % 16 == 0;
   { decodeKernel<<<gridOf(c, n), kBlock, 0, c->stream>>>(a); ++c->launches; }
   cudaError_t e = cudaGetLastError();
+  if (host)
+    for (Field &f : fs)
+      if (f.host && e == cudaSuccess)
+        e = cudaMemcpyAsync(f.host, *f.dev, n * f.size, cudaMemcpyDefault, c->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
@@ -890,6 +998,8 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   for (int k = 0; k < 3; k++)
     setScale(opt->min_cor[k], opt->max_cor[k], opt->scale[k], opt->unit, a.e.scale[k], a.e.off[k]);
   a.e.unit = opt->unit;
+  if ((rc = angleTables(c, a.t)))
+    return rc;
   for (int k = 0; k < 3; k++)
     if (!(a.e.scale[k] > 0) || !std::isfinite(a.e.scale[k]))
       return wb_fail(c, WB_EINVAL, "wb_las_write_output: the output box and scale give no positive record scale");
@@ -958,25 +1068,37 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   std::vector<uint64_t> fileCount(P.nFiles, 0), base(L * S, 0);
   std::vector<uint32_t> fof(L * S, 0);
   typedef std::pair<uint64_t, int> Entry;
-  std::vector<std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>>> heaps(S);
   for (uint32_t s = 0; s < S; s++)
-    for (int i = 0; i < P.setFiles[s]; i++)
-      heaps[s].push(Entry(0, P.setFile0[s] + i));
-  for (uint64_t leaf = 0; leaf < L; leaf++)
-    for (uint32_t s = 0; s < S; s++)
+  {
+    const int f0 = P.setFile0[s], nf = P.setFiles[s];
+    std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> heap;
+    if (nf > 16)
+      for (int i = 0; i < nf; i++)
+        heap.push(Entry(0, f0 + i));
+    for (uint64_t leaf = 0; leaf < L; leaf++)
     {
       const uint32_t k = cnt[leaf * S + s];
       if (!k)
         continue;
-      if (heaps[s].empty())
+      if (!nf)
         return wb_fail(c, WB_ESTATE, "wb_las_write_output: points of a class without a file");
-      Entry e = heaps[s].top();
-      heaps[s].pop();
-      base[leaf * S + s] = fileCount[e.second];
-      fof[leaf * S + s] = (uint32_t)e.second;
-      fileCount[e.second] += k;
-      heaps[s].push(Entry(fileCount[e.second], e.second));
+      int f = f0;
+      if (nf > 16)
+      {
+        f = heap.top().second;
+        heap.pop();
+      }
+      else
+        for (int i = 1; i < nf; i++)
+          if (fileCount[f0 + i] < fileCount[f])
+            f = f0 + i;
+      base[leaf * S + s] = fileCount[f];
+      fof[leaf * S + s] = (uint32_t)f;
+      fileCount[f] += k;
+      if (nf > 16)
+        heap.push(Entry(fileCount[f], f));
     }
+  }
   std::vector<uint64_t> fileFirst(P.nFiles + 1, 0);
   for (int f = 0; f < P.nFiles; f++)
     fileFirst[f + 1] = fileFirst[f] + fileCount[f];
