@@ -85,7 +85,8 @@ __host__ __device__ inline Layout layoutOf(int f)
 /* A LasPoint in registers. */
 struct LasPt
 {
-  double x, y, z, gps;
+  int32_t X[3];        /* the record integers */
+  double gps;
   int32_t angle;
   uint32_t angleRaw;   /* the record's scan-angle byte or short */
   uint16_t intensity, ret, nret, cls, flags, chan, user, src, r, g, b, nir;
@@ -238,16 +239,9 @@ __device__ __forceinline__ void storeRecord(uint8_t *dst, const uint8_t *slot, i
 __device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layout &L, const Decode &d,
                                             const AngleTabs &at, LasPt &p)
 {
-  const int32_t X = (int32_t)rd32(s, 0), Y = (int32_t)rd32(s, 4), Z = (int32_t)rd32(s, 8);
-  p.x = d.off[0] + d.scale[0] * (double)X;
-  p.y = d.off[1] + d.scale[1] * (double)Y;
-  p.z = d.off[2] + d.scale[2] * (double)Z;
-  if (d.unit != 1)   // x * 1 == x: the product only where it can change the value
-  {
-    p.x *= d.unit;
-    p.y *= d.unit;
-    p.z *= d.unit;
-  }
+  p.X[0] = (int32_t)rd32(s, 0);
+  p.X[1] = (int32_t)rd32(s, 4);
+  p.X[2] = (int32_t)rd32(s, 8);
   p.intensity = (uint16_t)rd16(s, 12);
   if (f < 6)
   {
@@ -291,17 +285,36 @@ __device__ __forceinline__ void parseRecord(const uint8_t *s, int f, const Layou
   p.nir = L.nir >= 0 ? (uint16_t)rd16(s, L.nir) : 0;
 }
 
+/* The location readPoint computes (las.cpp:808): (offset + scale*X) * unit. */
+__device__ __forceinline__ double decodeAxis(const Decode &d, int32_t X, int k)
+{
+  const double v = d.off[k] + d.scale[k] * (double)X;
+  return d.unit != 1 ? v * d.unit : v;   // x * 1 == x
+}
+
 struct Encode
 {
-  double off[3], scale[3], unit;
+  double off[3], scale[3], inv[3], unit;   /* inv = 1/scale rounded */
+  bool shift[3];                           /* the record integer moves by a constant */
+  long long by[3];
 };
 
-/* The record integer writePoint computes (las.cpp:827-829). */
-__device__ __forceinline__ int32_t quantise(double v, double unit, double off, double scale)
+/* The record integer writePoint computes (las.cpp:827-829):
+ * lrint((v/unit - off)/scale), wrapped to int.  The quotient is first taken
+ * as a product with the rounded reciprocal, which lies within 3 units in the
+ * last place of the rounded quotient; unless that puts it within 2^-19 of a
+ * half-integer (or outside the int range), both round to the same integer, so
+ * the FP64 division runs only in those rare cases. */
+__device__ __forceinline__ int32_t quantise(double v, const Encode &e, int k)
 {
-  if (unit != 1)   // v / 1 == v
-    v = v / unit;
-  return (int32_t)(uint32_t)lrintBits((v - off) / scale);
+  if (e.unit != 1)   // v / 1 == v
+    v = v / e.unit;
+  const double t = v - e.off[k];
+  const double y = t * e.inv[k];
+  const double r = rint(y);
+  if (fabs(y) < 2147483648.0 && 0.5 - fabs(y - r) > 0x1p-19)
+    return (int32_t)(long long)r;
+  return (int32_t)(uint32_t)lrintBits(t / e.scale[k]);
 }
 
 /* LasHeader::writePoint (las.cpp:822-904) into a shared-memory slot; the
@@ -404,9 +417,9 @@ __global__ void __launch_bounds__(kBlock) decodeKernel(const DecodeArgs a)
       LasPt p;
       parseRecord(s, a.fmt, L, a.d, a.t, p);
       const wb_las_points &o = a.o;
-      if (o.x) o.x[i] = p.x;
-      if (o.y) o.y[i] = p.y;
-      if (o.z) o.z[i] = p.z;
+      if (o.x) o.x[i] = decodeAxis(a.d, p.X[0], 0);
+      if (o.y) o.y[i] = decodeAxis(a.d, p.X[1], 1);
+      if (o.z) o.z[i] = decodeAxis(a.d, p.X[2], 2);
       if (o.intensity) o.intensity[i] = p.intensity;
       if (o.return_num) o.return_num[i] = p.ret;
       if (o.n_returns) o.n_returns[i] = p.nret;
@@ -530,9 +543,9 @@ __global__ void __launch_bounds__(kBlock) writeKernel(const WriteArgs a)
         parseRecord(si, a.inFmt, Li, a.d, a.t, p);
         p.cls = cl;
         int32_t q[3];
-        q[0] = quantise(p.x, a.e.unit, a.e.off[0], a.e.scale[0]);
-        q[1] = quantise(p.y, a.e.unit, a.e.off[1], a.e.scale[1]);
-        q[2] = quantise(p.z, a.e.unit, a.e.off[2], a.e.scale[2]);
+        for (int k = 0; k < 3; k++)
+          q[k] = a.e.shift[k] ? (int32_t)(uint32_t)(unsigned long long)((long long)p.X[k] + a.e.by[k])
+                              : quantise(decodeAxis(a.d, p.X[k], k), a.e, k);
         encodeRecord(so, a.outFmt, Lo, p, q, a.inFmt >= 6, a.t);
         // the block's points of one set go to one file, in store order
         const unsigned gm = __match_any_sync(act, s);
@@ -998,6 +1011,29 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   for (int k = 0; k < 3; k++)
     setScale(opt->min_cor[k], opt->max_cor[k], opt->scale[k], opt->unit, a.e.scale[k], a.e.off[k]);
   a.e.unit = opt->unit;
+  for (int k = 0; k < 3; k++)
+  {
+    a.e.inv[k] = 1 / a.e.scale[k];
+    // Same unit and scale in and out: writePoint's integer is X + D whenever
+    // delta = (offset_in - offset_out)/scale lies within 1/4 - err of the
+    // integer D, err bounding every rounding of decode and re-encode over the
+    // whole int32 range (a few units of 2^-53 times the magnitudes involved).
+    a.e.shift[k] = false;
+    a.e.by[k] = 0;
+    if (cloud->unit == opt->unit && cloud->scale[k] == a.e.scale[k] && a.e.scale[k] > 0)
+    {
+      const double delta = (cloud->offset[k] - a.e.off[k]) / a.e.scale[k];
+      const double D = std::rint(delta);
+      const double err = 8 * 0x1p-53 *
+                         (4294967296.0 + (std::fabs(cloud->offset[k]) + std::fabs(a.e.off[k])) / a.e.scale[k] +
+                          std::fabs(delta));
+      if (std::isfinite(delta) && std::fabs(D) < 0x1p60 && std::fabs(delta - D) + err < 0.25)
+      {
+        a.e.shift[k] = true;
+        a.e.by[k] = (long long)D;
+      }
+    }
+  }
   if ((rc = angleTables(c, a.t)))
     return rc;
   for (int k = 0; k < 3; k++)
