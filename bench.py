@@ -11,7 +11,8 @@ value:  points / second with the cloud already resident in HBM (device
         pointer in, device class bytes out), CUDA events on the library's
         stream, max over ranks.
 e2e:    the same through wb_classify_cloud with pinned host buffers: the
-        int32 XYZ copy in and the class-byte copy out are inside the timing.
+        int32 XYZ and initial class-byte copies in and the class-byte copy
+        out are inside the timing.
 --impl reference: the reference's CPU algorithm (the oracle restatement,
         oracle/) on this machine's cores, on a bounded sample of the workload.
 Multi-GPU runs are independent replicas (one cloud per rank, no collective).
@@ -575,6 +576,12 @@ def main():
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, f"cuda:{local}")
     e2e_value = world * n / e2e_s / 1e6
     same = bool(np.array_equal(pin_cls.numpy(), cls_dev))
+    # where the end-to-end step's extra time goes: one more (untimed) host-buffer
+    # step with the library's stage events on
+    clf.profile(True)
+    step_host()
+    e2e_stages = {k: round(v, 3) for k, v in clf.stage_times()}
+    clf.profile(False)
 
     las = las_measure(clf, cloud, n, stream, local) if rank == 0 else None
     paging = paging_measure(cloud, params, cls_dev, local, args) if rank == 0 and not args.no_forms else None
@@ -611,8 +618,8 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n, "d2h_bytes_per_step": n,
-                   "same_labels_as_device_run": same},
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 13 * n, "d2h_bytes_per_step": n,
+                   "same_labels_as_device_run": same, "ms_per_step": e2e_s * 1e3, "stages_ms": e2e_stages},
            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
            "stages_ms": {k: round(v, 3) for k, v in stage_ms.items()},
            "build": {"ms": build_ms, "achieved_GBps": BUILD_BYTES_PER_POINT * n / (build_ms / 1e3) / 1e9

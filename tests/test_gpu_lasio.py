@@ -174,3 +174,34 @@ def test_write_files_to_disk(classifier, tmp_path):
     assert len(names) == len(written)
     assert sum(w["n_points"][0] for w in written) == classifier.info()["n_distinct"]
     assert not any(os.path.basename(w["name"]).startswith("cloud-raw") for w in written)   # ppf > 0: no empty raw file
+
+
+@pytest.mark.parametrize("offset,unit", [((1000.0005, 2000.00025, 100.0), 1.0),       # half-unit offsets: FP64 path
+                                         ((0.0, 0.0, 0.0), 1200 / 3937),                 # feet, integer path
+                                         ((333.3333, -7.0, 0.1), 1.0)])
+def test_writer_coordinate_paths_match_restatement(classifier, offset, unit):
+    """Same scale in and out takes the integer path when the offsets allow it
+    and the FP64 path otherwise; both equal writePoint's arithmetic."""
+    import wolkenbase_gb300 as wb
+    from oracle import las_oracle as LO
+    from wolkenbase_gb300 import synth
+    base = synth.density_tile(30_000, 55)
+    cloud = synth.Cloud(base.xyz, base.scale, offset, unit, base.minc, base.maxc)
+    d = cloud.decoded()
+    cloud.minc = tuple(float(v) / unit for v in d.min(axis=0))
+    cloud.maxc = tuple(float(v) / unit for v in d.max(axis=0))
+    rec = _attributed_records(cloud, 1, 21)
+    cls = np.random.default_rng(4).integers(1, 3, cloud.n).astype(np.uint8)
+    classifier.build(cloud)
+    _, first, count = classifier.leaves()
+    sidx = classifier.store_order().astype(np.int64)
+    scale_m = tuple(float(s) * unit for s in cloud.scale)      # the same record scale out
+    o = wb.LasOutput(point_format=1, separate_classes=True, unit=unit, min_cor=tuple(d.min(axis=0)),
+                     max_cor=tuple(d.max(axis=0)), scale=scale_m)
+    recs, files, _ = classifier.las_write_output(rec, 1, cloud.scale, cloud.offset, unit, o, cls=cls)
+    want_recs, want_files = LO.write_output(rec, 1, cloud.scale, cloud.offset, unit, cls, first, count, sidx,
+                                            dict(point_format=1, separate_classes=True, points_per_file=0, unit=unit,
+                                                 min_cor=o.min_cor, max_cor=o.max_cor, scale=o.scale))
+    assert np.array_equal(recs, want_recs)
+    for f, w in zip(files, want_files):
+        assert (f["min"], f["max"], f["n_points"]) == (w["min"], w["max"], list(w["n_points"]))

@@ -47,3 +47,26 @@ def test_paging_host_budget_is_respected():
         assert clf.paging_stats()["host_peak"] <= 16 << 20
     finally:
         clf.close()
+
+
+def test_pinned_inputs_are_read_in_place():
+    """Records and class bytes in pinned host memory are pulled by a kernel;
+    the labels equal those of a pageable-buffer run (odd byte counts take the
+    tail through the copy engine)."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import synth
+    cloud = synth.density_tile(300_001, 63)
+    clf = wb.Classifier(0)
+    try:
+        want = clf.classify_cloud(cloud)
+        pin = torch.from_numpy(np.ascontiguousarray(cloud.xyz)).pin_memory()
+        pcls = torch.zeros(cloud.n, dtype=torch.uint8).pin_memory()
+        cs = wb.cloud_struct(pin.data_ptr(), cloud.n, 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc,
+                             cloud.maxc)
+        clf._check(clf.L.wb_classify_cloud(clf.ctx, C.byref(cs), C.byref(wb.Params().c()),
+                                           C.c_void_p(pcls.data_ptr())))
+        assert np.array_equal(pcls.numpy(), want)
+    finally:
+        clf.close()

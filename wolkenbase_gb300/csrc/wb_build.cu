@@ -561,7 +561,8 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   {
     if ((rc = wb_ensure(c, c->rec, n * (uint64_t)cl->stride)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(c->rec.p, cl->records, n * (uint64_t)cl->stride, cudaMemcpyDefault, c->stream));
+    if ((rc = wb_copy_in(c, c->rec.p, cl->records, n * (uint64_t)cl->stride)))
+      return rc;
     a.rec = (const uint8_t *)c->rec.p;
   }
   wb_mark(c, "upload");

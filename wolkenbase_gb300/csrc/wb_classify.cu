@@ -1055,8 +1055,8 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   WB_CUDA(c, cudaMemcpyAsync(tab + 511, kWbSin, 512 * 8, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaMemcpyAsync(tab + 1023, kWbCos, 512 * 8, cudaMemcpyDefault, c->stream));
   uint8_t *clsDev = onDevice ? cls : (uint8_t *)c->clsDev.p;
-  if (!onDevice && n)
-    WB_CUDA(c, cudaMemcpyAsync(clsDev, cls, n, cudaMemcpyDefault, c->stream));
+  if (!onDevice && n && (rc = wb_copy_in(c, clsDev, cls, n)))
+    return rc;
   wb_mark(c, "cls_upload");
   a.nd = nd;
   const WbGeom &g = c->g;

@@ -228,7 +228,42 @@ __global__ void keySpread(const uint64_t *__restrict__ keys, uint64_t n, unsigne
   if ((threadIdx.x & 31) == 0 && acc)
     atomicOr(orBits, (unsigned long long)acc);
 }
+__global__ void pullKernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, uint64_t n16)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
 }  // namespace
+
+/* Copy of a caller's host buffer into device memory, in stream order.  Pinned
+ * host memory is read in place by a kernel over the CPU link (GB300: NVLink-C2C,
+ * the same rate as the copy engine); anything else goes through
+ * cudaMemcpyAsync. */
+int wb_copy_in(wb_ctx *c, void *dst, const void *src, size_t bytes)
+{
+  cudaPointerAttributes at;
+  const void *view = nullptr;
+  if (cudaPointerGetAttributes(&at, src) == cudaSuccess)
+  {
+    if (at.type == cudaMemoryTypeHost && at.devicePointer)
+      view = at.devicePointer;
+  }
+  else
+    cudaGetLastError();
+  if (view && bytes >= (1u << 20) && (uintptr_t)view % 16 == 0 && (uintptr_t)dst % 16 == 0)
+  {
+    const uint64_t n16 = bytes / 16;
+    const unsigned grid = (unsigned)c->sm_count * 8;
+    { pullKernel<<<grid, 256, 0, c->stream>>>((const uint4 *)view, (uint4 *)dst, n16); ++c->launches; }
+    WB_CUDA(c, cudaGetLastError());
+    if (bytes > n16 * 16)
+      WB_CUDA(c, cudaMemcpyAsync((uint8_t *)dst + n16 * 16, (const uint8_t *)src + n16 * 16, bytes - n16 * 16,
+                                 cudaMemcpyDefault, c->stream));
+    return 0;
+  }
+  WB_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
+  return 0;
+}
 
 int wb_exclusive_scan_u32(wb_ctx *c, const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total_dev)
 {
