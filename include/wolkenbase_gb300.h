@@ -405,6 +405,9 @@ typedef struct
   int autotune;          /* 1: on the first batch, time column densities, kernel
                             shapes and chunks on a sample and keep the fastest     */
   int pad;
+  uint64_t host_budget;  /* > 0: a job whose estimate is above hbm_budget runs alone
+                            with paging (wb_set_paging) up to this many host bytes,
+                            instead of failing with WB_ENOMEM                      */
 } wb_server_config;
 
 typedef struct

@@ -205,3 +205,70 @@ def test_writer_coordinate_paths_match_restatement(classifier, offset, unit):
     assert np.array_equal(recs, want_recs)
     for f, w in zip(files, want_files):
         assert (f["min"], f["max"], f["n_points"]) == (w["min"], w["max"], list(w["n_points"]))
+
+
+def test_device_resident_decode_and_writer_equal_host_path(classifier, tmp_path):
+    """Records, field arrays and output on the device give the host path's bytes."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    cloud = synth.density_tile(50_000, 71)
+    rec = _attributed_records(cloud, 3, 5)
+    n = cloud.n
+    cls = classifier.classify_cloud(cloud)
+    d = cloud.decoded()
+    o = wb.LasOutput(point_format=8, separate_classes=True, points_per_file=9000, unit=cloud.unit,
+                     min_cor=tuple(d.min(axis=0)), max_cor=tuple(d.max(axis=0)), scale=(0.001, 0.001, 0.001))
+    want_recs, want_files, _ = classifier.las_write_output(rec, 3, cloud.scale, cloud.offset, cloud.unit, o)
+    want_fields = classifier.las_decode(rec, 3, cloud.scale, cloud.offset, cloud.unit)
+    drec = torch.from_numpy(rec).cuda()
+    cs = wb.cloud_struct(drec.data_ptr(), n, rec.shape[1], cloud.scale, cloud.offset, cloud.unit, cloud.minc,
+                         cloud.maxc, device_resident=True)
+    tdt = {C.c_double: torch.float64, C.c_uint16: torch.int16, C.c_uint8: torch.uint8, C.c_int32: torch.int32}
+    fields = {name: torch.zeros(n, dtype=tdt[t], device="cuda") for name, t in _lib.LAS_POINT_FIELDS}
+    pts = _lib.wb_las_points(**{name: t.data_ptr() for name, t in fields.items()})
+    classifier._check(classifier.L.wb_las_decode(classifier.ctx, C.byref(cs), 3, C.byref(pts)))
+    for name, _ in _lib.LAS_POINT_FIELDS:
+        got = fields[name].cpu().numpy().view(want_fields[name].dtype)
+        assert np.array_equal(got, want_fields[name]), name
+    nd = classifier.info()["n_distinct"]
+    dout = torch.zeros((nd, wb.las_point_length(8)), dtype=torch.uint8, device="cuda")
+    files = (_lib.wb_las_file * 64)()
+    nf = C.c_int(0)
+    oc = o.c()
+    classifier._check(classifier.L.wb_las_write_output(classifier.ctx, C.byref(cs), 3, None, C.byref(oc),
+                                                       C.c_void_p(dout.data_ptr()), 1, files, 64, C.byref(nf)))
+    assert nf.value == len(want_files)
+    assert np.array_equal(dout.cpu().numpy(), want_recs)
+    for i, w in enumerate(want_files):
+        assert list(files[i].n_points) == w["n_points"] and files[i].first == w["first"]
+
+
+def test_writer_errors(classifier, tmp_path):
+    """Too little room for the files, and an unwritable destination."""
+    import ctypes as C
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    cloud = synth.density_tile(20_000, 72)
+    rec = _attributed_records(cloud, 1, 6)
+    classifier.classify_cloud(cloud)
+    d = cloud.decoded()
+    o = wb.LasOutput(point_format=1, separate_classes=True, points_per_file=1000, unit=1.0,
+                     min_cor=tuple(d.min(axis=0)), max_cor=tuple(d.max(axis=0)), scale=(0.001, 0.001, 0.001))
+    cs = wb.cloud_struct(rec, cloud.n, 28, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc)
+    out = np.zeros((classifier.info()["n_distinct"], 28), np.uint8)
+    files = (_lib.wb_las_file * 2)()
+    nf = C.c_int(0)
+    oc = o.c()
+    rc = classifier.L.wb_las_write_output(classifier.ctx, C.byref(cs), 1, None, C.byref(oc), out.ctypes.data, 0,
+                                          files, 2, C.byref(nf))
+    assert rc == _lib.WB_EINVAL and nf.value >= 20      # 20k points, 1000 per file
+    with pytest.raises(wb.WolkenbaseError) as e:
+        classifier.las_write_files(rec, 1, cloud.scale, cloud.offset, cloud.unit, o,
+                                   str(tmp_path / "missing" / "dir" / "cloud"))
+    assert e.value.code == _lib.WB_EIO
+    bad = wb.LasOutput(point_format=11, unit=1.0)
+    with pytest.raises(wb.WolkenbaseError) as e:
+        classifier.las_write_output(rec, 1, cloud.scale, cloud.offset, cloud.unit, bad)
+    assert e.value.code == _lib.WB_EINVAL

@@ -70,3 +70,25 @@ def test_pinned_inputs_are_read_in_place():
         assert np.array_equal(pcls.numpy(), want)
     finally:
         clf.close()
+
+
+def test_server_runs_over_budget_job_paged():
+    """With a host allowance, a job above the whole HBM budget runs alone with
+    paging instead of failing; the jobs around it are unaffected."""
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import synth
+    big = synth.density_tile(200_000, 907)
+    small = synth.density_tile(2_000, 908)
+    clf = wb.Classifier(0)
+    want_big, want_small = clf.classify_cloud(big), clf.classify_cloud(small)
+    clf.close()
+    srv = wb.Server(0, prep_slots=2, hbm_budget=80 << 20, host_budget=1 << 30)
+    try:
+        ids = [srv.submit(small), srv.submit(big), srv.submit(small)]
+        got = [srv.result(i) for i in ids]
+        for (cls, st), want in zip(got, [want_small, want_big, want_small]):
+            assert st["rc"] == 0 and np.array_equal(cls, want)
+        s = srv.stats()
+        assert s["completed"] == 3 and s["failed"] == 0 and s["peak_bytes"] <= 80 << 20
+    finally:
+        srv.close()

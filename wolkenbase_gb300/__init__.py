@@ -416,10 +416,10 @@ class Server:
     Classifier.classify_cloud on the same cloud."""
 
     def __init__(self, device=0, prep_slots=4, hbm_budget=0, flush=_lib.WB_FLUSH_EAGER, max_batch=0,
-                 shape=0, chunk=0, grid_points=0.0, autotune=False):
+                 shape=0, chunk=0, grid_points=0.0, autotune=False, host_budget=0):
         self.L = _lib.load()
         cfg = _lib.wb_server_config(device, prep_slots, hbm_budget, flush, max_batch, shape, chunk, grid_points,
-                                    1 if autotune else 0, 0)
+                                    1 if autotune else 0, 0, host_budget)
         self.s = self.L.wb_server_open(C.byref(cfg))
         if not self.s:
             raise WolkenbaseError(_lib.WB_ECUDA, self.L.wb_last_error(None).decode())

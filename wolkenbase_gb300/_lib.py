@@ -57,7 +57,7 @@ class wb_tuning(C.Structure):
 class wb_server_config(C.Structure):
     _fields_ = [("device", C.c_int), ("prep_slots", C.c_int), ("hbm_budget", C.c_uint64), ("flush", C.c_int),
                 ("max_batch", C.c_int), ("shape", C.c_int), ("chunk", C.c_int), ("grid_points", C.c_double),
-                ("autotune", C.c_int), ("pad", C.c_int)]
+                ("autotune", C.c_int), ("pad", C.c_int), ("host_budget", C.c_uint64)]
 
 
 class wb_job(C.Structure):

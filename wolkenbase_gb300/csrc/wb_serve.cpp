@@ -40,6 +40,7 @@ struct JobRec
   wb_job_status st{};
   wb_ctx *ctx = nullptr;
   uint64_t est = 0;
+  bool paged = false;   /* above the whole budget: runs alone with paging */
   cudaEvent_t ev = nullptr;
 };
 
@@ -190,11 +191,13 @@ void finish(wb_server *s, JobRec *j, int rc, const std::string &msg)
   }
 }
 
-int runPrep(JobRec *j, wb_ctx *c, double gridPoints)
+int runPrep(JobRec *j, wb_ctx *c, double gridPoints, uint64_t hostBudget)
 {
   c->budget = std::max<uint64_t>(c->used, j->est);
   c->grid_points = gridPoints;
-  int rc = wb_build_impl(c, &j->spec.cloud);
+  int rc = wb_set_paging(c, j->paged ? hostBudget : 0);
+  if (rc == 0)
+    rc = wb_build_impl(c, &j->spec.cloud);
   if (rc == 0)
     rc = wb_scan_impl(c, &j->spec.params);
   if (rc == 0)
@@ -227,7 +230,7 @@ void prepLoop(wb_server *s)
     s->stats.peak_bytes = std::max<uint64_t>(s->stats.peak_bytes, heldBytes(s));
     double gp = s->cfg.grid_points;
     lk.unlock();
-    int rc = runPrep(j, c, gp);
+    int rc = runPrep(j, c, gp, s->cfg.host_budget);
     std::string msg = rc ? c->err : std::string();
     lk.lock();
     s->prepBusy--;
@@ -344,6 +347,11 @@ void classifyLoop(wb_server *s)
     }
     if (rc == 0)
       wb_batch_collect(s->batch, ctxs.data(), k);
+    // a paged job's context gives its host memory back before it serves
+    // another job (whose buffers must not stay in host memory)
+    for (JobRec *j : batch)
+      if (j->paged)
+        wb_release_buffers(j->ctx);
     lk.lock();
     s->classifying--;
     s->graphLaunches += launches;
@@ -487,7 +495,14 @@ int64_t wb_submit(wb_server *s, const wb_job *job)
   j->st.tag = job->tag;
   j->st.n_points = job->cloud.n;
   j->st.t_submit = s->now();
-  if (j->est > s->budget)
+  if (j->est > s->budget && s->cfg.host_budget)
+  {
+    // runs alone, holding the whole HBM budget, with the rest in host memory
+    j->paged = true;
+    j->est = s->budget;
+    s->queue.push_back(j);
+  }
+  else if (j->est > s->budget)
   {
     // cannot be admitted even alone
     j->st.state = WB_JOB_FAILED;
