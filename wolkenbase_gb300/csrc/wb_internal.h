@@ -129,7 +129,18 @@ int wb_fail(wb_ctx *c, int code, const std::string &msg);
   } while (0)
 
 int wb_ensure(wb_ctx *c, DevBuf &b, size_t bytes);
-void wb_free_buf(wb_ctx *c, DevBuf &b);   /* stream-ordered free */
+void wb_free_buf(wb_ctx *c, DevBuf &b);   /* stream-ordered free (host buffers after a sync) */
+
+/* A scratch buffer of one call, freed when it leaves scope. */
+struct WbScratch
+{
+  wb_ctx *c;
+  DevBuf b;
+  explicit WbScratch(wb_ctx *ctx) : c(ctx) {}
+  WbScratch(const WbScratch &) = delete;
+  WbScratch &operator=(const WbScratch &) = delete;
+  ~WbScratch() { wb_free_buf(c, b); }
+};
 void wb_release_buffers(wb_ctx *c);       /* frees every buffer of c */
 void wb_mark(wb_ctx *c, const char *name);   /* profiling event after a stage */
 

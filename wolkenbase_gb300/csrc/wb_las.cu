@@ -111,14 +111,6 @@ __global__ void gatherRecordsKernel(const uint8_t *__restrict__ in, uint8_t *__r
   }
 }
 
-/* A scratch device buffer freed (stream-ordered) when it leaves scope. */
-struct TmpBuf
-{
-  wb_ctx *c;
-  DevBuf b;
-  ~TmpBuf() { wb_free_buf(c, b); }
-};
-
 unsigned gridOf(const wb_ctx *c, uint64_t n)
 {
   return (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
@@ -134,7 +126,7 @@ int wb_class_totals(wb_ctx *c, uint64_t *totals)
   if (c->stage < 3 || !c->clsFinal)
     return wb_fail(c, WB_ESTATE, "wb_class_totals: classify first");
   cudaSetDevice(c->device);
-  TmpBuf out{c, {}};
+  WbScratch out(c);
   int rc = wb_ensure(c, out.b, 256 * 8);
   if (rc)
     return rc;
@@ -160,7 +152,7 @@ int wb_duplicates(wb_ctx *c, uint64_t *n_dup, uint32_t *dup_of)
   if (!dup_of || !c->n)
     return 0;
   cudaSetDevice(c->device);
-  TmpBuf out{c, {}};
+  WbScratch out(c);
   int rc = wb_ensure(c, out.b, c->n * 4);
   if (rc)
     return rc;
@@ -187,7 +179,7 @@ int wb_las_write_classes(wb_ctx *c, void *records, uint64_t n, uint32_t stride, 
     return 0;
   cudaSetDevice(c->device);
   int rc;
-  TmpBuf rbuf{c, {}}, cbuf{c, {}};
+  WbScratch rbuf(c), cbuf(c);
   uint8_t *drec = (uint8_t *)records;
   const uint8_t *dcls = cls ? cls : c->clsFinal;
   if (!on_device)
@@ -229,7 +221,7 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
     return 0;
   cudaSetDevice(c->device);
   int rc;
-  TmpBuf rin{c, {}}, rout{c, {}}, hist{c, {}};
+  WbScratch rin(c), rout(c), hist(c);
   const uint8_t *din = (const uint8_t *)records;
   uint8_t *dout = (uint8_t *)out;
   if (!on_device)
@@ -347,7 +339,7 @@ extern "C" int wb_preview(wb_ctx *c, double x0, double y0, double side, int w, i
     return wb_fail(c, WB_EINVAL, "wb_preview: needs a positive z scale (elevation increasing in Z)");
   cudaSetDevice(c->device);
   const uint64_t npix = (uint64_t)w * h;
-  TmpBuf cnt{c, {}}, zl{c, {}}, zh{c, {}};
+  WbScratch cnt(c), zl(c), zh(c);
   int rc;
   if ((rc = wb_ensure(c, cnt.b, npix * 8)) || (rc = wb_ensure(c, zl.b, npix * 4)) || (rc = wb_ensure(c, zh.b, npix * 4)))
     return rc;

@@ -631,13 +631,6 @@ __global__ void storedTotals(uint64_t nd, const uint32_t *__restrict__ sidx, con
       atomicAdd(&totals[i], (unsigned long long)h[i]);
 }
 
-struct TmpBuf
-{
-  wb_ctx *c;
-  DevBuf b;
-  ~TmpBuf() { wb_free_buf(c, b); }
-};
-
 unsigned gridOf(const wb_ctx *c, uint64_t n, int per = 16)
 {
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + kBlock - 1) / kBlock, (uint64_t)c->sm_count * per));
@@ -907,7 +900,7 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
     a.d.scale[k] = cloud->scale[k];
   }
   a.d.unit = cloud->unit;
-  TmpBuf rin{c, {}}, fields{c, {}};
+  WbScratch rin(c), fields(c);
   const bool host = !cloud->device_resident;
   a.rec = (const uint8_t *)cloud->records;
   a.o = *out;
@@ -995,7 +988,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   const uint64_t n = c->n, nd = c->nd, L = c->n_leaves;
   const Layout Li = layoutOf(in_format), Lo = layoutOf(opt->point_format);
   int rc;
-  TmpBuf rin{c, {}}, cin{c, {}}, dout{c, {}}, tot{c, {}}, counts{c, {}}, bases{c, {}}, fileOf{c, {}}, stats{c, {}};
+  WbScratch rin(c), cin(c), dout(c), tot(c), counts(c), bases(c), fileOf(c), stats(c);
 
   WriteArgs a;
   a.stride = cloud->stride;
