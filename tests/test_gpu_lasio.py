@@ -272,3 +272,53 @@ def test_writer_errors(classifier, tmp_path):
     with pytest.raises(wb.WolkenbaseError) as e:
         classifier.las_write_output(rec, 1, cloud.scale, cloud.offset, cloud.unit, bad)
     assert e.value.code == _lib.WB_EINVAL
+
+
+def test_written_files_census(classifier, tmp_path):
+    """censusPoints (testpattern.cpp:56-123) on the files: with the GPS time of
+    every record set to its index, the files hold every surviving record once
+    and no overwritten duplicate."""
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import synth
+    base = synth.density_tile(40_000, 73)
+    rng = np.random.default_rng(9)
+    dup = rng.choice(base.n, 1500, replace=False)
+    xyz = np.concatenate([base.xyz, base.xyz[dup]])
+    cloud = synth.Cloud(xyz, base.scale, base.offset, base.unit, base.minc, base.maxc)
+    rec = _attributed_records(cloud, 1, 10)
+    rec[:, 20:28] = np.arange(cloud.n, dtype="<f8").view(np.uint8).reshape(-1, 8)
+    classifier.classify_cloud(cloud)
+    survivors = np.sort(classifier.store_order().astype(np.int64))
+    d = cloud.decoded()
+    o = wb.LasOutput(point_format=1, separate_classes=True, points_per_file=6000, unit=1.0,
+                     min_cor=tuple(d.min(axis=0)), max_cor=tuple(d.max(axis=0)), scale=(0.001, 0.001, 0.001))
+    written = classifier.las_write_files(rec, 1, cloud.scale, cloud.offset, cloud.unit, o, str(tmp_path / "c"))
+    ids = []
+    for w in written:
+        data = np.fromfile(w["name"], np.uint8)[375:].reshape(-1, 28)
+        ids.append(np.ascontiguousarray(data[:, 20:28]).view("<f8").ravel())
+        assert w["n_points"][0] == len(data)
+    ids = np.sort(np.concatenate(ids)).astype(np.int64)
+    assert np.array_equal(ids, survivors)
+    assert len(ids) <= cloud.n - 1500                    # every appended copy overwrote its original
+    assert not np.isin(dup, ids).any()
+
+
+def test_wrong_side_pointers_are_refused(classifier):
+    """A host array passed as a device pointer is refused before any kernel
+    reads it."""
+    import ctypes as C
+    import wolkenbase_gb300 as wb
+    from wolkenbase_gb300 import _lib, synth
+    cloud = synth.density_tile(5_000, 74)
+    xyz = np.ascontiguousarray(cloud.xyz, np.int32)
+    cs = wb.cloud_struct(xyz, cloud.n, 12, cloud.scale, cloud.offset, cloud.unit, cloud.minc, cloud.maxc,
+                         device_resident=True)
+    assert classifier.L.wb_octree_build(classifier.ctx, C.byref(cs)) == _lib.WB_EINVAL
+    cls = np.zeros(cloud.n, np.uint8)
+    classifier.classify_cloud(cloud)
+    rec = np.zeros((cloud.n, 28), np.uint8)
+    assert classifier.L.wb_las_write_classes(classifier.ctx, rec.ctypes.data, cloud.n, 28, 1, 1,
+                                             cls.ctypes.data) == _lib.WB_EINVAL
+    p = wb.Params().c()
+    assert classifier.L.wb_classify(classifier.ctx, C.byref(p), cls.ctypes.data, 1) == _lib.WB_EINVAL

@@ -555,6 +555,8 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
     keyFixedPoint(g, mn[k], mx[k], k, a);
 
   int rc;
+  if (cl->device_resident && n && !wb_device_accessible(cl->records))
+    return wb_fail(c, WB_EINVAL, "wb_octree_build: device_resident records must be device memory");
   if (cl->device_resident)
     a.rec = (const uint8_t *)cl->records;
   else

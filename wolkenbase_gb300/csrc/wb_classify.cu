@@ -1042,6 +1042,8 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
     return wb_fail(c, WB_EINVAL, "wb_classify: cls must not be NULL");
   if (!(p->max_slope > 0))
     return wb_fail(c, WB_EINVAL, "wb_classify: max_slope must be > 0");
+  if (onDevice && c->n && !wb_device_accessible(cls))
+    return wb_fail(c, WB_EINVAL, "wb_classify: device class bytes must be device memory");
   int rc;
   uint64_t nd = c->nd, n = c->n;
   if ((rc = wb_ensure(c, c->label, nd + 64)) || (rc = wb_ensure(c, c->angleT, (511 + 512 + 512) * 8)) ||

@@ -153,6 +153,7 @@ void wb_flowsnake_order(int idx, std::vector<int32_t> &ex, std::vector<int32_t> 
 /* primitives (wb_prims.cu) */
 int wb_exclusive_scan_u32(wb_ctx *c, const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total_dev);
 int wb_copy_in(wb_ctx *c, void *dst, const void *src, size_t bytes);   /* caller's host buffer -> device */
+bool wb_device_accessible(const void *p);   /* device, managed or device-mapped host memory */
 int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *keysAlt, uint32_t *valsAlt,
                         uint64_t n, int beginBit, int endBit);
 

@@ -177,6 +177,8 @@ int wb_las_write_classes(wb_ctx *c, void *records, uint64_t n, uint32_t stride, 
     return wb_fail(c, WB_ESTATE, "wb_las_write_classes: no class bytes of a classified cloud of n records");
   if (!n)
     return 0;
+  if (on_device && (!wb_device_accessible(records) || (cls && !wb_device_accessible(cls))))
+    return wb_fail(c, WB_EINVAL, "wb_las_write_classes: on_device needs device pointers");
   cudaSetDevice(c->device);
   int rc;
   WbScratch rbuf(c), cbuf(c);
@@ -219,6 +221,8 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
   memset(offsets, 0, 257 * sizeof(uint64_t));
   if (!n)
     return 0;
+  if (on_device && (!wb_device_accessible(records) || !wb_device_accessible(out)))
+    return wb_fail(c, WB_EINVAL, "wb_las_split_by_class: on_device needs device pointers");
   cudaSetDevice(c->device);
   int rc;
   WbScratch rin(c), rout(c), hist(c);

@@ -888,6 +888,8 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
   const uint64_t n = cloud->n;
   if (!n)
     return 0;
+  if (cloud->device_resident && !wb_device_accessible(cloud->records))
+    return wb_fail(c, WB_EINVAL, "wb_las_decode: device_resident records must be device memory");
   cudaSetDevice(c->device);
   int rc;
   DecodeArgs a;
@@ -984,6 +986,13 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
     return wb_fail(c, WB_ESTATE, "wb_las_write_output: build the octree of this cloud first");
   if (!cls && (c->stage < 3 || !c->clsFinal))
     return wb_fail(c, WB_ESTATE, "wb_las_write_output: no class bytes (classify first or pass them)");
+  if (c->nd && !out)
+    return wb_fail(c, WB_EINVAL, "wb_las_write_output: no output buffer");
+  if (c->nd && out_on_device && !wb_device_accessible(out))
+    return wb_fail(c, WB_EINVAL, "wb_las_write_output: out_on_device needs a device pointer");
+  if (cloud->device_resident && c->n &&
+      (!wb_device_accessible(cloud->records) || (cls && !wb_device_accessible(cls))))
+    return wb_fail(c, WB_EINVAL, "wb_las_write_output: device_resident records (and class bytes) must be device memory");
   cudaSetDevice(c->device);
   const uint64_t n = c->n, nd = c->nd, L = c->n_leaves;
   const Layout Li = layoutOf(in_format), Lo = layoutOf(opt->point_format);

@@ -265,6 +265,23 @@ int wb_copy_in(wb_ctx *c, void *dst, const void *src, size_t bytes)
   return 0;
 }
 
+/* Whether kernels can dereference p: device or managed memory, or host memory
+ * mapped for the device.  A pageable host pointer passed where the API wants
+ * a device pointer is refused with WB_EINVAL instead of reaching a kernel. */
+bool wb_device_accessible(const void *p)
+{
+  if (!p)
+    return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
+         (at.type == cudaMemoryTypeHost && at.devicePointer == p);
+}
+
 int wb_exclusive_scan_u32(wb_ctx *c, const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total_dev)
 {
   if (n == 0)
