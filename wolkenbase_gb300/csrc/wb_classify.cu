@@ -791,37 +791,31 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       const uint32_t e = (uint32_t)r1.z;
       const int32_t zl = envZlim(box, r1);
       bool got = false;
-      // the lane's test of candidate c against its own point
-      auto testOne = [&](const int4 &c, uint32_t &u) -> bool {
+      // whether candidate c is inside the lane's hyperboloid; dx, dy its
+      // offset for the direction
+      auto memberOf = [&](const int4 &c, float &dx, float &dy) -> bool {
         const int32_t dxi = c.x - me.x, dyi = c.y - me.y;
-        // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
-        if (dxi == 0 && dyi == 0)
-          return false;
-        const float dx = (float)dxi * sx, dy = (float)dyi * sy;
+        dx = (float)dxi * sx;
+        dy = (float)dyi * sy;
         const uint32_t gp = (uint32_t)c.w;
-        bool in;
-        if (gp & kStray)
-          in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
-        else
+        const float dzm = (float)(me.z - c.z) * sz;
+        const float zd = dzm + czp;
+        const float r2 = s2 * (dx * dx + dy * dy);
+        const float f = zd * zd - r2 - por2;
+        const float tol = 1e-5f * (zd * zd + r2 + por2) + 1e-12f;
+        const float ztol = 1e-5f * (fabsf(dzm) + fabsf(czp)) + 1e-12f;
+        const bool sureIn = zd > ztol && f > tol, sureOut = zd < -ztol || f < -tol;
+        bool in = sureIn;
+        // points outside the root cube, and the band where FP32 cannot tell
+        if ((gp & kStray) || (!sureIn && !sureOut))
         {
-          float dzm = (float)(me.z - c.z) * sz;
-          float zd = dzm + czp;
-          float r2 = s2 * (dx * dx + dy * dy);
-          float f = zd * zd - r2 - por2;
-          float tol = 1e-5f * (zd * zd + r2 + por2) + 1e-12f;
-          float ztol = 1e-5f * (fabsf(dzm) + fabsf(czp)) + 1e-12f;
-          if (zd > ztol && f > tol)
-            in = true;
-          else if (zd < -ztol || f < -tol)
-            in = false;
-          else if (a.fp32Only)
+          if (!(gp & kStray) && a.fp32Only)
             in = zd > 0 && f > 0;
           else
             in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
         }
-        if (in)
-          u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
-        return in;
+        // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
+        return in && (dxi != 0 || dyi != 0);
       };
       auto addDir = [&](uint32_t u) {
         const int bin = (int)(u >> 28);
@@ -860,6 +854,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         sm.cand[lane] = q;
         __syncwarp();
         // two candidates per step: independent work for the scheduler
+        // Every lane runs the tests (a decided lane's results are dropped), so
+        // the warp does not diverge on them; the directions are formed only
+        // when some lane has a candidate inside.
         while (lm)
         {
           const int k1 = __ffs(lm) - 1;
@@ -867,15 +864,18 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           const int k2 = lm ? __ffs(lm) - 1 : -1;
           if (k2 >= 0)
             lm &= lm - 1;
-          if (done)
-            continue;
-          uint32_t u1 = 0, u2 = 0;
-          const bool in1 = testOne(sm.cand[k1], u1);
-          const bool in2 = k2 >= 0 && testOne(sm.cand[k2], u2);
-          if (in1)
-            addDir(u1);
-          if (in2)
-            addDir(u2);
+          float dx1, dy1, dx2 = 0.f, dy2 = 0.f;
+          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done;
+          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done;
+          if (__any_sync(0xffffffffu, in1 || in2))
+          {
+            const uint32_t u1 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy1, dx1)) & 0x7fffffffu;
+            const uint32_t u2 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy2, dx2)) & 0x7fffffffu;
+            if (in1)
+              addDir(u1);
+            if (in2)
+              addDir(u2);
+          }
         }
         __syncwarp();
       }
