@@ -205,6 +205,8 @@ void wb_close(wb_ctx *c)
     cudaEventDestroy(e);
   wb_release_buffers(c);
   cudaStreamSynchronize(c->stream);
+  if (c->hostStage)
+    cudaFreeHost(c->hostStage);
   wb_batch_destroy(c->batch);
   if (c->own_stream && c->stream)
     cudaStreamDestroy(c->stream);

@@ -91,6 +91,8 @@ struct wb_ctx
   double grid_bounds[4] = {0, 0, 0, 0};   /* x0, y0, x1, y1 the column grid spans */
   DevBuf flowCache;
   DevBuf lasAngles;                 /* scan-angle tables of the LAS decode and writer */
+  void *hostStage = nullptr;        /* pinned staging for per-block tables (grow-only) */
+  size_t hostStageCap = 0;
   std::vector<int32_t> flowHostEx, flowHostEy;   /* cached flowsnake order for snake_idx */
   int flowIdxCached = -1;
   int lookupX0 = 0, lookupY0 = 0, lookupW = 0, lookupH = 0;

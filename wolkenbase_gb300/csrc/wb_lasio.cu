@@ -1090,21 +1090,36 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   a.nFiles = (uint32_t)P.nFiles;
 
   // stored points per (block, set)
-  std::vector<uint32_t> cnt(L * S);
+  // per (block, set) counts, first records and files go through one pinned
+  // host buffer of the context (16 bytes per entry)
+  const size_t stageBytes = L * S * 16 + 64;
+  if (c->hostStageCap < stageBytes)
+  {
+    WB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->hostStage)
+      cudaFreeHost(c->hostStage);
+    c->hostStage = nullptr;
+    c->hostStageCap = 0;
+    WB_CUDA(c, cudaHostAlloc(&c->hostStage, stageBytes, cudaHostAllocDefault));
+    c->hostStageCap = stageBytes;
+  }
+  uint64_t *base = (uint64_t *)c->hostStage;
+  uint32_t *cnt = (uint32_t *)(base + L * S), *fof = cnt + L * S;
   if (L)
   {
     if ((rc = wb_ensure(c, counts.b, L * S * 4)))
       return rc;
     WB_CUDA(c, cudaMemsetAsync(counts.b.p, 0, L * S * 4, c->stream));
     { setCountKernel<<<gridOf(c, L * 32, 8), kBlock, 0, c->stream>>>(a, (uint32_t *)counts.b.p); ++c->launches; }
-    WB_CUDA(c, cudaMemcpyAsync(cnt.data(), counts.b.p, L * S * 4, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(cnt, counts.b.p, L * S * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
   }
+  memset(base, 0, L * S * 8);
+  memset(fof, 0, L * S * 4);
 
   // writeFiles: at each block, each set's points go to its file holding the
   // fewest points, the first of them on a tie (cloudoutput.cpp:196-209)
-  std::vector<uint64_t> fileCount(P.nFiles, 0), base(L * S, 0);
-  std::vector<uint32_t> fof(L * S, 0);
+  std::vector<uint64_t> fileCount(P.nFiles, 0);
   typedef std::pair<uint64_t, int> Entry;
   for (uint32_t s = 0; s < S; s++)
   {
@@ -1161,8 +1176,8 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   {
     if ((rc = wb_ensure(c, bases.b, L * S * 8)) || (rc = wb_ensure(c, fileOf.b, L * S * 4)))
       return rc;
-    WB_CUDA(c, cudaMemcpyAsync(bases.b.p, base.data(), L * S * 8, cudaMemcpyDefault, c->stream));
-    WB_CUDA(c, cudaMemcpyAsync(fileOf.b.p, fof.data(), L * S * 4, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(bases.b.p, base, L * S * 8, cudaMemcpyDefault, c->stream));
+    WB_CUDA(c, cudaMemcpyAsync(fileOf.b.p, fof, L * S * 4, cudaMemcpyDefault, c->stream));
     a.base = (unsigned long long *)bases.b.p;
     a.fileOf = (const uint32_t *)fileOf.b.p;
     const size_t slots = 2 * (size_t)kBlock * kSlotWords * 4;
