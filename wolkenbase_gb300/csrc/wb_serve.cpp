@@ -232,6 +232,8 @@ void prepLoop(wb_server *s)
     lk.unlock();
     int rc = runPrep(j, c, gp, s->cfg.host_budget);
     std::string msg = rc ? c->err : std::string();
+    if (rc && j->paged)
+      wb_release_buffers(c);   // no host-memory buffers left behind for the next job
     lk.lock();
     s->prepBusy--;
     s->stats.peak_bytes = std::max<uint64_t>(s->stats.peak_bytes, heldBytes(s));
