@@ -29,6 +29,11 @@
  *                                     as CloudOutput::openFiles opens a file
  *                                     (openWrite, setUnit, setScale, setVersion
  *                                     1.4, setPointFormat), then writeHeader
+ *   wb_ref preview IN OUT X0 Y0 SIDE W H
+ *                                     the octree built as in pipeline mode, then
+ *                                     OctStore::countPointsIn and hiLoPointsIn of
+ *                                     the Column of every pixel (uint64 count,
+ *                                     double lo, double hi per pixel, row-major)
  *   wb_ref combine N S0x S0y S0z O0x O0y O0z ...   combineScales per axis
  *   wb_ref join F0 F1 ...             joinPointFormat
  */
@@ -40,6 +45,7 @@
 #include <chrono>
 #include <string>
 #include <vector>
+#include <array>
 #include <fstream>
 #include <iostream>
 #include <unistd.h>
@@ -421,6 +427,57 @@ static int runLasRW(int argc, char **argv)
   return 0;
 }
 
+static int runPreview(int argc, char **argv)
+{
+  if (argc < 9)
+    die("preview IN OUT X0 Y0 SIDE W H");
+  FILE *f = fopen(argv[2], "rb");
+  if (!f) die("cannot open input");
+  WbxyzHeader h;
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, "WBXYZ1", 6)) die("bad header");
+  vector<int32_t> q(3 * h.n);
+  if (h.n && fread(q.data(), 12, h.n, f) != h.n) die("short input");
+  fclose(f);
+  const double x0 = atof(argv[4]), y0 = atof(argv[5]), side = atof(argv[6]);
+  const int w = atoi(argv[7]), hgt = atoi(argv[8]);
+  char tmpl[] = "/tmp/wbrefXXXXXX";
+  char *dir = mkdtemp(tmpl);
+  if (!dir) die("mkdtemp");
+  startSerialStore(dir);
+  vector<xyz> limits;
+  limits.push_back(xyz(h.minc[0] * h.unit, h.minc[1] * h.unit, h.minc[2] * h.unit));
+  limits.push_back(xyz(h.maxc[0] * h.unit, h.maxc[1] * h.unit, h.maxc[2] * h.unit));
+  octRoot.sizeFit(limits);
+  for (uint64_t i = 0; i < h.n; i++)
+  {
+    LasPoint p;
+    p.location = xyz(h.offset[0] + h.scale[0] * q[3 * i], h.offset[1] + h.scale[1] * q[3 * i + 1],
+                     h.offset[2] + h.scale[2] * q[3 * i + 2]) * h.unit;
+    p.returnNum = 1;
+    p.nReturns = 1;
+    p.gpsTime = (double)i;
+    octStore.put(p);
+    drainBuffer();
+  }
+  FILE *o = fopen(argv[3], "wb");
+  if (!o) die("cannot open output");
+  for (int j = 0; j < hgt; j++)
+    for (int i = 0; i < w; i++)
+    {
+      Column col(xy(x0 + i * side, y0 + j * side), side);
+      uint64_t cnt = octStore.countPointsIn(col);
+      array<double, 2> hl = octStore.hiLoPointsIn(col);
+      octStore.disown();
+      fwrite(&cnt, 8, 1, o);
+      fwrite(&hl[0], 8, 1, o);
+      fwrite(&hl[1], 8, 1, o);
+    }
+  fclose(o);
+  string cmd = string("rm -rf ") + dir;
+  if (system(cmd.c_str())) {}
+  return 0;
+}
+
 static int runCombine(int argc, char **argv)
 {
   if (argc < 3) die("combine N S O ...");
@@ -459,6 +516,7 @@ int main(int argc, char **argv)
   if (mode == "flowsnake") return runFlowsnake(argc, argv);
   if (mode == "lsq") return runLsq(argc, argv);
   if (mode == "lasrw") return runLasRW(argc, argv);
+  if (mode == "preview") return runPreview(argc, argv);
   if (mode == "combine") return runCombine(argc, argv);
   if (mode == "join") return runJoin(argc, argv);
   die("unknown mode");

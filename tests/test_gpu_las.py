@@ -84,3 +84,22 @@ def test_preview_matches_restatement(classifier, side):
     assert np.array_equal(cnt, rc)
     assert np.array_equal(lo, rl) and np.array_equal(hi, rh)
     assert cnt.sum() > 0 and (cnt == 0).any()
+
+
+def test_preview_matches_reference_goldens(classifier):
+    """wb_preview against the reference's own countPointsIn / hiLoPointsIn
+    (tests/golden/preview.npz, written by tests/golden/make_preview_golden.py)."""
+    import os
+    from conftest import ROOT
+    from wolkenbase_gb300 import synth
+    g = np.load(os.path.join(ROOT, "tests", "golden", "preview.npz"))
+    for name in g["cases"]:
+        c = np.load(os.path.join(ROOT, "tests", "golden", str(name) + ".npz"))
+        cloud = synth.Cloud(c["xyz"].astype(np.int32), tuple(c["scale"]), tuple(c["offset"]), float(c["unit"]),
+                            tuple(c["minc"]), tuple(c["maxc"]))
+        classifier.build(cloud)
+        for k in range(3):
+            x0, y0, side, w, h = g[f"{name}_{k}_view"]
+            cnt, lo, hi = classifier.preview(float(x0), float(y0), float(side), int(w), int(h))
+            assert np.array_equal(cnt, g[f"{name}_{k}_count"]), (name, k)
+            assert np.array_equal(lo, g[f"{name}_{k}_lo"]) and np.array_equal(hi, g[f"{name}_{k}_hi"]), (name, k)

@@ -1,6 +1,8 @@
-"""The LAS record restatement (oracle/las_oracle.py) against the reference's own
-readPoint / writePoint / writeHeader / combineScales / joinPointFormat outputs
-(tests/golden/lasio.npz, written by tests/golden/make_las_golden.py), and the
+"""The restatements of the steps either side of the path (oracle/las_oracle.py)
+against the reference's own outputs: readPoint / writePoint / writeHeader /
+combineScales / joinPointFormat (tests/golden/lasio.npz, written by
+tests/golden/make_las_golden.py) and the preview queries countPointsIn /
+hiLoPointsIn (tests/golden/preview.npz, make_preview_golden.py); and the
 library's host-side writer pieces (header bytes, file names, scale
 combination, format join) against the same fixtures.  No GPU."""
 import os
@@ -173,3 +175,25 @@ def test_library_host_pieces_match_reference(golden):
     # manygcd that would never return (a zero offset beside a nonzero one) is refused
     with pytest.raises(wb.WolkenbaseError):
         wb.combine_scales([[0.01] * 3, [0.001] * 3], [[500000.0] * 3, [0.0] * 3])
+
+
+def _golden_cloud(name):
+    from wolkenbase_gb300 import synth
+    c = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    return synth.Cloud(c["xyz"].astype(np.int32), tuple(c["scale"]), tuple(c["offset"]), float(c["unit"]),
+                       tuple(c["minc"]), tuple(c["maxc"]))
+
+
+def test_preview_matches_reference():
+    """OctStore::countPointsIn / hiLoPointsIn of every pixel Column, as the
+    reference's own octree answered them (tests/golden/preview.npz)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "preview.npz"))
+    for name in g["cases"]:
+        cloud = _golden_cloud(str(name))
+        stored = np.unique(LO.survivors(cloud.xyz))
+        pts = cloud.decoded()[stored]
+        for k in range(3):
+            x0, y0, side, w, h = g[f"{name}_{k}_view"]
+            cnt, lo, hi = LO.preview(pts, x0, y0, side, int(w), int(h))
+            assert np.array_equal(cnt, g[f"{name}_{k}_count"]), (name, k)
+            assert np.array_equal(lo, g[f"{name}_{k}_lo"]) and np.array_equal(hi, g[f"{name}_{k}_hi"]), (name, k)
