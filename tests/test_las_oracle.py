@@ -197,3 +197,19 @@ def test_preview_matches_reference():
             cnt, lo, hi = LO.preview(pts, x0, y0, side, int(w), int(h))
             assert np.array_equal(cnt, g[f"{name}_{k}_count"]), (name, k)
             assert np.array_equal(lo, g[f"{name}_{k}_lo"]) and np.array_equal(hi, g[f"{name}_{k}_hi"]), (name, k)
+
+
+@pytest.mark.parametrize("name", ["dups5k", "tile20k", "split"])
+def test_duplicates_and_class_totals_match_reference(name):
+    """OctBuffer::put's overwrites and countClasses, as the reference's own run
+    recorded them in the golden fixtures: a record has no block exactly when a
+    later identical point replaced it, and the class totals count the stored
+    points."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    surv = LO.survivors(g["xyz"])
+    replaced = surv != np.arange(len(surv))
+    assert np.array_equal(g["block"] < 0, replaced)
+    stored = np.flatnonzero(~replaced)
+    if int(g["phases"]) >= 3:
+        want = np.bincount(g["cls"][g["block"] >= 0].astype(np.int64), minlength=256)
+        assert np.array_equal(LO.class_totals(stored, g["cls"]).astype(np.int64), want)
