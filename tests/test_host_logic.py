@@ -1,0 +1,102 @@
+"""Host-side logic that needs no GPU: the precision report's arithmetic (on a
+stand-in context), the synthetic workloads' determinism, the LAS output
+settings as the C struct sees them, and the bench's sampling helpers."""
+import numpy as np
+import pytest
+
+
+class _FakeContext:
+    """Answers the calls precision.compare makes, with fixed results per mode."""
+
+    def __init__(self, results, spacing=1.2):
+        self.results = results
+        self.mode = 0
+        self.spacing = spacing
+
+    def set_precision(self, mode):
+        self.mode = mode
+
+    def build(self, cloud):
+        pass
+
+    def synchronize(self):
+        pass
+
+    def scan(self, params=None):
+        pass
+
+    def classify(self, params=None):
+        return self.results[self.mode][0]
+
+    def planes(self):
+        return self.results[self.mode][1]
+
+    def tiles(self):
+        return self.results[self.mode][2]
+
+    def info(self):
+        return {"spacing": self.spacing}
+
+
+def _tiles(n_points, height, h, flags):
+    from wolkenbase_gb300 import TILE_DTYPE
+    t = np.zeros(len(n_points), TILE_DTYPE)
+    t["n_points"] = n_points
+    t["height"] = height
+    t["hyperboloid_size"] = h
+    t["tree_flags"] = flags
+    return t
+
+
+def test_precision_report_arithmetic():
+    from wolkenbase_gb300 import _lib, precision, synth
+    cls64 = np.array([1, 2, 2, 1, 2], np.uint8)
+    cls32 = np.array([1, 2, 1, 1, 2], np.uint8)
+    p64 = np.array([[0.1, 0.2, 5.0], [0.0, 0.0, 1.0], [0.3, 0.1, 2.0]])
+    p32 = p64 + np.array([[3e-7, -4e-7, 1e-6], [0, 0, 0], [0, 0, 0]])
+    t64 = _tiles([10, 2, 7], [0.5, 0.1, 0.8], [0.4, 0.0, 1.0], [0, 0, 1])
+    t32 = _tiles([10, 2, 7], [0.5, 0.1, 0.8], [0.41, 0.0, 1.0], [0, 1, 1])
+    clf = _FakeContext({_lib.WB_PRECISION_EXACT: (cls64, p64, t64), _lib.WB_PRECISION_FP32: (cls32, p32, t32)})
+    cloud = synth.Cloud(np.zeros((5, 3), np.int32), (0.001,) * 3, (0.0,) * 3, 1.0, (0, 0, 0), (1, 1, 1))
+    r = precision.compare(clf, cloud)
+    assert r["points"] == 5 and r["flips"] == 1 and r["agreement"] == pytest.approx(0.8)
+    assert r["tiles_compared"] == 2                      # the 2-point tile is not a fit
+    assert r["slope_err"] == pytest.approx(5e-7)
+    R = 1.2 * 41.0 / 71.0
+    bound = 3e-7 * R + 4e-7 * R + 1e-6
+    assert r["residual_abs_err_m"] == pytest.approx(bound)
+    assert r["residual_err"] == pytest.approx(bound / 0.25)
+    assert r["h_rel_err"] == pytest.approx(0.025)
+    assert r["tree_flag_changes"] == 1
+
+
+def test_synthetic_workloads_are_seeded():
+    from wolkenbase_gb300 import synth
+    a, b, c = synth.density_tile(3000, 7), synth.density_tile(3000, 7), synth.density_tile(3000, 8)
+    assert np.array_equal(a.xyz, b.xyz) and not np.array_equal(a.xyz, c.xyz)
+    d = a.decoded()
+    assert (d.min(axis=0) >= np.array(a.minc) * a.unit - 1e-9).all()
+    assert (d.max(axis=0) <= np.array(a.maxc) * a.unit + 1e-9).all()
+
+
+def test_las_output_settings_reach_the_struct():
+    import wolkenbase_gb300 as wb
+    o = wb.LasOutput(point_format=7, separate_classes=False, n_input_files=3, points_per_file=12345,
+                     unit=0.3048, min_cor=(1, 2, 3), max_cor=(4, 5, 6), scale=(0.01, 0.02, 0.03),
+                     creation_day=45, creation_year=2026, software="tool 1")
+    c = o.c()
+    assert (c.point_format, c.separate_classes, c.n_input_files, c.points_per_file) == (7, 0, 3, 12345)
+    assert (c.creation_day, c.creation_year, c.software) == (45, 2026, b"tool 1")
+    assert tuple(c.min_cor) == (1, 2, 3) and tuple(c.max_cor) == (4, 5, 6) and tuple(c.scale) == (0.01, 0.02, 0.03)
+    assert wb.LasOutput().c().software is None
+
+
+def test_bench_crop_and_single_rank_max():
+    import bench
+    from wolkenbase_gb300 import synth
+    cloud = synth.density_tile(20_000, 3)
+    sub, side = bench.crop(cloud, 5_000)
+    d = sub.decoded()
+    assert 0 < sub.n < cloud.n
+    assert (d[:, 0].max() - d[:, 0].min()) <= side + 1e-6 and (d[:, 1].max() - d[:, 1].min()) <= side + 1e-6
+    assert bench.max_over_ranks(3.5, "cpu") == 3.5
