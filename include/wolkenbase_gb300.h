@@ -158,7 +158,10 @@ int wb_octree_find_block(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *le
  * with WB_EINVAL.  All calls share the one array: calls that overlap on the
  * GPU (two host threads, or two contexts on one device) race and must be
  * serialised by the caller.  Every result slot is written by each call, so
- * nothing left over from an earlier call is read.  Synchronous. */
+ * nothing left over from an earlier call is read.  Like every context on
+ * that device, the looked-up address does not survive cudaDeviceReset of the
+ * device: a process that resets a device must not use this library on it
+ * again.  Synchronous. */
 #define WB_FIND_BLOCK_STATIC_MAX 65536
 int wb_octree_find_block_static(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *leaf);
 

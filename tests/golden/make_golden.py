@@ -3,9 +3,9 @@
 Runs oracle/_ref/wb_ref -- the reference's octree / scan / classify / angle /
 flowsnake / least-squares sources compiled unchanged by `make -C oracle ref`
 -- on small seeded inputs and stores inputs and outputs as compressed .npz
-files.  Needs the reference source tree (REF env var, default the path the
-Makefile uses) and runs on the development machine only; the tests read the
-committed .npz files.
+files.  Needs the reference source tree (the REF environment variable, passed
+on to `make -C oracle ref`) and runs on the development machine only; the
+tests read the committed .npz files.
 
     python tests/golden/make_golden.py
 """

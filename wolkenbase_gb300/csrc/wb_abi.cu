@@ -172,7 +172,8 @@ wb_ctx *wb_open(int device, size_t hbm_budget)
     wb_fail(nullptr, WB_EINVAL, "wb_open: bad device ordinal");
     return nullptr;
   }
-  if (cudaSetDevice(device) != cudaSuccess)
+  WbDeviceGuard deviceGuard(device);
+  if (!deviceGuard.ok)
   {
     wb_fail(nullptr, WB_ECUDA, "wb_open: cudaSetDevice failed");
     return nullptr;
@@ -198,7 +199,7 @@ void wb_close(wb_ctx *c)
 {
   if (!c)
     return;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stream)
     cudaStreamSynchronize(c->stream);
   for (cudaEvent_t e : c->events)
@@ -222,6 +223,7 @@ int wb_set_stream(wb_ctx *c, void *s)
 {
   if (!c)
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stream)
     cudaStreamSynchronize(c->stream);
   if (c->own_stream && c->stream)
@@ -243,6 +245,7 @@ int wb_synchronize(wb_ctx *c)
 {
   if (!c)
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -314,7 +317,7 @@ int wb_octree_build(wb_ctx *c, const wb_cloud *cloud)
 {
   if (!c || !cloud)
     return WB_EINVAL;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   beginRun(c);
   int rc = wb_build_impl(c, cloud);
   endRun(c);
@@ -354,6 +357,7 @@ int wb_octree_leaves(wb_ctx *c, double *cs, uint32_t *first, uint32_t *count)
 {
   if (!c)
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stage < 1)
     return wb_fail(c, WB_ESTATE, "wb_octree_leaves: no octree built");
   uint64_t L = c->n_leaves;
@@ -394,6 +398,7 @@ int wb_octree_point_leaf(wb_ctx *c, uint32_t *out)
 {
   if (!c || (!out && c->n))
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stage < 1)
     return wb_fail(c, WB_ESTATE, "wb_octree_point_leaf: no octree built");
   if (c->n)
@@ -408,6 +413,7 @@ int wb_octree_store_order(wb_ctx *c, uint32_t *out)
 {
   if (!c || (!out && c->nd))
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stage < 1)
     return wb_fail(c, WB_ESTATE, "wb_octree_store_order: no octree built");
   if (c->nd)
@@ -422,6 +428,7 @@ int wb_octree_find_block(wb_ctx *c, const double *xyz, uint64_t m, int64_t *leaf
 {
   if (!c || (m && (!xyz || !leaf)))
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stage < 1)
     return wb_fail(c, WB_ESTATE, "wb_octree_find_block: no octree built");
   return wb_find_block_impl(c, xyz, m, leaf);
@@ -431,7 +438,7 @@ int wb_scan_tiles(wb_ctx *c, const wb_params *p)
 {
   if (!c || !p)
     return WB_EINVAL;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   beginRun(c);
   int rc = wb_scan_impl(c, p);
   endRun(c);
@@ -442,6 +449,7 @@ int wb_tiles(wb_ctx *c, wb_tile *out, uint64_t capacity, uint64_t *count)
 {
   if (!c)
     return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
   if (c->stage < 2)
     return wb_fail(c, WB_ESTATE, "wb_tiles: scan the tiles first");
   uint64_t T = c->n_tiles;
@@ -475,7 +483,7 @@ int wb_classify(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
 {
   if (!c || !p)
     return WB_EINVAL;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   beginRun(c);
   int rc = wb_classify_impl(c, p, cls, onDevice);
   if (rc == 0 && !onDevice)
@@ -522,7 +530,7 @@ int wb_tile_planes(wb_ctx *c, double *abc, uint64_t capacity)
   uint64_t T = c->n_tiles;
   if (capacity < T)
     return wb_fail(c, WB_EINVAL, "wb_tile_planes: capacity below the tile count");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   std::vector<TileRes> r(T);
   if (T)
     WB_CUDA(c, cudaMemcpyAsync(r.data(), c->tileRes.p, T * sizeof(TileRes), cudaMemcpyDefault, c->stream));
@@ -549,7 +557,7 @@ int wb_autotune(wb_ctx *c, const wb_params *p)
     return WB_EINVAL;
   if (c->stage < 2)
     return wb_fail(c, WB_ESTATE, "wb_autotune: scan the tiles first");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   std::string err;
   int rc = 0;
   if (!c->batch && (rc = wb_batch_create(c->device, &c->batch, err)))
@@ -575,7 +583,7 @@ int wb_classify_cloud(wb_ctx *c, const wb_cloud *cloud, const wb_params *p, uint
 {
   if (!c || !cloud || !p)
     return WB_EINVAL;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   beginRun(c);
   int rc = wb_build_impl(c, cloud);
   if (rc == 0)
@@ -680,7 +688,7 @@ extern "C" int wb_octree_find_block_static(wb_ctx *c, const double *xyz, uint64_
                                      std::to_string(WB_FIND_BLOCK_STATIC_MAX) + "-entry static staging array");
   if (m == 0)
     return 0;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   StaticSlots s;
   int rc = staticSlots(c, s);
   if (rc)

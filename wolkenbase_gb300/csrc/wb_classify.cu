@@ -1531,7 +1531,7 @@ int wb_batch_create(int device, WbBatch **out, std::string &err)
   if (!b)
     return WB_ENOMEM;
   b->device = device;
-  cudaSetDevice(device);
+  WbDeviceGuard deviceGuard(device);
   cudaDeviceGetAttribute(&b->sm, cudaDevAttrMultiProcessorCount, device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
   if (e == cudaSuccess)
@@ -1557,7 +1557,7 @@ void wb_batch_destroy(WbBatch *b)
 {
   if (!b)
     return;
-  cudaSetDevice(b->device);
+  WbDeviceGuard deviceGuard(b->device);
   for (cudaGraphExec_t g : b->graphs)
     if (g)
       cudaGraphExecDestroy(g);
@@ -1589,7 +1589,7 @@ int wb_batch_time(WbBatch *b, wb_ctx *const *jobs, int k, uint64_t sample, int s
   int rc = fillTable(b, jobs, k, chunk, sample, err);
   if (rc)
     return rc;
-  cudaSetDevice(b->device);
+  WbDeviceGuard deviceGuard(b->device);
   unsigned grids[3];
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = batchGrids(b, shape, grids);
@@ -1633,7 +1633,7 @@ int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int 
   int rc = fillTable(b, jobs, k, chunk, 0, err);
   if (rc)
     return rc;
-  cudaSetDevice(b->device);
+  WbDeviceGuard deviceGuard(b->device);
   if (!b->graphs[shape])
   {
     cudaError_t e = captureBatch(b, shape, &b->graphs[shape]);

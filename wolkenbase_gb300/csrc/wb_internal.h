@@ -120,6 +120,33 @@ struct TileRes
   double plane[3];   /* least-squares plane z = a*x + b*y + c, x and y from the tile centre */
 };
 
+/* Makes `device` current for the guard's lifetime and gives the caller's
+ * current device back when it ends, so that no entry point leaves the host
+ * application on another device than the one it was using. */
+struct WbDeviceGuard
+{
+  int prev = -1;
+  bool ok = true;
+  explicit WbDeviceGuard(int device)
+  {
+    if (cudaGetDevice(&prev) != cudaSuccess)
+    {
+      prev = -1;
+      cudaGetLastError();
+    }
+    if (prev != device)
+      ok = cudaSetDevice(device) == cudaSuccess;
+  }
+  WbDeviceGuard(const WbDeviceGuard &) = delete;
+  WbDeviceGuard &operator=(const WbDeviceGuard &) = delete;
+  ~WbDeviceGuard()
+  {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+};
+
 /* error helpers */
 int wb_fail(wb_ctx *c, int code, const std::string &msg);
 #define WB_CUDA(c, call)                                                        \

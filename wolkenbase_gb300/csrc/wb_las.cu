@@ -125,7 +125,7 @@ int wb_class_totals(wb_ctx *c, uint64_t *totals)
     return WB_EINVAL;
   if (c->stage < 3 || !c->clsFinal)
     return wb_fail(c, WB_ESTATE, "wb_class_totals: classify first");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   WbScratch out(c);
   int rc = wb_ensure(c, out.b, 256 * 8);
   if (rc)
@@ -151,7 +151,7 @@ int wb_duplicates(wb_ctx *c, uint64_t *n_dup, uint32_t *dup_of)
   *n_dup = c->n - c->nd;
   if (!dup_of || !c->n)
     return 0;
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   WbScratch out(c);
   int rc = wb_ensure(c, out.b, c->n * 4);
   if (rc)
@@ -179,7 +179,7 @@ int wb_las_write_classes(wb_ctx *c, void *records, uint64_t n, uint32_t stride, 
     return 0;
   if (on_device && (!wb_device_accessible(records) || (cls && !wb_device_accessible(cls))))
     return wb_fail(c, WB_EINVAL, "wb_las_write_classes: on_device needs device pointers");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   int rc;
   WbScratch rbuf(c), cbuf(c);
   uint8_t *drec = (uint8_t *)records;
@@ -223,7 +223,7 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
     return 0;
   if (on_device && (!wb_device_accessible(records) || !wb_device_accessible(out)))
     return wb_fail(c, WB_EINVAL, "wb_las_split_by_class: on_device needs device pointers");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   int rc;
   WbScratch rin(c), rout(c), hist(c);
   const uint8_t *din = (const uint8_t *)records;
@@ -341,7 +341,7 @@ extern "C" int wb_preview(wb_ctx *c, double x0, double y0, double side, int w, i
     return wb_fail(c, WB_ESTATE, "wb_preview: build the octree first");
   if (!(c->g.scale[2] * c->g.unit > 0))
     return wb_fail(c, WB_EINVAL, "wb_preview: needs a positive z scale (elevation increasing in Z)");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   const uint64_t npix = (uint64_t)w * h;
   WbScratch cnt(c), zl(c), zh(c);
   int rc;

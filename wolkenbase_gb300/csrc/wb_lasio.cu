@@ -890,7 +890,7 @@ int wb_las_decode(wb_ctx *c, const wb_cloud *cloud, int fmt, const wb_las_points
     return 0;
   if (cloud->device_resident && !wb_device_accessible(cloud->records))
     return wb_fail(c, WB_EINVAL, "wb_las_decode: device_resident records must be device memory");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   int rc;
   DecodeArgs a;
   a.n = n;
@@ -993,7 +993,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   if (cloud->device_resident && c->n &&
       (!wb_device_accessible(cloud->records) || (cls && !wb_device_accessible(cls))))
     return wb_fail(c, WB_EINVAL, "wb_las_write_output: device_resident records (and class bytes) must be device memory");
-  cudaSetDevice(c->device);
+  WbDeviceGuard deviceGuard(c->device);
   const uint64_t n = c->n, nd = c->nd, L = c->n_leaves;
   const Layout Li = layoutOf(in_format), Lo = layoutOf(opt->point_format);
   int rc;

@@ -386,7 +386,8 @@ wb_server *wb_server_open(const wb_server_config *cfg)
     wb_fail(nullptr, WB_EINVAL, "wb_server_open: cfg is NULL");
     return nullptr;
   }
-  wb_ctx *probe = wb_open(cfg->device, 0);   // validates the device, sets it current
+  WbDeviceGuard deviceGuard(cfg->device);
+  wb_ctx *probe = wb_open(cfg->device, 0);   // validates the device
   if (!probe)
     return nullptr;
   wb_server *s = new (std::nothrow) wb_server;
@@ -456,7 +457,7 @@ void wb_server_close(wb_server *s)
   for (auto &t : s->preps)
     t.join();
   s->classifier.join();
-  cudaSetDevice(s->cfg.device);
+  WbDeviceGuard deviceGuard(s->cfg.device);
   for (wb_ctx *c : s->all)
     wb_close(c);
   wb_batch_destroy(s->batch);

@@ -1274,6 +1274,18 @@ static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
   return 0;
 }
 
+/* Sum of the tiles' room bounds in 64 bits. */
+__global__ void boundTotal64(const uint32_t *bound, uint64_t T, unsigned long long *tot)
+{
+  unsigned long long s = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < T; i += (uint64_t)gridDim.x * blockDim.x)
+    s += bound[i];
+  for (int o = 16; o; o >>= 1)
+    s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s)
+    atomicAdd(tot, s);
+}
+
 int wb_scan_impl(wb_ctx *c, const wb_params *p)
 {
   if (c->stage < 1)
@@ -1313,12 +1325,23 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
         a, gd, bound); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
+  // Cylinders overlap, so the rooms add up to more than the points; their sum
+  // is taken in 64 bits first, because the list offsets below are 32-bit.
+  unsigned long long *dTot64 = (unsigned long long *)((char *)c->small.p + 768);
+  WB_CUDA(c, cudaMemsetAsync(dTot64, 0, 8, c->stream));
+  { boundTotal64<<<(unsigned)std::min<uint64_t>((T + 255) / 256, (uint64_t)c->sm_count * 8), 256, 0, c->stream>>>(
+        bound, T, dTot64); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  unsigned long long room64 = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&room64, dTot64, 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (room64 > 0xfffffff0ull)
+    return wb_fail(c, WB_EINVAL, "wb_scan_tiles: the tiles' point lists would hold " + std::to_string(room64) +
+                                     " entries, above the 2^32 that their 32-bit offsets address");
   if ((rc = wb_exclusive_scan_u32(c, bound, tileStart, T, dTot)))
     return rc;
   WB_CUDA(c, cudaMemcpyAsync(tileStart + T, dTot, 4, cudaMemcpyDefault, c->stream));
-  uint32_t room = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&room, dTot, 4, cudaMemcpyDefault, c->stream));
-  WB_CUDA(c, cudaStreamSynchronize(c->stream));
+  uint32_t room = (uint32_t)room64;
   if ((rc = wb_ensure(c, c->tilePts, (uint64_t)room * 4 + 64)))
     return rc;
   { fillOwner<<<(unsigned)std::min<uint64_t>((nd + 255) / 256 + 1, (uint64_t)c->sm_count * 16), 256, 0, c->stream>>>(owner, nd); ++c->launches; }
