@@ -34,7 +34,8 @@ class RunIO(C.Structure):
                 ("snake_center", C.c_double * 3), ("snake_side", C.c_double), ("spacing", C.c_double),
                 ("snake_index", C.c_int),
                 ("t_build", C.c_double), ("t_scan", C.c_double), ("t_postscan", C.c_double),
-                ("t_classify", C.c_double)]
+                ("t_classify", C.c_double), ("sample_tiles", C.POINTER(C.c_int64)), ("n_sample", C.c_uint64),
+                ("n_scanned", C.c_uint64), ("n_sample_points", C.c_uint64)]
 
 
 TILE_DTYPE = np.dtype([("ex", "<i4"), ("ey", "<i4"), ("n_points", "<i4"), ("n_ground", "<i4"),
@@ -89,8 +90,13 @@ def _ptr(a, ct):
 
 
 def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
-        phases=3, canonical_order=False, threads=1):
-    """Runs the restated pipeline; returns a dict of numpy arrays and scalars."""
+        phases=3, canonical_order=False, threads=1, sample_tiles=None, want_leaves=True):
+    """Runs the restated pipeline; returns a dict of numpy arrays and scalars.
+
+    sample_tiles: positions in flowsnake order of the only tiles to post-scan
+    and classify (the tiles their postscan reads are scanned on demand); cls is
+    then written only for the points those tiles decide (their last
+    containing tile in flowsnake order), 0 elsewhere."""
     L = lib()
     xyz = np.ascontiguousarray(cloud.xyz, dtype=np.int32)
     n = xyz.shape[0]
@@ -113,6 +119,10 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
     io.block_pos = _ptr(pos, C.c_int32)
     io.leaf = _ptr(leaf, C.c_int64)
     io.cls = _ptr(cls, C.c_uint8)
+    if sample_tiles is not None:
+        smp = np.ascontiguousarray(sample_tiles, dtype=np.int64)
+        io.sample_tiles = _ptr(smp, C.c_int64)
+        io.n_sample = smp.shape[0]
     prm = Params(tile_size, max_slope, thickness, min_hyp_size)
     rc = L.wbo_run(C.byref(io), C.byref(prm))
     if rc != 0:
@@ -120,7 +130,8 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
     nl = io.n_leaves
     leaves = np.zeros((nl, 4))
     counts = np.zeros(nl, np.int64)
-    L.wbo_leaves(leaves.ctypes.data, counts.ctypes.data)
+    if want_leaves:
+        L.wbo_leaves(leaves.ctypes.data, counts.ctypes.data)
     tiles = np.zeros(io.n_tiles, TILE_DTYPE)
     if phases >= 2:
         L.wbo_tiles(tiles.ctypes.data)
@@ -129,7 +140,8 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
                root_center=tuple(io.root_center), root_side=io.root_side,
                snake_center=tuple(io.snake_center), snake_side=io.snake_side, spacing=io.spacing,
                snake_index=io.snake_index,
-               t_build=io.t_build, t_scan=io.t_scan, t_postscan=io.t_postscan, t_classify=io.t_classify)
+               t_build=io.t_build, t_scan=io.t_scan, t_postscan=io.t_postscan, t_classify=io.t_classify,
+               n_scanned=io.n_scanned, n_sample_points=io.n_sample_points)
     L.wbo_reset()
     return out
 

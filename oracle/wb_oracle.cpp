@@ -27,6 +27,7 @@
 #include <complex>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <set>
 #include <thread>
 #include <unordered_map>
@@ -842,8 +843,28 @@ struct Pipeline
     t.height = top - bottom;
   }
 
+  /* Tiles scanned on demand in a sampled run (each exactly once). */
+  std::vector<std::once_flag> *scanOnce = nullptr;
+  std::atomic<uint64_t> nScanned{0};
+  void ensureScanned(size_t k)
+  {
+    if (scanOnce)
+      std::call_once((*scanOnce)[k], [&] {
+        scanTile(k);
+        nScanned++;
+      });
+  }
+  const TileR *tileAtScanned(Eis e)
+  {
+    auto it = addrToK.find(akey(e));
+    if (it == addrToK.end())
+      return nullptr;
+    ensureScanned((size_t)it->second);
+    return &tiles[it->second];
+  }
+
   /* postscanCylinder (scan.cpp:142-179) */
-  double postscanTile(size_t k) const
+  double postscanTile(size_t k)
   {
     const TileR &me = tiles[k];
     if (!me.nPoints)
@@ -856,7 +877,7 @@ struct Pipeline
       for (int j = 0; j < 6 && (me.treeFlags & 1); j++)
       {
         Eis a{order[k].x + ring[j].x * i, order[k].y + ring[j].y * i};
-        const TileR *t = tileAt(a);
+        const TileR *t = tileAtScanned(a);
         if (t && t->nPoints)
         {
           ringcount++;
@@ -940,6 +961,22 @@ struct Pipeline
     }
   }
 };
+
+/* Whether tile k is the last tile in flowsnake order whose cylinder holds the
+ * point at p: only the six tiles around k can reach it (a cylinder's radius,
+ * 41/71 of the spacing, is below the distance to the second ring minus that
+ * radius). */
+bool ownsPoint(const Pipeline &P, size_t k, const V3 &p)
+{
+  static const Eis ring[6] = {{1, 0}, {1, 1}, {0, 1}, {-1, 0}, {-1, -1}, {0, -1}};
+  for (const Eis &r : ring)
+  {
+    auto it = P.addrToK.find(Pipeline::akey(Eis{P.order[k].x + r.x, P.order[k].y + r.y}));
+    if (it != P.addrToK.end() && (size_t)it->second > k && P.snake.cyl(P.order[it->second]).in(p))
+      return false;
+  }
+  return true;
+}
 
 Pipeline *gPipe = nullptr;
 
@@ -1049,7 +1086,48 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
   P.tiles.assign(P.order.size(), TileR());
   int thr = io->threads > 0 ? io->threads : 1;
   double t2 = t1, t3 = t1, t4 = t1;
-  if (io->phases >= 2)
+  io->n_scanned = 0;
+  io->n_sample_points = 0;
+  if (io->phases >= 2 && io->n_sample > 0)
+  {
+    std::vector<size_t> smp;
+    for (uint64_t i = 0; i < io->n_sample; i++)
+      if (io->sample_tiles[i] >= 0 && (size_t)io->sample_tiles[i] < P.order.size())
+        smp.push_back((size_t)io->sample_tiles[i]);
+    std::vector<std::once_flag> once(P.order.size());
+    P.scanOnce = &once;
+    std::vector<double> hNew(smp.size());
+    parallelFor(smp.size(), thr, [&](size_t i) {
+      P.ensureScanned(smp[i]);
+      hNew[i] = P.postscanTile(smp[i]);
+    });
+    for (size_t i = 0; i < smp.size(); i++)
+      P.tiles[smp[i]].h = hNew[i];
+    P.scanOnce = nullptr;
+    t2 = t3 = nowSec();
+    io->n_scanned = P.nScanned.load();
+    if (io->cls)
+      memset(io->cls, 0, n);
+    if (io->phases >= 3)
+    {
+      std::atomic<uint64_t> pts(0);
+      parallelFor(smp.size(), thr, [&](size_t i) {
+        size_t k = smp[i];
+        std::vector<std::pair<uint32_t, uint8_t>> res;
+        int ng = 0;
+        P.classifyTile(k, res, ng);
+        P.tiles[k].nGround = ng;
+        pts += res.size();
+        if (io->cls)
+          for (auto &r : res)
+            if (ownsPoint(P, k, P.st.loc[r.first]))
+              io->cls[r.first] = r.second;
+      });
+      io->n_sample_points = pts.load();
+      t4 = nowSec();
+    }
+  }
+  else if (io->phases >= 2)
   {
     parallelFor(P.order.size(), thr, [&](size_t k) { P.scanTile(k); });
     t2 = nowSec();
@@ -1059,9 +1137,9 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
       P.tiles[k].h = hNew[k];
     t3 = nowSec();
   }
-  if (io->cls)
+  if (io->cls && io->n_sample == 0)
     memset(io->cls, 0, n);
-  if (io->phases >= 3)
+  if (io->phases >= 3 && io->n_sample == 0)
   {
     std::vector<std::atomic<int64_t>> best(n);
     for (uint64_t i = 0; i < n; i++)

@@ -51,6 +51,15 @@ typedef struct
   double snake_center[3], snake_side, spacing;
   int snake_index;         /* which Gosper island size was chosen        */
   double t_build, t_scan, t_postscan, t_classify;  /* seconds */
+  /* Sampled run (n_sample > 0, phases >= 2): only these tiles (positions in
+     flowsnake order, 0-based) are post-scanned and classified; the tiles
+     their postscan walks are scanned on demand.  cls is written only for the
+     stored points whose last containing tile in flowsnake order is sampled,
+     so every written byte is final. */
+  const int64_t *sample_tiles;
+  uint64_t n_sample;
+  uint64_t n_scanned;      /* tiles scanned (sampled run: the sample plus what postscan needed) */
+  uint64_t n_sample_points;   /* points in the sampled tiles' cylinders (classified, overlaps counted) */
 } wbo_run_io;
 
 /* Whole pipeline; returns 0 on success. */

@@ -10,8 +10,11 @@ machine only; the fixture keeps what the tests need in little room:
 
   xyz_sha256      digest of the int32 input, so a test knows it regenerated
                   the same cloud
-  leaf_cube       every leaf cube (center xyz, side) in depth-first order
-  leaf_of_point   per point, the index of its leaf cube (uint16: < 65536 leaves)
+  leaf_cube       every distinct leaf cube (center xyz, side), sorted
+  stored_bits     per point, 1 where the record is stored (not overwritten by a
+                  later identical point), bit-packed
+  point_cube_sha256  digest of the (n, 4) float64 array of every point's leaf
+                  cube (center xyz, side; zeros where not stored)
   cls_bits        per point, 1 where the reference wrote class 2 (ground),
                   bit-packed; cls_set_bits: 1 where it wrote any class
   tile_n          points per tile (flowsnake order)
@@ -66,18 +69,16 @@ def main():
             f.write(r.stdout.strip().splitlines()[-1])
     res = O.read_ref_output(out)
     timing = json.load(open(tim)) if os.path.exists(tim) else {}
-    lc = res["leaf_cube"]
     have = res["block"] >= 0          # records a later identical point overwrote have no block
-    uniq, inv = np.unique(lc[have], axis=0, return_inverse=True)
-    leaf_of_point = np.full(res["n"], 65535, np.uint16)
-    assert uniq.shape[0] < 65535
-    leaf_of_point[have] = inv.astype(np.uint16).ravel()
+    lc = np.where(have[:, None], res["leaf_cube"], 0.0)
+    uniq = np.unique(lc[have], axis=0)
     cls = res["cls"]
     np.savez_compressed(
         os.path.join(HERE, "c1_ref.npz"),
         xyz_sha256=np.array(xyz_digest(cloud.xyz)), n=np.array(cloud.n),
         scale=np.array(cloud.scale), offset=np.array(cloud.offset), minc=np.array(cloud.minc),
-        maxc=np.array(cloud.maxc), leaf_cube=uniq, leaf_of_point=leaf_of_point,
+        maxc=np.array(cloud.maxc), leaf_cube=uniq, stored_bits=np.packbits(have),
+        point_cube_sha256=np.array(hashlib.sha256(np.ascontiguousarray(lc, dtype="<f8").tobytes()).hexdigest()),
         cls_bits=np.packbits(cls == 2), cls_set_bits=np.packbits(cls != 0),
         tile_n=res["tiles"]["n_points"].astype(np.int32), tile_flags=res["tiles"]["tree_flags"].astype(np.int8),
         tile_h=res["tiles"]["h_final"], root=np.array(list(res["root_center"]) + [res["root_side"]]),
