@@ -406,6 +406,10 @@ struct Store
   std::vector<V3> loc;
   std::vector<Node> nodes;                    // nodes[0] is the root
   std::vector<std::vector<uint32_t>> blocks;  // storage order
+  /* the coordinates of blocks[b]'s points in the same order, kept during the
+     build so that the de-duplication scan reads one block's memory in
+     sequence instead of one random location per stored point */
+  std::vector<std::vector<V3>> bloc;
   std::vector<uint32_t> spill;                // thread buffer 0 (LIFO)
 
   static int octant(const Node &nd, const V3 &p)
@@ -489,10 +493,11 @@ struct Store
   bool blockPut(int64_t b, uint32_t id)
   {
     std::vector<uint32_t> &v = blocks[b];
-    const V3 &p = loc[id];
-    for (size_t i = 0; i < v.size(); i++)
+    std::vector<V3> &w = bloc[b];
+    const V3 p = loc[id];
+    for (size_t i = 0; i < w.size(); i++)
     {
-      const V3 &q = loc[v[i]];
+      const V3 &q = w[i];
       if (q.x == p.x && q.y == p.y && q.z == p.z)
       {
         v[i] = id;   // last one wins
@@ -502,6 +507,7 @@ struct Store
     if ((int)v.size() < kRecords)
     {
       v.push_back(id);
+      w.push_back(p);
       return true;
     }
     return false;
@@ -516,12 +522,14 @@ struct Store
     {
       b = (int64_t)blocks.size();
       blocks.emplace_back();
+      bloc.emplace_back();
       setBlock(p, b);
     }
     if (!blockPut(b, id))
     {
       std::vector<uint32_t> moved;
       moved.swap(blocks[b]);
+      bloc[b].clear();
       splitAt(p);
       for (uint32_t m : moved)
         spill.push_back(m);
@@ -1046,6 +1054,7 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
     P.st.put((uint32_t)i);
     P.st.drain();
   }
+  std::vector<std::vector<V3>>().swap(P.st.bloc);
   if (io->canonical_order)
     for (auto &b : P.st.blocks)
       std::sort(b.begin(), b.end());

@@ -50,7 +50,11 @@
  * 0 points, 1 near columns tested, 2 super-cells tested, 3 far columns
  * tested, 4 candidates read, 5 candidates inside, 6 surround tests,
  * 7 columns scanned; SM clock cycles 8 near field, 9 far field, 10 final
- * gap, 11 whole point, 12 inside column scans, 13 inside surround tests. */
+ * gap, 11 whole point, 12 inside column scans, 13 inside surround tests.
+ * Row 0 is the column-group kernel: 0 groups, 1 columns read, 2 candidates
+ * kept, 3 kept x undecided lanes, 4 active lanes, 5 lanes handed over,
+ * 6 cycles, 7 super-cell rings, 8 lanes ending ground; 9-11 cycles, count
+ * and kept candidates of the groups that kept more than 1000. */
 #ifdef WB_CLASSIFY_STATS
 __device__ unsigned long long gClassifyStats[3][16];
 extern "C" int wb_classify_stats(unsigned long long *out, int reset)
@@ -700,7 +704,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       return;
 #ifdef WB_CLASSIFY_STATS
     const long long tG = clock64();
-    unsigned long long gst[8] = {0};
+    unsigned long long gst[12] = {0};
 #endif
     if (!a.exactInts)
     {
@@ -983,20 +987,24 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       }
     }
 #ifdef WB_CLASSIFY_STATS
+    const unsigned bAct = __ballot_sync(0xffffffffu, act), bDef = __ballot_sync(0xffffffffu, deferred);
+    const unsigned bGnd = __ballot_sync(0xffffffffu, act && !deferred && !done);
     if (lane == 0)
     {
       gst[0] = 1;
-      gst[4] = __popc(__ballot_sync(0xffffffffu, act));
-      gst[5] = __popc(__ballot_sync(0xffffffffu, deferred));
+      gst[4] = __popc(bAct);
+      gst[5] = __popc(bDef);
       gst[6] = clock64() - tG;
       gst[7] = smaxG;
-      for (int q = 0; q < 8; q++)
+      gst[8] = __popc(bGnd);
+      if (gst[2] > 1000)
+      {
+        gst[9] = gst[6];
+        gst[10] = 1;
+        gst[11] = gst[2];
+      }
+      for (int q = 0; q < 12; q++)
         atomicAdd(&gClassifyStats[0][q], gst[q]);
-    }
-    else
-    {
-      __ballot_sync(0xffffffffu, act);
-      __ballot_sync(0xffffffffu, deferred);
     }
 #endif
     if (act && !deferred)
