@@ -74,6 +74,10 @@ def lib():
         L.wbo_size_fit.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.wbo_flowsnake.argtypes = [C.c_int, C.c_void_p]
         L.wbo_flowsnake_limits.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        L.wbo_sample.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p]
+        L.wbo_snake_tiles.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double]
+        L.wbo_snake_tiles.restype = C.c_int64
         _lib = L
         # The reference's atan2i tables come from x86-64 80-bit long double;
         # hosts with another long double (aarch64: 128-bit) would round a few
@@ -90,13 +94,14 @@ def _ptr(a, ct):
 
 
 def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
-        phases=3, canonical_order=False, threads=1, sample_tiles=None, want_leaves=True):
+        phases=3, canonical_order=False, threads=1, sample_tiles=None, want_leaves=True, keep=False):
     """Runs the restated pipeline; returns a dict of numpy arrays and scalars.
 
     sample_tiles: positions in flowsnake order of the only tiles to post-scan
     and classify (the tiles their postscan reads are scanned on demand); cls is
     then written only for the points those tiles decide (their last
-    containing tile in flowsnake order), 0 elsewhere."""
+    containing tile in flowsnake order), 0 elsewhere.  keep: the octree stays
+    for sample() calls until reset()."""
     L = lib()
     xyz = np.ascontiguousarray(cloud.xyz, dtype=np.int32)
     n = xyz.shape[0]
@@ -142,8 +147,43 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
                snake_index=io.snake_index,
                t_build=io.t_build, t_scan=io.t_scan, t_postscan=io.t_postscan, t_classify=io.t_classify,
                n_scanned=io.n_scanned, n_sample_points=io.n_sample_points)
-    L.wbo_reset()
+    if not keep:
+        L.wbo_reset()
     return out
+
+
+def sample(tiles, n_points, threads=1):
+    """Another sampled scan + classify over the octree a run(keep=True) left:
+    class bytes of the points the sampled tiles decide (0 elsewhere), the
+    tiles' fields, and the times."""
+    L = lib()
+    smp = np.ascontiguousarray(tiles, dtype=np.int64)
+    cls = np.zeros(n_points, np.uint8)
+    ts, tc = C.c_double(0), C.c_double(0)
+    ns, npt = C.c_uint64(0), C.c_uint64(0)
+    rc = L.wbo_sample(smp.ctypes.data, smp.shape[0], threads, cls.ctypes.data, C.byref(ts), C.byref(tc),
+                      C.byref(ns), C.byref(npt))
+    if rc != 0:
+        raise RuntimeError("wbo_sample: no octree kept (run(keep=True) first)")
+    return dict(cls=cls, t_scan=ts.value, t_classify=tc.value, n_scanned=ns.value, n_sample_points=npt.value)
+
+
+def sample_tiles_fields(n_tiles):
+    """The tile table after the last sample() (fields of tiles it did not scan are zero)."""
+    tiles = np.zeros(n_tiles, TILE_DTYPE)
+    lib().wbo_tiles(tiles.ctypes.data)
+    return tiles
+
+
+def reset():
+    lib().wbo_reset()
+
+
+def snake_tiles(cloud, tile_size=1.0):
+    """Tiles of the flowsnake island the reference sizes for this cloud."""
+    mn = np.ascontiguousarray(cloud.minc, np.float64)
+    mx = np.ascontiguousarray(cloud.maxc, np.float64)
+    return int(lib().wbo_snake_tiles(mn.ctypes.data, mx.ctypes.data, float(cloud.unit), float(tile_size)))
 
 
 def atan2i(y, x):

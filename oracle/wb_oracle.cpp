@@ -410,7 +410,27 @@ struct Store
      build so that the de-duplication scan reads one block's memory in
      sequence instead of one random location per stored point */
   std::vector<std::vector<V3>> bloc;
+  /* per block, an open-addressing table of positions (+1) in bloc[b] keyed by
+     the coordinates: finds the equal point the reference's linear scan finds,
+     without reading the whole block */
+  static const int kHash = 1024;
+  std::vector<std::vector<uint16_t>> bhash;
   std::vector<uint32_t> spill;                // thread buffer 0 (LIFO)
+
+  static uint32_t hashOf(const V3 &p)
+  {
+    // +0.0 and -0.0 compare equal, so they must hash alike
+    double c[3] = {p.x == 0 ? 0.0 : p.x, p.y == 0 ? 0.0 : p.y, p.z == 0 ? 0.0 : p.z};
+    uint64_t h = 1469598103934665603ull;
+    for (double v : c)
+    {
+      uint64_t u;
+      memcpy(&u, &v, 8);
+      h = (h ^ u) * 1099511628211ull;
+      h ^= h >> 29;
+    }
+    return (uint32_t)(h ^ (h >> 32));
+  }
 
   static int octant(const Node &nd, const V3 &p)
   {
@@ -494,13 +514,17 @@ struct Store
   {
     std::vector<uint32_t> &v = blocks[b];
     std::vector<V3> &w = bloc[b];
+    std::vector<uint16_t> &ht = bhash[b];
+    if (ht.empty())
+      ht.assign(kHash, 0);
     const V3 p = loc[id];
-    for (size_t i = 0; i < w.size(); i++)
+    uint32_t h = hashOf(p) & (kHash - 1);
+    for (; ht[h]; h = (h + 1) & (kHash - 1))
     {
-      const V3 &q = w[i];
+      const V3 &q = w[ht[h] - 1];
       if (q.x == p.x && q.y == p.y && q.z == p.z)
       {
-        v[i] = id;   // last one wins
+        v[ht[h] - 1] = id;   // last one wins
         return true;
       }
     }
@@ -508,6 +532,7 @@ struct Store
     {
       v.push_back(id);
       w.push_back(p);
+      ht[h] = (uint16_t)w.size();
       return true;
     }
     return false;
@@ -523,6 +548,7 @@ struct Store
       b = (int64_t)blocks.size();
       blocks.emplace_back();
       bloc.emplace_back();
+      bhash.emplace_back();
       setBlock(p, b);
     }
     if (!blockPut(b, id))
@@ -530,6 +556,7 @@ struct Store
       std::vector<uint32_t> moved;
       moved.swap(blocks[b]);
       bloc[b].clear();
+      bhash[b].assign(kHash, 0);
       splitAt(p);
       for (uint32_t m : moved)
         spill.push_back(m);
@@ -1013,6 +1040,63 @@ void parallelFor(size_t count, int threads, F f)
     t.join();
 }
 
+struct SampleOut
+{
+  double tScan = 0, tClassify = 0;
+  uint64_t nScanned = 0, nPoints = 0;
+};
+
+/* Scans, post-scans and (classify) classifies only the given tiles, scanning
+ * the tiles their postscan reads on demand, from a fresh tile table; cls
+ * (n entries) is zeroed and receives the class of every point a sampled tile
+ * decides. */
+SampleOut runSample(Pipeline &P, const int64_t *tiles, uint64_t count, int thr, uint8_t *cls, uint64_t n,
+                    bool classify)
+{
+  SampleOut so;
+  double t0 = nowSec();
+  P.tiles.assign(P.order.size(), TileR());
+  P.nScanned = 0;
+  std::vector<size_t> smp;
+  for (uint64_t i = 0; i < count; i++)
+    if (tiles[i] >= 0 && (size_t)tiles[i] < P.order.size())
+      smp.push_back((size_t)tiles[i]);
+  std::vector<std::once_flag> once(P.order.size());
+  P.scanOnce = &once;
+  std::vector<double> hNew(smp.size());
+  parallelFor(smp.size(), thr, [&](size_t i) {
+    P.ensureScanned(smp[i]);
+    hNew[i] = P.postscanTile(smp[i]);
+  });
+  for (size_t i = 0; i < smp.size(); i++)
+    P.tiles[smp[i]].h = hNew[i];
+  P.scanOnce = nullptr;
+  double t1 = nowSec();
+  so.tScan = t1 - t0;
+  so.nScanned = P.nScanned.load();
+  if (cls)
+    memset(cls, 0, n);
+  if (classify)
+  {
+    std::atomic<uint64_t> pts(0);
+    parallelFor(smp.size(), thr, [&](size_t i) {
+      size_t k = smp[i];
+      std::vector<std::pair<uint32_t, uint8_t>> res;
+      int ng = 0;
+      P.classifyTile(k, res, ng);
+      P.tiles[k].nGround = ng;
+      pts += res.size();
+      if (cls)
+        for (auto &r : res)
+          if (ownsPoint(P, k, P.st.loc[r.first]))
+            cls[r.first] = r.second;
+    });
+    so.nPoints = pts.load();
+    so.tClassify = nowSec() - t1;
+  }
+  return so;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1055,6 +1139,7 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
     P.st.drain();
   }
   std::vector<std::vector<V3>>().swap(P.st.bloc);
+  std::vector<std::vector<uint16_t>>().swap(P.st.bhash);
   if (io->canonical_order)
     for (auto &b : P.st.blocks)
       std::sort(b.begin(), b.end());
@@ -1099,42 +1184,11 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
   io->n_sample_points = 0;
   if (io->phases >= 2 && io->n_sample > 0)
   {
-    std::vector<size_t> smp;
-    for (uint64_t i = 0; i < io->n_sample; i++)
-      if (io->sample_tiles[i] >= 0 && (size_t)io->sample_tiles[i] < P.order.size())
-        smp.push_back((size_t)io->sample_tiles[i]);
-    std::vector<std::once_flag> once(P.order.size());
-    P.scanOnce = &once;
-    std::vector<double> hNew(smp.size());
-    parallelFor(smp.size(), thr, [&](size_t i) {
-      P.ensureScanned(smp[i]);
-      hNew[i] = P.postscanTile(smp[i]);
-    });
-    for (size_t i = 0; i < smp.size(); i++)
-      P.tiles[smp[i]].h = hNew[i];
-    P.scanOnce = nullptr;
-    t2 = t3 = nowSec();
-    io->n_scanned = P.nScanned.load();
-    if (io->cls)
-      memset(io->cls, 0, n);
-    if (io->phases >= 3)
-    {
-      std::atomic<uint64_t> pts(0);
-      parallelFor(smp.size(), thr, [&](size_t i) {
-        size_t k = smp[i];
-        std::vector<std::pair<uint32_t, uint8_t>> res;
-        int ng = 0;
-        P.classifyTile(k, res, ng);
-        P.tiles[k].nGround = ng;
-        pts += res.size();
-        if (io->cls)
-          for (auto &r : res)
-            if (ownsPoint(P, k, P.st.loc[r.first]))
-              io->cls[r.first] = r.second;
-      });
-      io->n_sample_points = pts.load();
-      t4 = nowSec();
-    }
+    SampleOut so = runSample(P, io->sample_tiles, io->n_sample, thr, io->cls, n, io->phases >= 3);
+    t2 = t3 = t1 + so.tScan;
+    t4 = t3 + so.tClassify;
+    io->n_scanned = so.nScanned;
+    io->n_sample_points = so.nPoints;
   }
   else if (io->phases >= 2)
   {
@@ -1191,6 +1245,33 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
   io->t_postscan = t3 - t2;
   io->t_classify = t4 - t3;
   return 0;
+}
+
+int wbo_sample(const int64_t *tiles, uint64_t count, int threads, uint8_t *cls, double *t_scan, double *t_classify,
+               uint64_t *n_scanned, uint64_t *n_points)
+{
+  if (!gPipe)
+    return -1;
+  SampleOut so = runSample(*gPipe, tiles, count, threads > 0 ? threads : 1, cls, gPipe->st.loc.size(), true);
+  if (t_scan)
+    *t_scan = so.tScan;
+  if (t_classify)
+    *t_classify = so.tClassify;
+  if (n_scanned)
+    *n_scanned = so.nScanned;
+  if (n_points)
+    *n_points = so.nPoints;
+  return 0;
+}
+
+int64_t wbo_snake_tiles(const double *minc, const double *maxc, double unit, double tile_size)
+{
+  ensureTables();
+  V3 mn{minc[0] * unit, minc[1] * unit, minc[2] * unit};
+  V3 mx{maxc[0] * unit, maxc[1] * unit, maxc[2] * unit};
+  Snake sn;
+  sn.setSize(snakeCube(mn, mx), tile_size);
+  return (int64_t)sn.hi - sn.lo + 1;
 }
 
 int wbo_leaves(double *cs, int64_t *count)

@@ -76,6 +76,15 @@ typedef struct
 } wbo_tile;
 int wbo_tiles(wbo_tile *out /* n_tiles */);
 
+/* After wbo_run: another sampled run (see sample_tiles above) over the same
+ * octree, from a fresh tile table; cls has one entry per input point. */
+int wbo_sample(const int64_t *tiles, uint64_t count, int threads, uint8_t *cls, double *t_scan, double *t_classify,
+               uint64_t *n_scanned, uint64_t *n_points);
+
+/* Tiles of the flowsnake island Flowsnake::setSize picks for a cloud with
+ * these header corners (file units) and tile size. */
+int64_t wbo_snake_tiles(const double *minc, const double *maxc, double unit, double tile_size);
+
 /* Frees the state kept by wbo_run. */
 void wbo_reset(void);
 

@@ -72,9 +72,22 @@ def _ground(x, y, params, steps):
 
 
 def _in_boxes(x, y, boxes):
+    """Whether each (x, y) lies inside a building footprint (|x-cx| < hx and
+    |y-cy| < hy for some box).  With many boxes the points are sorted by x
+    once and each box tests only its strip (a little wider than the box, so
+    the same exact test decides every point)."""
     inside = np.zeros(x.shape, dtype=bool)
+    if len(boxes) <= 8 or x.size < 200_000:
+        for (cx, cy, hx, hy, _roof, _h) in boxes:
+            inside |= (np.abs(x - cx) < hx) & (np.abs(y - cy) < hy)
+        return inside
+    order = np.argsort(x)
+    xs = x[order]
     for (cx, cy, hx, hy, _roof, _h) in boxes:
-        inside |= (np.abs(x - cx) < hx) & (np.abs(y - cy) < hy)
+        pad = 1e-3 + 1e-9 * abs(cx)
+        idx = order[np.searchsorted(xs, cx - hx - pad, side="left"):np.searchsorted(xs, cx + hx + pad, side="right")]
+        hit = (np.abs(x[idx] - cx) < hx) & (np.abs(y[idx] - cy) < hy)
+        inside[idx[hit]] = True
     return inside
 
 
