@@ -82,6 +82,13 @@ constexpr uint32_t kStray = 0x80000000u;
  * atan2i on random and edge-case differences), so this is twice that. */
 constexpr uint32_t kMargin = 2048;
 
+/* Radians per unit of the reference's integer angle (2^31 per turn). */
+constexpr float kUnitRad = 2.925836158534319e-09f;
+/* How far an arc's rays are moved outward: far above the FP32 direction's
+ * error bound (kMargin units, 6e-6 rad), the arc endpoints' float rounding
+ * (128 units) and the box test's rounding. */
+constexpr float kArcPad = 4e-5f;
+
 /* Per-point values the warp kernel needs, formed once per point by a
  * thread-per-point kernel: double arithmetic costs 16 cycles per warp
  * instruction on this GPU, so it is kept out of the 32-lane warp kernel. */
@@ -274,6 +281,59 @@ __device__ __forceinline__ uint32_t largestGap(const uint32_t *bmin, const uint3
   return worst;
 }
 
+/* largestGap, plus the gaps at or above thr: how many there are and, for the
+ * last one found, where it starts (u0, a bin's largest direction) and how
+ * wide it is; every lane receives the same values. */
+__device__ __forceinline__ uint32_t largestGapArc(const uint32_t *bmin, const uint32_t *bmax, int lane, uint32_t thr,
+                                                  int &nocc, int &nbig, uint32_t &u0, uint32_t &w)
+{
+  uint32_t mn0 = bmin[lane], mn1 = bmin[lane + 32];
+  uint32_t mx0 = bmax[lane], mx1 = bmax[lane + 32];
+  unsigned lo = __ballot_sync(0xffffffffu, mn0 != 0xffffffffu);
+  unsigned hi = __ballot_sync(0xffffffffu, mn1 != 0xffffffffu);
+  uint64_t occ = ((uint64_t)hi << 32) | lo;
+  nocc = __popcll(occ);
+  nbig = 0;
+  u0 = w = 0;
+  uint32_t worst = 0, myU0 = 0, myW = 0;
+  bool big = false;
+  if (nocc >= 2)
+  {
+    for (int half = 0; half < 2; half++)
+    {
+      int b = lane + 32 * half;
+      if ((occ >> b) & 1)
+      {
+        uint64_t rot = (b == 63) ? 0 : (occ >> (b + 1));
+        int nb = rot ? b + 1 + __ffsll((long long)rot) - 1 : __ffsll((long long)occ) - 1;
+        const uint32_t start = half ? mx1 : mx0;
+        uint32_t gap = (bmin[nb] - start) & 0x7fffffffu;
+        worst = max(worst, gap);
+        if (gap >= thr)
+        {
+          nbig += 1;
+          big = true;
+          myU0 = start;
+          myW = gap;
+        }
+      }
+    }
+    for (int o = 16; o; o >>= 1)
+    {
+      worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+      nbig += __shfl_xor_sync(0xffffffffu, nbig, o);
+    }
+    const unsigned bl = __ballot_sync(0xffffffffu, big);
+    if (bl)
+    {
+      const int src = 31 - __clz(bl);
+      u0 = __shfl_sync(0xffffffffu, myU0, src);
+      w = __shfl_sync(0xffffffffu, myW, src);
+    }
+  }
+  return worst;
+}
+
 /* The double-precision set-up of point j's query, one thread per point. */
 __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
 {
@@ -343,6 +403,27 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   // Directions are kept as exact per-bin extremes in shared memory plus a
   // 64-bit occupancy mask in registers (uniform across the warp).
   uint32_t occLo = 0, occHi = 0;
+  // The fast pass's arc (see setArc): directions outside the one gap that can
+  // still decide the point change nothing, so boxes outside it are skipped.
+  int amode = 0;
+  float e0x = 0.f, e0y = 0.f, e1x = 0.f, e1y = 0.f;
+  auto arcWants = [&](const int4 &b) -> bool {
+    if (amode == 0)
+      return true;
+    const float x0 = (float)(b.x - h.qx) * h.sx, x1 = (float)(b.z - h.qx) * h.sx;
+    const float y0 = (float)(b.y - h.qy) * h.sy, y1 = (float)(b.w - h.qy) * h.sy;
+    if (amode == 1)
+    {
+      const float A = fmaxf(e0x * y0, e0x * y1) + fmaxf(-e0y * x0, -e0y * x1);
+      const float B = fmaxf(e1y * x0, e1y * x1) + fmaxf(-e1x * y0, -e1x * y1);
+      const float bx = e0x + e1x, by = e0y + e1y;
+      const float D = fmaxf(bx * x0, bx * x1) + fmaxf(by * y0, by * y1);
+      return A >= 0.f && B >= 0.f && D >= 0.f;
+    }
+    const float A = fminf(e1x * y0, e1x * y1) + fminf(-e1y * x0, -e1y * x1);
+    const float B = fminf(e0y * x0, e0y * x1) + fminf(-e0x * y0, -e0x * y1);
+    return !(A > 0.f && B > 0.f);
+  };
   unsigned long long stat[16] = {0};
 #ifdef WB_CLASSIFY_STATS
   const long long tStart = clock64();
@@ -492,6 +573,35 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     uint64_t occ = ((uint64_t)occHi << 32) | occLo;
     if (__popcll(occ) < 2)
       return;
+    if (fast)
+    {
+      // the fast pass always forms the gaps: they give the arc
+      __syncwarp();
+      int nocc, nbig;
+      uint32_t u0, w;
+      const uint32_t thr = a.fp32Only ? (uint32_t)WB_DEG144 : (uint32_t)WB_DEG144 - 2 * kMargin;
+      uint32_t gap = largestGapArc(bminW, bmaxW, lane, thr, nocc, nbig, u0, w);
+      if (nocc >= 2)
+        surrounded = a.fp32Only ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+      amode = 0;
+      if (!surrounded && nbig == 1)
+      {
+        const float a0 = (float)u0 * kUnitRad - kArcPad;
+        const float W = (float)w * kUnitRad + 2.f * kArcPad;
+        if (W < 6.2f)
+        {
+          float s0, c0, s1, c1;
+          sincosf(a0, &s0, &c0);
+          sincosf(a0 + W, &s1, &c1);
+          e0x = c0;
+          e0y = s0;
+          e1x = c1;
+          e1y = s1;
+          amode = W < 3.14159f ? 1 : 2;
+        }
+      }
+      return;
+    }
     uint64_t r = ~occ;
     r &= (r << 1) | (r >> 63);
     r &= (r << 2) | (r >> 62);
@@ -504,8 +614,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     int nocc;
     uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
     if (nocc >= 2)
-      surrounded = (EXACT || !fast || a.fp32Only) ? gap < (uint32_t)WB_DEG144
-                                                  : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+      surrounded = gap < (uint32_t)WB_DEG144;
   };
   auto decide = [&]() {
 #ifdef WB_CLASSIFY_STATS
@@ -547,7 +656,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       {
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        if (column(__shfl_sync(0xffffffffu, c, src)))
+        const uint64_t cc = __shfl_sync(0xffffffffu, c, src);
+        if (arcWants(a.col[2 * cc]) && column(cc))
           decide();
       }
     }
@@ -586,7 +696,10 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       {
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        int bi = __shfl_sync(0xffffffffu, SI, src) * S, bj = __shfl_sync(0xffffffffu, SJ, src) * S;
+        const int SIs = __shfl_sync(0xffffffffu, SI, src), SJs = __shfl_sync(0xffffffffu, SJ, src);
+        if (!arcWants(a.super[2 * ((uint64_t)SJs * a.snx + SIs)]))
+          continue;
+        int bi = SIs * S, bj = SJs * S;
         // lanes 0..S*S-1 take the block's columns
         uint64_t c = 0;
         bool cok = false;
@@ -607,7 +720,9 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         {
           int cs = __ffs(cm) - 1;
           cm &= cm - 1;
-          gotAny |= column(__shfl_sync(0xffffffffu, c, cs));
+          const uint64_t cc = __shfl_sync(0xffffffffu, c, cs);
+          if (arcWants(a.col[2 * cc]))
+            gotAny |= column(cc);
         }
         if (gotAny)
           decide();
@@ -671,7 +786,57 @@ struct GroupSmem
 {
   int4 cand[32];
   uint32_t bmin[kGroupBins][32], bmax[kGroupBins][32];
+  /* each lane's open arc of directions that can still change its decision:
+     rays e0 = (ex0, ey0) and e1 = (ex1, ey1), widened beyond the gap's ends;
+     amode 0: every direction counts, 1: the wedge from e0 to e1
+     counter-clockwise (narrower than a half turn), 2: everything except the
+     wedge from e1 to e0 */
+  float ex0[32], ey0[32], ex1[32], ey1[32];
+  int amode[32];
 };
+
+
+/* Can a box {x0 <= x <= x1, y0 <= y <= y1} (metres from the point) hold a
+ * direction inside the lane's arc?  The largest (smallest) value of a linear
+ * form over a box is the sum of its two per-axis extremes. */
+__device__ __forceinline__ bool arcMeetsBox(const GroupSmem &sm, int lane, float x0, float x1, float y0, float y1)
+{
+  const int m = sm.amode[lane];
+  if (m == 0)
+    return true;
+  const float e0x = sm.ex0[lane], e0y = sm.ey0[lane], e1x = sm.ex1[lane], e1y = sm.ey1[lane];
+  if (m == 1)
+  {
+    const float A = fmaxf(e0x * y0, e0x * y1) + fmaxf(-e0y * x0, -e0y * x1);   // max cross(e0, c)
+    const float B = fmaxf(e1y * x0, e1y * x1) + fmaxf(-e1x * y0, -e1x * y1);   // max cross(c, e1)
+    const float bx = e0x + e1x, by = e0y + e1y;                                // the wedge's bisector
+    const float D = fmaxf(bx * x0, bx * x1) + fmaxf(by * y0, by * y1);
+    return A >= 0.f && B >= 0.f && D >= 0.f;
+  }
+  const float A = fminf(e1x * y0, e1x * y1) + fminf(-e1y * x0, -e1y * x1);     // min cross(e1, c)
+  const float B = fminf(e0y * x0, e0y * x1) + fminf(-e0x * y0, -e0x * y1);     // min cross(c, e0)
+  return !(A > 0.f && B > 0.f);   // the box lies inside the complement wedge from e1 to e0
+}
+
+/* The lane's arc from its largest gap (u0 counter-clockwise over w units). */
+__device__ __forceinline__ void setArc(GroupSmem &sm, int lane, uint32_t u0, uint32_t w)
+{
+  const float a0 = (float)u0 * kUnitRad - kArcPad;
+  const float W = (float)w * kUnitRad + 2.f * kArcPad;
+  if (!(W < 6.2f))
+  {
+    sm.amode[lane] = 0;
+    return;
+  }
+  float s0, c0, s1, c1;
+  sincosf(a0, &s0, &c0);
+  sincosf(a0 + W, &s1, &c1);
+  sm.ex0[lane] = c0;
+  sm.ey0[lane] = s0;
+  sm.ex1[lane] = c1;
+  sm.ey1[lane] = s1;
+  sm.amode[lane] = W < 3.14159f ? 1 : 2;
+}
 
 __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int lane, GroupSmem &sm)
 {
@@ -721,6 +886,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       sm.bmin[b][lane] = 0xffffffffu;
       sm.bmax[b][lane] = 0;
     }
+    sm.amode[lane] = 0;
     unsigned occ = 0;
     bool done = !act;
     // The envelope of the lanes still undecided: highest apex above oz,
@@ -772,19 +938,46 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       float dz = (apex - need + 1e-4f * (fabsf(apex) + need) + 1e-6f) / sz + 2.f;
       return dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
     };
-    // the lane's surround test from its bins
+    // the lane's surround test from its bins.  A gap below the decision
+    // threshold can never decide the lane, so directions that can only fall
+    // into such gaps change nothing: when one gap alone is wide enough to
+    // matter, the lane's arc is that gap, and boxes outside it are skipped.
     auto decideLane = [&](uint32_t &worst) -> bool {
       worst = 0;
       if (__popc(occ) < 2)
         return false;
+      const uint32_t thr = a.fp32Only ? (uint32_t)WB_DEG144 : (uint32_t)WB_DEG144 - 2 * kMargin;
+      uint32_t g0 = 0, gw = 0;
+      int nbig = 0;
       for (int b = 0; b < kGroupBins; b++)
         if ((occ >> b) & 1)
         {
           unsigned rest = occ >> (b + 1);
           int nb = rest ? b + __ffs(rest) : __ffs(occ) - 1;
-          worst = max(worst, (sm.bmin[nb][lane] - sm.bmax[b][lane]) & 0x7fffffffu);
+          const uint32_t u0 = sm.bmax[b][lane];
+          const uint32_t gap = (sm.bmin[nb][lane] - u0) & 0x7fffffffu;
+          worst = max(worst, gap);
+          if (gap >= thr)
+          {
+            nbig++;
+            g0 = u0;
+            gw = gap;
+          }
         }
-      return a.fp32Only ? worst < (uint32_t)WB_DEG144 : worst + 2 * kMargin < (uint32_t)WB_DEG144;
+      const bool dec = a.fp32Only ? worst < (uint32_t)WB_DEG144 : worst + 2 * kMargin < (uint32_t)WB_DEG144;
+      if (!dec && nbig == 1)
+        setArc(sm, lane, g0, gw);
+      else
+        sm.amode[lane] = 0;
+      return dec;
+    };
+    // whether any undecided lane's arc meets a box (record integers)
+    auto boxWanted = [&](const int4 &b) -> bool {
+      bool want = false;
+      if (!done)
+        want = arcMeetsBox(sm, lane, (float)(b.x - me.x) * sx, (float)(b.z - me.x) * sx, (float)(b.y - me.y) * sy,
+                           (float)(b.w - me.y) * sy);
+      return __any_sync(0xffffffffu, want);
     };
     // reads column cc's candidates below the envelope's height bound, each
     // tested by every lane still undecided
@@ -931,7 +1124,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       {
         const int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        scanColumn(__shfl_sync(0xffffffffu, c, src));
+        const uint64_t cc = __shfl_sync(0xffffffffu, c, src);
+        if (boxWanted(a.col[2 * cc]))
+          scanColumn(cc);
       }
     }
     // far field: rings of super-cells, then their columns outside the near field
@@ -964,7 +1159,10 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         {
           const int src = __ffs(mask) - 1;
           mask &= mask - 1;
-          const int bi = __shfl_sync(0xffffffffu, SI, src) * S, bj = __shfl_sync(0xffffffffu, SJ, src) * S;
+          const int SIs = __shfl_sync(0xffffffffu, SI, src), SJs = __shfl_sync(0xffffffffu, SJ, src);
+          if (!boxWanted(a.super[2 * ((uint64_t)SJs * a.snx + SIs)]))
+            continue;
+          const int bi = SIs * S, bj = SJs * S;
           uint64_t c = 0;
           bool cok = false;
           if (lane < S * S)
@@ -981,7 +1179,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           {
             const int cs = __ffs(cm) - 1;
             cm &= cm - 1;
-            scanColumn(__shfl_sync(0xffffffffu, c, cs));
+            const uint64_t cc = __shfl_sync(0xffffffffu, c, cs);
+            if (boxWanted(a.col[2 * cc]))
+              scanColumn(cc);
           }
         }
       }
