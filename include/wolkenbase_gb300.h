@@ -165,6 +165,38 @@ int wb_octree_find_block(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *le
 #define WB_FIND_BLOCK_STATIC_MAX 65536
 int wb_octree_find_block_static(wb_ctx *ctx, const double *xyz, uint64_t m, int64_t *leaf);
 
+/* A shape of the neighbourhood queries, as the reference constructs them:
+ * WB_SHAPE_CYLINDER    Cylinder(xy c, double r) (shape.cpp:207-218):
+ *                      v[0], v[1] = c, r = radius (any height)
+ * WB_SHAPE_HYPERBOLOID Hyperboloid(xyz v, double r, double s) (shape.cpp:
+ *                      119-135): vertex v, radius of curvature r, slope s
+ *                      (s > 0 opens downward, as classifyCylinder uses it) */
+#define WB_SHAPE_CYLINDER 1
+#define WB_SHAPE_HYPERBOLOID 2
+typedef struct
+{
+  int kind;
+  int pad;
+  double v[3];
+  double r, s;
+} wb_shape;
+
+/* Octree::findBlocks (octree.cpp:234-251): the leaves whose cube the shape
+ * intersects, depth-first (the leaf numbering).  *count receives how many;
+ * WB_EINVAL when that exceeds capacity (nothing written).  Synchronous. */
+int wb_find_blocks(wb_ctx *ctx, const wb_shape *shape, int64_t *leaves, uint64_t capacity, uint64_t *count);
+
+/* OctStore::pointsIn (octree.cpp:1214-1242): the stored points the shape
+ * holds -- every point of a block whose cube's eight corners are inside,
+ * the points inside for the other blocks findBlocks returns -- as input
+ * record indices (the surviving record of a duplicated location), blocks
+ * depth-first and store order inside a block; sorted != 0 orders them by
+ * height (ties keep that order; the reference's std::sort leaves them in no
+ * particular order).  *count receives how many; WB_EINVAL when that exceeds
+ * capacity (nothing written).  Synchronous. */
+int wb_points_in(wb_ctx *ctx, const wb_shape *shape, int sorted, uint32_t *records, uint64_t capacity,
+                 uint64_t *count);
+
 /* scanCylinder over every tile then postscanCylinder over every tile
  * (scan.cpp:31-179), in flowsnake order. */
 int wb_scan_tiles(wb_ctx *ctx, const wb_params *params);
@@ -177,6 +209,19 @@ int wb_tiles(wb_ctx *ctx, wb_tile *out, uint64_t capacity, uint64_t *count);
  * order that contains it; other bytes are left unchanged.  cls may be a host
  * or (cls_on_device=1) a device pointer. */
 int wb_classify(wb_ctx *ctx, const wb_params *params, uint8_t *cls, int cls_on_device);
+
+/* wb_classify plus each point's decision margin (the margin_out of the
+ * classify entry point): margin[i] (per input record, on the side of cls)
+ * is, in degrees, the largest circular gap between the directions of the
+ * point's hyperboloid neighbours minus 144 (surround, classify.cpp:67-94):
+ * negative for class 1, positive for class 2, 216 when fewer than two
+ * directions exist, NaN for a record no tile cylinder holds.  A point proven
+ * surrounded before all its neighbours were seen reports the gap at that
+ * moment (the full set's gap is no larger, so its true margin is at least as
+ * far from zero).  Gaps decided by the FP32 filter carry its direction error,
+ * below 3.5e-4 degrees; ambiguous points are re-run with exact directions.
+ * margin may be NULL (then this is wb_classify). */
+int wb_classify_ex(wb_ctx *ctx, const wb_params *params, uint8_t *cls, int cls_on_device, float *margin);
 
 /* Build + scan + postscan + classify in one call. */
 int wb_classify_cloud(wb_ctx *ctx, const wb_cloud *cloud, const wb_params *params, uint8_t *cls);

@@ -35,7 +35,7 @@ class RunIO(C.Structure):
                 ("snake_index", C.c_int),
                 ("t_build", C.c_double), ("t_scan", C.c_double), ("t_postscan", C.c_double),
                 ("t_classify", C.c_double), ("sample_tiles", C.POINTER(C.c_int64)), ("n_sample", C.c_uint64),
-                ("n_scanned", C.c_uint64), ("n_sample_points", C.c_uint64)]
+                ("n_scanned", C.c_uint64), ("n_sample_points", C.c_uint64), ("margin", C.POINTER(C.c_double))]
 
 
 TILE_DTYPE = np.dtype([("ex", "<i4"), ("ey", "<i4"), ("n_points", "<i4"), ("n_ground", "<i4"),
@@ -76,6 +76,10 @@ def lib():
         L.wbo_flowsnake_limits.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
         L.wbo_sample.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]
+        L.wbo_points_in.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_uint64]
+        L.wbo_points_in.restype = C.c_int64
+        L.wbo_find_blocks.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_uint64]
+        L.wbo_find_blocks.restype = C.c_int64
         L.wbo_snake_tiles.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double]
         L.wbo_snake_tiles.restype = C.c_int64
         _lib = L
@@ -94,7 +98,8 @@ def _ptr(a, ct):
 
 
 def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
-        phases=3, canonical_order=False, threads=1, sample_tiles=None, want_leaves=True, keep=False):
+        phases=3, canonical_order=False, threads=1, sample_tiles=None, want_leaves=True, keep=False,
+        margins=False):
     """Runs the restated pipeline; returns a dict of numpy arrays and scalars.
 
     sample_tiles: positions in flowsnake order of the only tiles to post-scan
@@ -124,6 +129,10 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
     io.block_pos = _ptr(pos, C.c_int32)
     io.leaf = _ptr(leaf, C.c_int64)
     io.cls = _ptr(cls, C.c_uint8)
+    margin = None
+    if margins:
+        margin = np.zeros(n, np.float64)
+        io.margin = _ptr(margin, C.c_double)
     if sample_tiles is not None:
         smp = np.ascontiguousarray(sample_tiles, dtype=np.int64)
         io.sample_tiles = _ptr(smp, C.c_int64)
@@ -146,7 +155,7 @@ def run(cloud, *, tile_size=1.0, max_slope=1.0, thickness=0.0, min_hyp_size=0.1,
                snake_center=tuple(io.snake_center), snake_side=io.snake_side, spacing=io.spacing,
                snake_index=io.snake_index,
                t_build=io.t_build, t_scan=io.t_scan, t_postscan=io.t_postscan, t_classify=io.t_classify,
-               n_scanned=io.n_scanned, n_sample_points=io.n_sample_points)
+               n_scanned=io.n_scanned, n_sample_points=io.n_sample_points, margin=margin)
     if not keep:
         L.wbo_reset()
     return out
@@ -173,6 +182,26 @@ def sample_tiles_fields(n_tiles):
     tiles = np.zeros(n_tiles, TILE_DTYPE)
     lib().wbo_tiles(tiles.ctypes.data)
     return tiles
+
+
+def points_in(kind, v, r, s=1.0, sorted=False):
+    """OctStore::pointsIn over the octree a run(keep=True) left (input indices)."""
+    L = lib()
+    vv = np.ascontiguousarray(list(v) + [0.0] * (3 - len(v)), np.float64)
+    n = L.wbo_points_in(kind, vv.ctypes.data, r, s, int(sorted), None, 0)
+    out = np.zeros(max(n, 0), np.uint32)
+    L.wbo_points_in(kind, vv.ctypes.data, r, s, int(sorted), out.ctypes.data, out.shape[0])
+    return out
+
+
+def find_blocks(kind, v, r, s=1.0):
+    """Octree::findBlocks over the octree a run(keep=True) left (depth-first leaf indices)."""
+    L = lib()
+    vv = np.ascontiguousarray(list(v) + [0.0] * (3 - len(v)), np.float64)
+    n = L.wbo_find_blocks(kind, vv.ctypes.data, r, s, None, 0)
+    out = np.zeros(max(n, 0), np.int64)
+    L.wbo_find_blocks(kind, vv.ctypes.data, r, s, out.ctypes.data, out.shape[0])
+    return out
 
 
 def reset():

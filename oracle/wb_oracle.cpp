@@ -953,8 +953,28 @@ struct Pipeline
     return ret;
   }
 
-  /* classifyCylinder (classify.cpp:96-173): labels are returned, not stored */
-  void classifyTile(size_t k, std::vector<std::pair<uint32_t, uint8_t>> &res, int &nGround) const
+  /* Largest circular gap of a direction set (0 and twoDirs false below two). */
+  static uint32_t largestGap(const std::set<int> &dirs, bool &twoDirs)
+  {
+    twoDirs = dirs.size() >= 2;
+    if (!twoDirs)
+      return 0;
+    uint32_t worst = 0;
+    int prev = *dirs.rbegin();
+    for (int d : dirs)
+    {
+      worst = std::max(worst, ((uint32_t)d - (uint32_t)prev) & (uint32_t)INT_MAX);
+      prev = d;
+    }
+    return worst;
+  }
+
+  /* classifyCylinder (classify.cpp:96-173): labels are returned, not stored;
+     gaps (optional) receives each point's largest direction gap at the end of
+     its loop (for a point that is not surrounded, that of all its neighbours)
+     in degrees minus 144, 216 with fewer than two directions */
+  void classifyTile(size_t k, std::vector<std::pair<uint32_t, uint8_t>> &res, int &nGround,
+                    std::vector<double> *gaps = nullptr) const
   {
     CylinderR cyl = snake.cyl(order[k]);
     std::vector<uint32_t> cp;
@@ -991,6 +1011,12 @@ struct Pipeline
           above = true;
       }
       res.push_back({id, (uint8_t)(above ? 1 : 2)});
+      if (gaps)
+      {
+        bool two;
+        uint32_t g = largestGap(dirs, two);
+        gaps->push_back(two ? ((double)g - (double)kDeg144) * (360.0 / 2147483648.0) : 216.0);
+      }
       if (!above)
         nGround++;
     }
@@ -1207,11 +1233,19 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
     std::vector<std::atomic<int64_t>> best(n);
     for (uint64_t i = 0; i < n; i++)
       best[i].store(-1);
+    if (io->margin)
+      for (uint64_t i = 0; i < n; i++)
+        io->margin[i] = NAN;
     parallelFor(P.order.size(), thr, [&](size_t k) {
       std::vector<std::pair<uint32_t, uint8_t>> res;
+      std::vector<double> gaps;
       int ng = 0;
-      P.classifyTile(k, res, ng);
+      P.classifyTile(k, res, ng, io->margin ? &gaps : nullptr);
       P.tiles[k].nGround = ng;
+      if (io->margin)
+        for (size_t q = 0; q < res.size(); q++)
+          if (ownsPoint(P, k, P.st.loc[res[q].first]))
+            io->margin[res[q].first] = gaps[q];
       for (auto &r : res)
       {
         int64_t v = ((int64_t)k << 8) | r.second;
@@ -1262,6 +1296,48 @@ int wbo_sample(const int64_t *tiles, uint64_t count, int threads, uint8_t *cls, 
   if (n_points)
     *n_points = so.nPoints;
   return 0;
+}
+
+int64_t wbo_points_in(int kind, const double *v, double r, double s, int sorted, uint32_t *out, uint64_t capacity)
+{
+  if (!gPipe)
+    return -1;
+  std::vector<uint32_t> ids;
+  if (kind == 1)
+    gPipe->st.pointsIn(CylinderR(v[0], v[1], r), ids);
+  else if (kind == 2)
+    gPipe->st.pointsIn(HyperboloidR(V3{v[0], v[1], v[2]}, r, s), ids);
+  else
+    return -1;
+  if (sorted)   // stable: equal heights keep the unsorted order
+    std::stable_sort(ids.begin(), ids.end(),
+                     [&](uint32_t a, uint32_t b) { return gPipe->st.loc[a].z < gPipe->st.loc[b].z; });
+  for (size_t i = 0; i < ids.size() && i < capacity; i++)
+    out[i] = ids[i];
+  return (int64_t)ids.size();
+}
+
+int64_t wbo_find_blocks(int kind, const double *v, double r, double s, int64_t *out, uint64_t capacity)
+{
+  if (!gPipe)
+    return -1;
+  std::vector<std::pair<CubeR, int64_t>> leaves;
+  gPipe->st.dfsLeaves(0, leaves);
+  std::vector<int64_t> leafOfBlock(gPipe->st.blocks.size(), -1);
+  for (size_t i = 0; i < leaves.size(); i++)
+    leafOfBlock[leaves[i].second] = (int64_t)i;
+  std::vector<int64_t> bl;
+  const Store &st = gPipe->st;
+  CubeR root{st.nodes[0].c, st.nodes[0].side};
+  if (kind == 1)
+    st.findBlocks(0, CylinderR(v[0], v[1], r), root, bl);
+  else if (kind == 2)
+    st.findBlocks(0, HyperboloidR(V3{v[0], v[1], v[2]}, r, s), root, bl);
+  else
+    return -1;
+  for (size_t i = 0; i < bl.size() && i < capacity; i++)
+    out[i] = leafOfBlock[bl[i]];
+  return (int64_t)bl.size();
 }
 
 int64_t wbo_snake_tiles(const double *minc, const double *maxc, double unit, double tile_size)

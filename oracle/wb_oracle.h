@@ -60,6 +60,9 @@ typedef struct
   uint64_t n_sample;
   uint64_t n_scanned;      /* tiles scanned (sampled run: the sample plus what postscan needed) */
   uint64_t n_sample_points;   /* points in the sampled tiles' cylinders (classified, overlaps counted) */
+  double *margin;          /* full run, optional (n): the deciding tile's largest direction gap of
+                              each point at the end of its loop, in degrees minus 144 (216 with
+                              fewer than two directions; NaN for points no tile holds) */
 } wbo_run_io;
 
 /* Whole pipeline; returns 0 on success. */
@@ -80,6 +83,14 @@ int wbo_tiles(wbo_tile *out /* n_tiles */);
  * octree, from a fresh tile table; cls has one entry per input point. */
 int wbo_sample(const int64_t *tiles, uint64_t count, int threads, uint8_t *cls, double *t_scan, double *t_classify,
                uint64_t *n_scanned, uint64_t *n_points);
+
+/* After wbo_run(keep): OctStore::pointsIn of a Cylinder (kind 1: v[0], v[1],
+ * radius r) or a Hyperboloid (kind 2: vertex v, r, slope s) as input point
+ * indices (sorted: by height, ties in unsorted order), and Octree::findBlocks
+ * as depth-first leaf indices; each returns the full count (at most capacity
+ * entries written), -1 on error. */
+int64_t wbo_points_in(int kind, const double *v, double r, double s, int sorted, uint32_t *out, uint64_t capacity);
+int64_t wbo_find_blocks(int kind, const double *v, double r, double s, int64_t *out, uint64_t capacity);
 
 /* Tiles of the flowsnake island Flowsnake::setSize picks for a cloud with
  * these header corners (file units) and tile size. */

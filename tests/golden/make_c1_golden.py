@@ -56,7 +56,7 @@ def main():
     if not os.path.exists(O.REF_BIN):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     cloud = synth.plain_small(seed=1)
-    raw = args.raw or os.path.join(ROOT, "_work", "c1_raw")
+    raw = args.raw or os.path.join(ROOT, "_work", "big", "c1_raw")
     os.makedirs(raw, exist_ok=True)
     inp = os.path.join(raw, "in.wbxyz")
     out = os.path.join(raw, "ref.out")

@@ -91,12 +91,31 @@ def test_las_output_settings_reach_the_struct():
     assert wb.LasOutput().c().software is None
 
 
-def test_bench_crop_and_single_rank_max():
+def test_bench_tile_sample_estimate_and_single_rank_max():
     import bench
-    from wolkenbase_gb300 import synth
-    cloud = synth.density_tile(20_000, 3)
-    sub, side = bench.crop(cloud, 5_000)
-    d = sub.decoded()
-    assert 0 < sub.n < cloud.n
-    assert (d[:, 0].max() - d[:, 0].min()) <= side + 1e-6 and (d[:, 1].max() - d[:, 1].min()) <= side + 1e-6
+    t = bench.sample_tiles(1000, 0.01, 7)
+    assert t.shape[0] == 10 and np.all(np.diff(t) > 0) and t.min() >= 0 and t.max() < 1000
+    assert np.array_equal(t, bench.sample_tiles(1000, 0.01, 7))
+    # build time plus the sample's scan time scaled by scanned tiles and its classify time by sampled tiles
+    est = bench.oracle_estimate(2.0, {"t_scan": 0.5, "t_classify": 3.0, "n_scanned": 50}, 1000, 10)
+    assert abs(est - (2.0 + 0.5 * 1000 / 50 + 3.0 * 1000 / 10)) < 1e-9
     assert bench.max_over_ranks(3.5, "cpu") == 3.5
+
+
+def test_bench_oracle_baseline_parity_on_a_small_cloud():
+    """The CPU baseline's parity check, run against the oracle's own full
+    answers: every count agrees and the agreement is 1."""
+    import bench
+    from oracle import oracle as O
+    from wolkenbase_gb300 import synth
+    cloud = synth.density_tile(12_000, 5)
+    full = O.run(cloud, canonical_order=True, threads=4)
+    tiles = full["tiles"]
+    gpu = {"n_leaves": full["n_leaves"], "leaves": full["leaves"], "count": full["leaf_count"].astype(np.uint32),
+           "pleaf": np.maximum(full["leaf"], 0).astype(np.uint32), "cls": full["cls"],
+           "tiles": {"n_points": tiles["n_points"], "tree_flags": tiles["tree_flags"], "density": tiles["density"],
+                     "h_scan": tiles["h_scan"], "hyperboloid_size": tiles["h_final"], "height": tiles["height"]}}
+    base, parity = bench.oracle_baseline(cloud, 4, 0.2, 3, gpu)
+    assert base["value"] > 0 and base["kind"] == "port"
+    assert parity["octree_exact"] and parity["sampled_tiles_exact"] == parity["sampled_tiles"]
+    assert parity["sampled_labels"] > 0 and parity["agreement"] == 1.0

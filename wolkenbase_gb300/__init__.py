@@ -147,6 +147,43 @@ class Classifier:
         self._check(self.L.wb_octree_find_block(self.ctx, xyz.ctypes.data, xyz.shape[0], out.ctypes.data))
         return out
 
+    @staticmethod
+    def _shape(kind, v, r, s):
+        sh = _lib.wb_shape()
+        sh.kind = int(kind)
+        vv = list(v) + [0.0] * (3 - len(v))
+        sh.v[:] = vv[:3]
+        sh.r = float(r)
+        sh.s = float(s)
+        return sh
+
+    def find_blocks(self, kind, v, r, s=1.0):
+        """Octree::findBlocks of a Cylinder (kind WB_SHAPE_CYLINDER: v = centre xy,
+        r = radius) or a Hyperboloid (WB_SHAPE_HYPERBOLOID: vertex v, r, slope s):
+        depth-first leaf indices."""
+        sh = self._shape(kind, v, r, s)
+        n = C.c_uint64(0)
+        rc = self.L.wb_find_blocks(self.ctx, C.byref(sh), None, 0, C.byref(n))
+        if rc not in (0, _lib.WB_EINVAL) or (rc == _lib.WB_EINVAL and n.value == 0):
+            self._check(rc)
+        out = np.zeros(n.value, np.int64)
+        self._check(self.L.wb_find_blocks(self.ctx, C.byref(sh), out.ctypes.data, out.shape[0], C.byref(n)))
+        return out
+
+    def points_in(self, kind, v, r, s=1.0, sorted=False):
+        """OctStore::pointsIn of a Cylinder or a Hyperboloid (see find_blocks):
+        input record indices, blocks depth-first, store order inside a block,
+        or by height when sorted."""
+        sh = self._shape(kind, v, r, s)
+        n = C.c_uint64(0)
+        rc = self.L.wb_points_in(self.ctx, C.byref(sh), int(sorted), None, 0, C.byref(n))
+        if rc not in (0, _lib.WB_EINVAL) or (rc == _lib.WB_EINVAL and n.value == 0):
+            self._check(rc)
+        out = np.zeros(n.value, np.uint32)
+        self._check(self.L.wb_points_in(self.ctx, C.byref(sh), int(sorted), out.ctypes.data, out.shape[0],
+                                        C.byref(n)))
+        return out
+
     # -- tiles --
     def scan(self, params=None):
         p = (params or Params()).c()
@@ -168,6 +205,18 @@ class Classifier:
         p = (params or Params()).c()
         self._check(self.L.wb_classify(self.ctx, C.byref(p), cls.ctypes.data, 0))
         return cls
+
+    def classify_margins(self, params=None, cls=None):
+        """classify() plus every record's decision margin in degrees (largest
+        direction gap minus 144; negative = not ground, NaN = in no tile)."""
+        n = self.info()["n_points"]
+        if cls is None:
+            cls = np.zeros(n, np.uint8)
+        cls = np.ascontiguousarray(cls, dtype=np.uint8)
+        margin = np.zeros(n, np.float32)
+        p = (params or Params()).c()
+        self._check(self.L.wb_classify_ex(self.ctx, C.byref(p), cls.ctypes.data, 0, margin.ctypes.data))
+        return cls, margin
 
     def classify_cloud(self, cloud, params=None, cls=None):
         """Build + scan + postscan + classify in one C call (host in, host out)."""

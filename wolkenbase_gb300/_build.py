@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwolkenbase_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["wb_abi.cu", "wb_prims.cu", "wb_build.cu", "wb_tiles.cu", "wb_classify.cu", "wb_grid.cu", "wb_geom.cpp", "wb_serve.cpp", "wb_las.cu", "wb_lasio.cu"]
+SOURCES = ["wb_abi.cu", "wb_prims.cu", "wb_build.cu", "wb_tiles.cu", "wb_classify.cu", "wb_grid.cu", "wb_geom.cpp", "wb_serve.cpp", "wb_las.cu", "wb_lasio.cu", "wb_query.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -48,6 +48,11 @@ class wb_tile(C.Structure):
 
 
 WB_N_SHAPES = 8
+WB_SHAPE_CYLINDER, WB_SHAPE_HYPERBOLOID = 1, 2
+
+
+class wb_shape(C.Structure):
+    _fields_ = [("kind", C.c_int), ("pad", C.c_int), ("v", C.c_double * 3), ("r", C.c_double), ("s", C.c_double)]
 
 
 class wb_tuning(C.Structure):
@@ -123,6 +128,9 @@ SIGNATURES = {
     "wb_octree_store_order": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wb_octree_find_block": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_octree_find_block_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_classify_ex": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "wb_find_blocks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wb_points_in": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.c_void_p]),
     "wb_scan_tiles": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
     "wb_tiles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wb_classify": (C.c_int, [C.c_void_p, C.POINTER(wb_params), C.c_void_p, C.c_int]),

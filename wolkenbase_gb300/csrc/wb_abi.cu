@@ -125,7 +125,8 @@ void wb_release_buffers(wb_ctx *c)
                    &c->tileHuge, &c->hugePre,
                    &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->deferred, &c->angleT,
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
-                   &c->gpt, &c->cellRec, &c->superRec, &c->ptSetup, &c->groups, &c->groupCnt, &c->lasAngles};
+                   &c->gpt, &c->cellRec, &c->superRec, &c->ptSetup, &c->groups, &c->groupCnt, &c->lasAngles,
+                   &c->marginBuf, &c->marginRec};
   for (DevBuf *b : all)
     wb_free_buf(c, *b);
   c->used = 0;
@@ -493,6 +494,27 @@ int wb_classify(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
       rc = wb_fail(c, WB_ECUDA, std::string("wb_classify: ") + cudaGetErrorString(e));
   }
   endRun(c);
+  return rc;
+}
+
+int wb_classify_ex(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice, float *margin)
+{
+  if (!c || !p)
+    return WB_EINVAL;
+  WbDeviceGuard deviceGuard(c->device);
+  if (margin && onDevice && c->n && !wb_device_accessible(margin))
+    return wb_fail(c, WB_EINVAL, "wb_classify_ex: device margins must be device memory");
+  c->marginDst = margin;
+  beginRun(c);
+  int rc = wb_classify_impl(c, p, cls, onDevice);
+  if (rc == 0 && !onDevice)
+  {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+      rc = wb_fail(c, WB_ECUDA, std::string("wb_classify_ex: ") + cudaGetErrorString(e));
+  }
+  endRun(c);
+  c->marginDst = nullptr;
   return rc;
 }
 

@@ -139,7 +139,18 @@ struct ClsArgs
   uint64_t n, nTiles;
   const uint32_t *storeOf;
   uint8_t *cls;
+  /* decision margins (wb_classify_ex): per store position, and per record */
+  float *margin, *marginOut;
 };
+
+/* Decision margin of a point in degrees: the largest gap between its
+ * neighbours' directions minus 144 degrees (negative: surrounded, not
+ * ground); with fewer than two directions there is no gap to speak of and
+ * the point is ground by 216 degrees. */
+__device__ __forceinline__ float marginDeg(uint32_t gap, bool twoDirs)
+{
+  return twoDirs ? (float)((double)gap - (double)WB_DEG144) * (float)(360.0 / 2147483648.0) : 216.f;
+}
 
 __device__ __forceinline__ double decA(const ClsArgs &a, int ax, int32_t q)
 {
@@ -203,12 +214,10 @@ __device__ __noinline__ bool memberExact(const ClsArgs &a, const HypExact &h, ui
 /* Can any point of a box (integer bounds, 6 planes of N entries) be inside?
  * FP32 with generous slack.  Record differences are exact in 32 bits: the
  * host checks that the cloud's integer extent fits. */
-__device__ __forceinline__ bool boxMeets(const Hyp &h, const int4 *rec, uint64_t c)
+__device__ __forceinline__ bool boxMeets(const Hyp &h, const int4 &b, int32_t zmin)
 {
-  int4 b = rec[2 * c];
   if (b.x == INT32_MAX)
     return false;   // empty block
-  int32_t zmin = rec[2 * c + 1].x;
   float xl = (float)(b.x - h.qx) * h.sx, xh = (float)(b.z - h.qx) * h.sx;
   float yl = (float)(b.y - h.qy) * h.sy, yh = (float)(b.w - h.qy) * h.sy;
   float zd = (float)(h.qz - zmin) * h.sz + h.czp;
@@ -370,7 +379,11 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   if (k < 0)
   {
     if (lane == 0)
+    {
       a.label[j] = 0;
+      if (a.margin)
+        a.margin[j] = __int_as_float(0x7fc00000);
+    }
     return;
   }
   Hyp h;
@@ -403,13 +416,20 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   // Directions are kept as exact per-bin extremes in shared memory plus a
   // 64-bit occupancy mask in registers (uniform across the warp).
   uint32_t occLo = 0, occHi = 0;
+  uint32_t gapNow = 0;   // the largest gap at the last surround test that formed it
+  bool gapValid = false;
   // The fast pass's arc (see setArc): directions outside the one gap that can
   // still decide the point change nothing, so boxes outside it are skipped.
   int amode = 0;
   float e0x = 0.f, e0y = 0.f, e1x = 0.f, e1y = 0.f;
-  auto arcWants = [&](const int4 &b) -> bool {
+  auto arcWants = [&](const int4 &mine, int src) -> bool {
     if (amode == 0)
       return true;
+    int4 b;
+    b.x = __shfl_sync(0xffffffffu, mine.x, src);
+    b.y = __shfl_sync(0xffffffffu, mine.y, src);
+    b.z = __shfl_sync(0xffffffffu, mine.z, src);
+    b.w = __shfl_sync(0xffffffffu, mine.w, src);
     const float x0 = (float)(b.x - h.qx) * h.sx, x1 = (float)(b.z - h.qx) * h.sx;
     const float y0 = (float)(b.y - h.qy) * h.sy, y1 = (float)(b.w - h.qy) * h.sy;
     if (amode == 1)
@@ -581,6 +601,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       uint32_t u0, w;
       const uint32_t thr = a.fp32Only ? (uint32_t)WB_DEG144 : (uint32_t)WB_DEG144 - 2 * kMargin;
       uint32_t gap = largestGapArc(bminW, bmaxW, lane, thr, nocc, nbig, u0, w);
+      gapNow = gap;
+      gapValid = nocc >= 2;
       if (nocc >= 2)
         surrounded = a.fp32Only ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
       amode = 0;
@@ -591,8 +613,9 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         if (W < 6.2f)
         {
           float s0, c0, s1, c1;
-          sincosf(a0, &s0, &c0);
-          sincosf(a0 + W, &s1, &c1);
+          const float a1 = a0 + W;
+          __sincosf(a0 > 3.14159265f ? a0 - 6.28318531f : a0, &s0, &c0);
+          __sincosf(a1 > 3.14159265f ? (a1 > 9.42477796f ? a1 - 12.56637061f : a1 - 6.28318531f) : a1, &s1, &c1);
           e0x = c0;
           e0y = s0;
           e1x = c1;
@@ -613,6 +636,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     __syncwarp();
     int nocc;
     uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
+    gapNow = gap;
+    gapValid = nocc >= 2;
     if (nocc >= 2)
       surrounded = gap < (uint32_t)WB_DEG144;
   };
@@ -640,6 +665,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       int m = m0 + lane;
       uint64_t c = 0;
       bool ok = false;
+      int4 cb = make_int4(0, 0, 0, 0);
       if (m < ncells)
       {
         int di, dj;
@@ -648,7 +674,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
           c = (uint64_t)jj * a.nx + i;
-          ok = boxMeets(h, a.col, c);
+          cb = a.col[2 * c];
+          ok = boxMeets(h, cb, a.col[2 * c + 1].x);
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
@@ -657,7 +684,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
         const uint64_t cc = __shfl_sync(0xffffffffu, c, src);
-        if (arcWants(a.col[2 * cc]) && column(cc))
+        if (arcWants(cb, src) && column(cc))
           decide();
       }
     }
@@ -682,6 +709,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
       int m = m0 + lane;
       int SI = 0, SJ = 0;
       bool ok = false;
+      int4 sb = make_int4(0, 0, 0, 0);
       if (m < nsc)
       {
         int di, dj;
@@ -689,7 +717,11 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         SI = si + di;
         SJ = sj + dj;
         if (SI >= 0 && SI < a.snx && SJ >= 0 && SJ < a.sny)
-          ok = boxMeets(h, a.super, (uint64_t)SJ * a.snx + SI);
+        {
+          const uint64_t sc = (uint64_t)SJ * a.snx + SI;
+          sb = a.super[2 * sc];
+          ok = boxMeets(h, sb, a.super[2 * sc + 1].x);
+        }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
       while (mask && !surrounded)
@@ -697,12 +729,13 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
         int src = __ffs(mask) - 1;
         mask &= mask - 1;
         const int SIs = __shfl_sync(0xffffffffu, SI, src), SJs = __shfl_sync(0xffffffffu, SJ, src);
-        if (!arcWants(a.super[2 * ((uint64_t)SJs * a.snx + SIs)]))
+        if (!arcWants(sb, src))
           continue;
         int bi = SIs * S, bj = SJs * S;
         // lanes 0..S*S-1 take the block's columns
         uint64_t c = 0;
         bool cok = false;
+        int4 cb = make_int4(0, 0, 0, 0);
         if (lane < S * S)
         {
           int i = bi + lane % S, jj = bj + lane / S;
@@ -710,7 +743,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           if (i < a.nx && jj < a.ny && cheb > kNear)
           {
             c = (uint64_t)jj * a.nx + i;
-            cok = boxMeets(h, a.col, c);
+            cb = a.col[2 * c];
+            cok = boxMeets(h, cb, a.col[2 * c + 1].x);
           }
         }
         unsigned cm = __ballot_sync(0xffffffffu, cok);
@@ -721,7 +755,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           int cs = __ffs(cm) - 1;
           cm &= cm - 1;
           const uint64_t cc = __shfl_sync(0xffffffffu, c, cs);
-          if (arcWants(a.col[2 * cc]))
+          if (arcWants(cb, cs))
             gotAny |= column(cc);
         }
         if (gotAny)
@@ -733,12 +767,14 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   const long long tFar = clock64();
   stat[9] += tFar - tNear;
 #endif
-  if (!surrounded && fast && !a.fp32Only)
+  if (!surrounded && ((fast && !a.fp32Only) || a.margin))
   {
     int nocc;
     __syncwarp();
     uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
-    ambiguous = nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
+    ambiguous = fast && !a.fp32Only && nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
+    gapNow = gap;
+    gapValid = nocc >= 2;
   }
 #ifdef WB_CLASSIFY_STATS
   stat[10] += clock64() - tFar;
@@ -754,6 +790,8 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   if (lane == 0)
   {
     a.label[j] = surrounded ? 1 : 2;
+    if (a.margin)
+      a.margin[j] = marginDeg(gapNow, gapValid);
     if (ambiguous)
       a.ambList[atomicAdd(a.ambCount, 1u)] = (uint32_t)j;
   }
@@ -793,6 +831,7 @@ struct GroupSmem
      wedge from e1 to e0 */
   float ex0[32], ey0[32], ex1[32], ey1[32];
   int amode[32];
+  uint32_t gapAt[32];   /* a lane's largest gap when its point was proven surrounded */
 };
 
 
@@ -829,8 +868,10 @@ __device__ __forceinline__ void setArc(GroupSmem &sm, int lane, uint32_t u0, uin
     return;
   }
   float s0, c0, s1, c1;
-  sincosf(a0, &s0, &c0);
-  sincosf(a0 + W, &s1, &c1);
+  // the fast intrinsics are accurate to 4e-7 on [-pi, pi], far inside kArcPad
+  const float a1 = a0 + W;
+  __sincosf(a0 > 3.14159265f ? a0 - 6.28318531f : a0, &s0, &c0);
+  __sincosf(a1 > 3.14159265f ? (a1 > 9.42477796f ? a1 - 12.56637061f : a1 - 6.28318531f) : a1, &s1, &c1);
   sm.ex0[lane] = c0;
   sm.ey0[lane] = s0;
   sm.ex1[lane] = c1;
@@ -863,7 +904,11 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         ps = a.setup[j];
       }
       else
+      {
         a.label[j] = 0;
+        if (a.margin)
+          a.margin[j] = __int_as_float(0x7fc00000);
+      }
     }
     if (!__any_sync(0xffffffffu, act))
       return;
@@ -965,14 +1010,24 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           }
         }
       const bool dec = a.fp32Only ? worst < (uint32_t)WB_DEG144 : worst + 2 * kMargin < (uint32_t)WB_DEG144;
+      if (dec)
+        sm.gapAt[lane] = worst;
       if (!dec && nbig == 1)
         setArc(sm, lane, g0, gw);
       else
         sm.amode[lane] = 0;
       return dec;
     };
-    // whether any undecided lane's arc meets a box (record integers)
-    auto boxWanted = [&](const int4 &b) -> bool {
+    // whether any undecided lane's arc meets the box that lane src holds
+    // (record integers); true at once while no undecided lane has an arc
+    auto boxWanted = [&](const int4 &mine, int src) -> bool {
+      if (!__any_sync(0xffffffffu, !done && sm.amode[lane] != 0))
+        return true;
+      int4 b;
+      b.x = __shfl_sync(0xffffffffu, mine.x, src);
+      b.y = __shfl_sync(0xffffffffu, mine.y, src);
+      b.z = __shfl_sync(0xffffffffu, mine.z, src);
+      b.w = __shfl_sync(0xffffffffu, mine.w, src);
       bool want = false;
       if (!done)
         want = arcMeetsBox(sm, lane, (float)(b.x - me.x) * sx, (float)(b.z - me.x) * sx, (float)(b.y - me.y) * sy,
@@ -1108,6 +1163,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       const int stride = ring == 0 ? 1 : 4 * ring - 1;
       uint64_t c = 0;
       bool ok = false;
+      int4 cb = make_int4(0, 0, 0, 0);
       if (lane < ncells)
       {
         int di, dj;
@@ -1116,7 +1172,8 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         if (i >= 0 && i < a.nx && jj >= 0 && jj < a.ny)
         {
           c = (uint64_t)jj * a.nx + i;
-          ok = envMeets(a.col[2 * c], a.col[2 * c + 1].x);
+          cb = a.col[2 * c];
+          ok = envMeets(cb, a.col[2 * c + 1].x);
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
@@ -1125,7 +1182,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         const int src = __ffs(mask) - 1;
         mask &= mask - 1;
         const uint64_t cc = __shfl_sync(0xffffffffu, c, src);
-        if (boxWanted(a.col[2 * cc]))
+        if (boxWanted(cb, src))
           scanColumn(cc);
       }
     }
@@ -1142,6 +1199,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         const int m = m0 + lane;
         int SI = 0, SJ = 0;
         bool ok = false;
+        int4 sb = make_int4(0, 0, 0, 0);
         if (m < nsc)
         {
           int di, dj;
@@ -1151,7 +1209,8 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           if (SI >= 0 && SI < a.snx && SJ >= 0 && SJ < a.sny)
           {
             const uint64_t sc = (uint64_t)SJ * a.snx + SI;
-            ok = envMeets(a.super[2 * sc], a.super[2 * sc + 1].x);
+            sb = a.super[2 * sc];
+            ok = envMeets(sb, a.super[2 * sc + 1].x);
           }
         }
         unsigned mask = __ballot_sync(0xffffffffu, ok);
@@ -1160,18 +1219,20 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           const int src = __ffs(mask) - 1;
           mask &= mask - 1;
           const int SIs = __shfl_sync(0xffffffffu, SI, src), SJs = __shfl_sync(0xffffffffu, SJ, src);
-          if (!boxWanted(a.super[2 * ((uint64_t)SJs * a.snx + SIs)]))
+          if (!boxWanted(sb, src))
             continue;
           const int bi = SIs * S, bj = SJs * S;
           uint64_t c = 0;
           bool cok = false;
+          int4 cb = make_int4(0, 0, 0, 0);
           if (lane < S * S)
           {
             const int i = bi + lane % S, jj = bj + lane / S;
             if (i < a.nx && jj < a.ny && max(abs(i - ci0), abs(jj - cj0)) > kNearG)
             {
               c = (uint64_t)jj * a.nx + i;
-              cok = envMeets(a.col[2 * c], a.col[2 * c + 1].x);
+              cb = a.col[2 * c];
+              cok = envMeets(cb, a.col[2 * c + 1].x);
             }
           }
           unsigned cm = __ballot_sync(0xffffffffu, cok);
@@ -1180,7 +1241,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
             const int cs = __ffs(cm) - 1;
             cm &= cm - 1;
             const uint64_t cc = __shfl_sync(0xffffffffu, c, cs);
-            if (boxWanted(a.col[2 * cc]))
+            if (boxWanted(cb, cs))
               scanColumn(cc);
           }
         }
@@ -1217,6 +1278,8 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         amb = !a.fp32Only && __popc(occ) >= 2 && worst < (uint32_t)WB_DEG144 + 2 * kMargin;
       }
       a.label[j] = done ? 1 : 2;
+      if (a.margin)
+        a.margin[j] = done ? marginDeg(sm.gapAt[lane], true) : marginDeg(worst, __popc(occ) >= 2);
       if (amb)
         a.ambList[atomicAdd(a.ambCount, 1u)] = j;
     }
@@ -1328,6 +1391,21 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.nTiles = c->n_tiles;
   a.storeOf = (const uint32_t *)c->storeOf.p;
   a.cls = clsDev;
+  a.margin = a.marginOut = nullptr;
+  if (c->marginDst)
+  {
+    if ((rc = wb_ensure(c, c->marginBuf, nd * 4 + 64)))
+      return rc;
+    a.margin = (float *)c->marginBuf.p;
+    if (onDevice)
+      a.marginOut = c->marginDst;
+    else
+    {
+      if ((rc = wb_ensure(c, c->marginRec, n * 4 + 64)))
+        return rc;
+      a.marginOut = (float *)c->marginRec.p;
+    }
+  }
   WB_CUDA(c, cudaMemsetAsync(a.ambCount, 0, 8, c->stream));   // ambiguous and deferred counts
   return 0;
 }
@@ -1550,6 +1628,8 @@ __global__ void batchScatter(const BatchHdr *__restrict__ h)
     uint32_t j = a.storeOf[i];
     if (a.owner[j] >= 0)
       a.cls[i] = a.label[j];
+    if (a.marginOut)
+      a.marginOut[i] = a.owner[j] >= 0 ? a.margin[j] : __int_as_float(0x7fc00000);
   }
 }
 }  // namespace
@@ -1907,6 +1987,8 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   ClsArgs *a = (ClsArgs *)c->clsArgs;
   if (!onDevice && c->n)
     WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDefault, c->stream));
+  if (!onDevice && c->n && a->marginOut)
+    WB_CUDA(c, cudaMemcpyAsync(c->marginDst, a->marginOut, c->n * 4, cudaMemcpyDefault, c->stream));
   wb_mark(c, "cls_download");
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
   wb_batch_collect(b, &c, 1);

@@ -103,6 +103,9 @@ struct wb_ctx
   uint8_t *clsHost = nullptr;       /* host destination of the class bytes, or NULL */
   const uint8_t *clsFinal = nullptr; /* device class bytes of the last classify (per record) */
   uint64_t n_ground = 0;
+  /* wb_classify_ex: where the decision margins go (NULL: not formed) */
+  float *marginDst = nullptr;
+  DevBuf marginBuf, marginRec;
 
   /* profiling */
   bool profile = false;
