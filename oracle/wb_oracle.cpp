@@ -1027,13 +1027,26 @@ struct Pipeline
  * point at p: only the six tiles around k can reach it (a cylinder's radius,
  * 41/71 of the spacing, is below the distance to the second ring minus that
  * radius). */
+/* Whether OctStore::pointsIn(cyl) holds the stored point p (octree.cpp:
+ * 1214-1242): its block must meet the cylinder, and then either the whole
+ * block is taken (all eight corners inside) or the point itself is inside --
+ * which differs from cyl.in(p) only for points outside the root cube. */
+bool tileHolds(const Pipeline &P, size_t k, const V3 &p)
+{
+  const CylinderR cyl = P.snake.cyl(P.order[k]);
+  const CubeR cube = P.st.findCube(p);
+  if (!cyl.meets(cube))
+    return false;
+  return cyl.inCube(cube) || cyl.in(p);
+}
+
 bool ownsPoint(const Pipeline &P, size_t k, const V3 &p)
 {
   static const Eis ring[6] = {{1, 0}, {1, 1}, {0, 1}, {-1, 0}, {-1, -1}, {0, -1}};
   for (const Eis &r : ring)
   {
     auto it = P.addrToK.find(Pipeline::akey(Eis{P.order[k].x + r.x, P.order[k].y + r.y}));
-    if (it != P.addrToK.end() && (size_t)it->second > k && P.snake.cyl(P.order[it->second]).in(p))
+    if (it != P.addrToK.end() && (size_t)it->second > k && tileHolds(P, (size_t)it->second, p))
       return false;
   }
   return true;
@@ -1233,9 +1246,11 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
     std::vector<std::atomic<int64_t>> best(n);
     for (uint64_t i = 0; i < n; i++)
       best[i].store(-1);
-    if (io->margin)
-      for (uint64_t i = 0; i < n; i++)
-        io->margin[i] = NAN;
+    // the margin of the tile that decides each point (the largest flowsnake
+    // position that classified it), packed as (position + 1, float bits)
+    std::vector<std::atomic<uint64_t>> mbest(io->margin ? n : 0);
+    for (auto &m : mbest)
+      m.store(0);
     parallelFor(P.order.size(), thr, [&](size_t k) {
       std::vector<std::pair<uint32_t, uint8_t>> res;
       std::vector<double> gaps;
@@ -1244,8 +1259,17 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
       P.tiles[k].nGround = ng;
       if (io->margin)
         for (size_t q = 0; q < res.size(); q++)
-          if (ownsPoint(P, k, P.st.loc[res[q].first]))
-            io->margin[res[q].first] = gaps[q];
+        {
+          float g = (float)gaps[q];
+          uint32_t bits;
+          memcpy(&bits, &g, 4);
+          uint64_t v = ((uint64_t)(k + 1) << 32) | bits;
+          std::atomic<uint64_t> &slot = mbest[res[q].first];
+          uint64_t cur = slot.load();
+          while (v > cur && !slot.compare_exchange_weak(cur, v))
+          {
+          }
+        }
       for (auto &r : res)
       {
         int64_t v = ((int64_t)k << 8) | r.second;
@@ -1260,6 +1284,15 @@ int wbo_run(wbo_run_io *io, const wbo_params *p)
       for (uint64_t i = 0; i < n; i++)
         if (best[i].load() >= 0)
           io->cls[i] = (uint8_t)(best[i].load() & 0xff);
+    if (io->margin)
+      for (uint64_t i = 0; i < n; i++)
+      {
+        uint64_t v = mbest[i].load();
+        float g;
+        uint32_t bits = (uint32_t)v;
+        memcpy(&g, &bits, 4);
+        io->margin[i] = v ? (double)g : NAN;
+      }
   }
   io->n_blocks = P.st.blocks.size();
   io->n_leaves = leaves.size();

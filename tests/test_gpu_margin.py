@@ -30,5 +30,7 @@ def test_margins_follow_labels_and_oracle(classifier, oracle_mod, case):
     assert np.all(margin[decided & (cls == 1)] < 0)
     assert np.all(margin[decided & (cls == 2)] >= 0)
     ground = decided & (cls == 2)
-    err = np.abs(margin[ground].astype(np.float64) - o["margin"][ground])
-    assert err.max() <= GAP_TOL_DEG, (err.max(), int(np.argmax(err)))
+    idx = np.nonzero(ground)[0]
+    err = np.abs(margin[idx].astype(np.float64) - o["margin"][idx])
+    worst = int(idx[np.argmax(err)])
+    assert err.max() <= GAP_TOL_DEG, (err.max(), worst, float(margin[worst]), float(o["margin"][worst]))

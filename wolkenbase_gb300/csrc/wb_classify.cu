@@ -54,7 +54,9 @@
  * Row 0 is the column-group kernel: 0 groups, 1 columns read, 2 candidates
  * kept, 3 kept x undecided lanes, 4 active lanes, 5 lanes handed over,
  * 6 cycles, 7 super-cell rings, 8 lanes ending ground; 9-11 cycles, count
- * and kept candidates of the groups that kept more than 1000. */
+ * and kept candidates of the groups that kept more than 1000; cycles 12 in
+ * column reads, 13 forming the envelope again, 14 candidate tests, 15
+ * surround tests. */
 #ifdef WB_CLASSIFY_STATS
 __device__ unsigned long long gClassifyStats[3][16];
 extern "C" int wb_classify_stats(unsigned long long *out, int reset)
@@ -914,7 +916,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       return;
 #ifdef WB_CLASSIFY_STATS
     const long long tG = clock64();
-    unsigned long long gst[12] = {0};
+    unsigned long long gst[16] = {0};
 #endif
     if (!a.exactInts)
     {
@@ -1038,6 +1040,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
     // tested by every lane still undecided
     auto scanColumn = [&](uint64_t cc) {
       WB_STAT(gst[1], 1);
+#ifdef WB_CLASSIFY_STATS
+      const long long tCol = clock64();
+#endif
       columnsRead++;
       const int4 box = a.col[2 * cc], r1 = a.col[2 * cc + 1];
       const uint32_t e = (uint32_t)r1.z;
@@ -1105,6 +1110,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         WB_STAT(gst[3], __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)));
         sm.cand[lane] = q;
         __syncwarp();
+#ifdef WB_CLASSIFY_STATS
+        const long long tCand = clock64();
+#endif
         // two candidates per step: independent work for the scheduler
         // Every lane runs the tests (a decided lane's results are dropped), so
         // the warp does not diverge on them; the directions are formed only
@@ -1130,12 +1138,28 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           }
         }
         __syncwarp();
+#ifdef WB_CLASSIFY_STATS
+        gst[14] += clock64() - tCand;
+#endif
       }
+#ifdef WB_CLASSIFY_STATS
+      const long long tDec = clock64();
+#endif
       uint32_t worst;
       if (got && !done)
         done = decideLane(worst);
+#ifdef WB_CLASSIFY_STATS
+      gst[15] += clock64() - tDec;
+#endif
+#ifdef WB_CLASSIFY_STATS
+      const long long tEnv = clock64();
+      gst[12] += tEnv - tCol;
+#endif
       if (__any_sync(0xffffffffu, got))
         envelope();
+#ifdef WB_CLASSIFY_STATS
+      gst[13] += clock64() - tEnv;
+#endif
     };
     // When few lanes remain undecided the warp would run at a fraction of its
     // width, and a group whose neighbourhood is very large would hold one warp
@@ -1264,7 +1288,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         gst[10] = 1;
         gst[11] = gst[2];
       }
-      for (int q = 0; q < 12; q++)
+      for (int q = 0; q < 16; q++)
         atomicAdd(&gClassifyStats[0][q], gst[q]);
     }
 #endif
