@@ -1002,11 +1002,22 @@ struct Pipeline
       }
       if (!above)
         st.pointsIn(hyp, down);
+      // dirsP: the directions of pointsIn(hyp) alone.  The first loop above
+      // can add a point the hyperboloid holds but pointsIn leaves out (one
+      // outside the root cube whose block the shape does not meet) when the
+      // previous point's list had it; the margin reports the pointsIn set's gap.
+      std::set<int> dirsP;
+      const bool secondLoop = !above;
       for (size_t j = 0; j < down.size() && !above; j++)
       {
         const V3 &q = st.loc[down[j]];
         if (hypotR(p.x - q.x, p.y - q.y) != 0)
-          dirs.insert(atan2iR(q.y - p.y, q.x - p.x));
+        {
+          int d = atan2iR(q.y - p.y, q.x - p.x);
+          dirs.insert(d);
+          if (gaps)
+            dirsP.insert(d);
+        }
         if (surround(dirs))
           above = true;
       }
@@ -1014,7 +1025,7 @@ struct Pipeline
       if (gaps)
       {
         bool two;
-        uint32_t g = largestGap(dirs, two);
+        uint32_t g = largestGap(secondLoop && !above ? dirsP : dirs, two);
         gaps->push_back(two ? ((double)g - (double)kDeg144) * (360.0 / 2147483648.0) : 216.0);
       }
       if (!above)
