@@ -126,7 +126,7 @@ void wb_release_buffers(wb_ctx *c)
                    &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->deferred, &c->angleT,
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
                    &c->gpt, &c->cellRec, &c->superRec, &c->ptSetup, &c->groups, &c->groupCnt, &c->lasAngles,
-                   &c->marginBuf, &c->marginRec, &c->sortAux};
+                   &c->marginBuf, &c->marginRec};
   for (DevBuf *b : all)
     wb_free_buf(c, *b);
   c->used = 0;

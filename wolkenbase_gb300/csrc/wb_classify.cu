@@ -498,6 +498,11 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           else
             in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
         }
+        // a direction outside the arc (see arcWants) changes nothing
+        if (in && fast && amode != 0)
+          in = amode == 1 ? (e0x * dy - e0y * dx >= 0.f && dx * e1y - dy * e1x >= 0.f &&
+                             (e0x + e1x) * dx + (e0y + e1y) * dy >= 0.f)
+                          : !(e1x * dy - e1y * dx > 0.f && dx * e0y - dy * e0x > 0.f);
         if (in && fast)
           u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
         else if (in)
@@ -777,6 +782,17 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     ambiguous = fast && !a.fp32Only && nocc >= 2 && gap < (uint32_t)WB_DEG144 + 2 * kMargin;
     gapNow = gap;
     gapValid = nocc >= 2;
+    if (nocc == 1)
+    {
+      // every direction in one bin: the gap is the rest of the circle
+      const bool mine0 = bminW[lane] != 0xffffffffu, mine1 = bminW[lane + 32] != 0xffffffffu;
+      const unsigned who = __ballot_sync(0xffffffffu, mine0 || mine1);
+      const int src = __ffs(who) - 1;
+      const int b = __shfl_sync(0xffffffffu, mine0 ? lane : lane + 32, src);
+      const uint32_t mn = bminW[b], mx = bmaxW[b];
+      gapNow = (mn - mx) & 0x7fffffffu;
+      gapValid = mn != mx;
+    }
   }
 #ifdef WB_CLASSIFY_STATS
   stat[10] += clock64() - tFar;
@@ -1074,6 +1090,17 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
         return in && (dxi != 0 || dyi != 0);
       };
+      // A direction outside the lane's arc lies in a gap too narrow to
+      // decide the point: it changes nothing, so it is not formed or kept.
+      auto arcHolds = [&](float dx, float dy) -> bool {
+        const int am = sm.amode[lane];
+        if (am == 0)
+          return true;
+        const float a0x = sm.ex0[lane], a0y = sm.ey0[lane], a1x = sm.ex1[lane], a1y = sm.ey1[lane];
+        if (am == 1)
+          return a0x * dy - a0y * dx >= 0.f && dx * a1y - dy * a1x >= 0.f && (a0x + a1x) * dx + (a0y + a1y) * dy >= 0.f;
+        return !(a1x * dy - a1y * dx > 0.f && dx * a0y - dy * a0x > 0.f);
+      };
       auto addDir = [&](uint32_t u) {
         const int bin = (int)(u >> 28);
         sm.bmin[bin][lane] = min(sm.bmin[bin][lane], u);
@@ -1125,8 +1152,8 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           if (k2 >= 0)
             lm &= lm - 1;
           float dx1, dy1, dx2 = 0.f, dy2 = 0.f;
-          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done;
-          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done;
+          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done && arcHolds(dx1, dy1);
+          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done && arcHolds(dx2, dy2);
           if (__any_sync(0xffffffffu, in1 || in2))
           {
             const uint32_t u1 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy1, dx1)) & 0x7fffffffu;
@@ -1303,7 +1330,19 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       }
       a.label[j] = done ? 1 : 2;
       if (a.margin)
-        a.margin[j] = done ? marginDeg(sm.gapAt[lane], true) : marginDeg(worst, __popc(occ) >= 2);
+      {
+        if (done)
+          a.margin[j] = marginDeg(sm.gapAt[lane], true);
+        else if (__popc(occ) == 1)
+        {
+          // every direction in one bin: the gap is the rest of the circle
+          const int b = __ffs(occ) - 1;
+          const uint32_t mn = sm.bmin[b][lane], mx = sm.bmax[b][lane];
+          a.margin[j] = marginDeg((mn - mx) & 0x7fffffffu, mn != mx);
+        }
+        else
+          a.margin[j] = marginDeg(worst, __popc(occ) >= 2);
+      }
       if (amb)
         a.ambList[atomicAdd(a.ambCount, 1u)] = j;
     }

@@ -70,7 +70,6 @@ struct wb_ctx
 
   /* named device buffers */
   DevBuf rec, key0, key1, idx0, idx1, tmp32, tmp32b, tmp8, scanTmp, small;
-  DevBuf sortAux;                   /* radix sort: digit histograms, bases, tickets, error word */
   DevBuf lev, cpl, pre, suf, leafId;
   DevBuf leafFirst, leafCount, leafLevel, leafKey, leafBox;
   DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;

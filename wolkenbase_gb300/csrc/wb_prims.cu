@@ -1,9 +1,13 @@
 /* Device-wide primitives written for this library: exclusive scan of u32 and
- * a stable LSD radix sort of (u64 key, u32 value) pairs (one sweep per 8-bit
- * digit, see below).
+ * a stable LSD radix sort of (u64 key, u32 value) pairs.
+ *
+ * Radix sort: 8-bit digits.  Per pass, one kernel counts digits per tile of
+ * 4096 keys, the digit-major count table is scanned, and a second kernel
+ * ranks each key inside its tile with warp __match_any_sync groups (stable:
+ * a warp walks its 512 keys in order, 32 at a time) and scatters.  Passes
+ * whose digit is constant over all keys are skipped.
  */
 #include <cuda_runtime.h>
-#include <algorithm>
 #include <cstdint>
 #include "wb_internal.h"
 
@@ -79,161 +83,93 @@ __global__ void totalOf(const uint32_t *in, const uint32_t *ex, uint64_t n, uint
   *total = n ? ex[n - 1] + in[n - 1] : 0;
 }
 
-/* ---------------- radix sort ----------------
- * One sweep per 8-bit digit (the decoupled look-back scheme of Merrill and
- * Garland's single-pass scan, applied per digit as in Adinets and Merrill's
- * "Onesweep" radix sort).  One kernel histograms every digit position of the
- * keys at once; the exclusive scans give each digit value's first output
- * slot per pass.  Each pass is then one kernel: a CTA takes the next tile of
- * kOsTile pairs in launch order (an atomic ticket), ranks its keys per digit
- * (warps walk their keys in order with match_any, so the sort is stable),
- * publishes its per-digit counts, looks back over the tiles before it for
- * their per-digit prefixes, and scatters its keys in digit order through
- * shared memory, so each digit's run is written contiguously.  A digit
- * position whose keys all share one value is skipped.  Every look-back wait
- * is bounded: a wait that runs out sets an error word and the sort reports
- * WB_ETIMEDOUT instead of hanging. */
-constexpr int kOsThreads = 256;
-constexpr int kOsWarps = kOsThreads / 32;
-constexpr int kOsPerLane = 12;
-constexpr int kOsTile = kOsThreads * kOsPerLane;   // 3072 pairs per tile
-constexpr unsigned long long kOsAgg = 1ull << 62, kOsPre = 2ull << 62, kOsVal = (1ull << 62) - 1;
-constexpr long long kOsSpinLimit = 1ll << 22;
+/* ---------------- radix sort ---------------- */
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortPerLane = 8;
+constexpr int kSortTile = kSortThreads * kSortPerLane;   // 2048
 
-/* Counts of every 8-bit digit value at every digit position: hist[p][v]. */
-__global__ void __launch_bounds__(256) osHistogram(const uint64_t *__restrict__ keys, uint64_t n,
-                                                   uint32_t *__restrict__ hist)
+__global__ void __launch_bounds__(kSortThreads) digitCounts(const uint64_t *__restrict__ keys, uint64_t n,
+                                                           int shift, uint32_t *__restrict__ counts,
+                                                           int numTiles)
 {
-  __shared__ uint32_t h[8][256];
-  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
-    (&h[0][0])[i] = 0;
+  __shared__ uint32_t h[256];
+  for (int i = threadIdx.x; i < 256; i += kSortThreads)
+    h[i] = 0;
   __syncthreads();
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  uint64_t base = (uint64_t)blockIdx.x * kSortTile;
+  for (int k = 0; k < kSortPerLane; k++)
   {
-    const uint64_t k = keys[i];
-#pragma unroll
-    for (int p = 0; p < 8; p++)
-      atomicAdd(&h[p][(k >> (8 * p)) & 255], 1u);
+    uint64_t i = base + (uint64_t)k * kSortThreads + threadIdx.x;
+    if (i < n)
+      atomicAdd(&h[(keys[i] >> shift) & 255], 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
-  {
-    const uint32_t v = (&h[0][0])[i];
-    if (v)
-      atomicAdd(&hist[i], v);
-  }
+  for (int d = threadIdx.x; d < 256; d += kSortThreads)
+    counts[(uint64_t)d * numTiles + blockIdx.x] = h[d];
 }
 
-/* base[p][v] = exclusive prefix of hist[p][.] at v; block p, 256 threads. */
-__global__ void __launch_bounds__(256) osBases(const uint32_t *__restrict__ hist, uint32_t *__restrict__ base)
+/* One stable pass of an 8-bit digit over a tile of kSortTile pairs: warps rank
+ * their keys per digit (match_any), the tile is put in digit order in shared
+ * memory, and consecutive threads then write consecutive positions of each
+ * digit's run, so the global writes coalesce. */
+__global__ void __launch_bounds__(kSortThreads) digitScatter(const uint64_t *__restrict__ keys,
+                                                            const uint32_t *__restrict__ vals, uint64_t n,
+                                                            int shift, const uint32_t *__restrict__ offsets,
+                                                            int numTiles, uint64_t *__restrict__ keysOut,
+                                                            uint32_t *__restrict__ valsOut)
 {
-  __shared__ uint32_t w[8];
-  const int p = blockIdx.x, v = threadIdx.x, lane = v & 31, warp = v >> 5;
-  const uint32_t x = hist[p * 256 + v];
-  const uint32_t inc = warpInclusive(x);
-  if (lane == 31)
-    w[warp] = inc;
-  __syncthreads();
-  uint32_t off = 0;
-  for (int k = 0; k < warp; k++)
-    off += w[k];
-  base[p * 256 + v] = off + inc - x;
-}
-
-__global__ void __launch_bounds__(kOsThreads) osPass(const uint64_t *__restrict__ keys,
-                                                     const uint32_t *__restrict__ vals, uint64_t n, int shift,
-                                                     const uint32_t *__restrict__ base,
-                                                     unsigned long long *__restrict__ status,
-                                                     uint32_t *__restrict__ ticket, int *__restrict__ err,
-                                                     uint64_t *__restrict__ keysOut, uint32_t *__restrict__ valsOut)
-{
-  __shared__ uint32_t wcount[kOsWarps][256];
+  __shared__ uint32_t wcount[kSortWarps][256];
   __shared__ uint32_t localStart[256], globalStart[256];
-  __shared__ uint64_t skeys[kOsTile];
-  __shared__ uint32_t svals[kOsTile];
-  __shared__ uint32_t sTile;
+  __shared__ uint64_t skeys[kSortTile];
+  __shared__ uint32_t svals[kSortTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0)
-    sTile = atomicAdd(ticket, 1u);
-  for (int i = threadIdx.x; i < kOsWarps * 256; i += kOsThreads)
+  for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads)
     (&wcount[0][0])[i] = 0;
   __syncthreads();
-  const uint64_t tile = sTile;
-  const uint64_t tbase = tile * kOsTile;
-  const uint32_t tileN = (uint32_t)(n - tbase < (uint64_t)kOsTile ? n - tbase : (uint64_t)kOsTile);
-  const uint64_t wbase = tbase + (uint64_t)warp * (kOsPerLane * 32);
-  uint64_t kk[kOsPerLane];
-  uint32_t vv[kOsPerLane];
-  uint32_t rank[kOsPerLane];
+  const uint64_t tbase = (uint64_t)blockIdx.x * kSortTile;
+  const uint32_t tileN = (uint32_t)(n - tbase < (uint64_t)kSortTile ? n - tbase : (uint64_t)kSortTile);
+  uint64_t wbase = tbase + (uint64_t)warp * (kSortPerLane * 32);
+  uint64_t k8[kSortPerLane];
+  uint32_t v8[kSortPerLane];
+  uint32_t rank[kSortPerLane];
   const unsigned lt = (1u << lane) - 1;
 #pragma unroll
-  for (int q = 0; q < kOsPerLane; q++)
+  for (int s = 0; s < kSortPerLane; s++)
   {
-    const uint64_t i = wbase + (uint64_t)q * 32 + lane;
-    const bool ok = i < n;
-    kk[q] = ok ? keys[i] : 0;
-    vv[q] = ok ? vals[i] : 0;
-  }
-#pragma unroll
-  for (int q = 0; q < kOsPerLane; q++)
-  {
-    const uint64_t i = wbase + (uint64_t)q * 32 + lane;
-    const uint32_t d = i < n ? (uint32_t)((kk[q] >> shift) & 255) : 256u;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t pre = d < 256 ? wcount[warp][d] : 0;
-    rank[q] = pre + __popc(peers & lt);
+    uint64_t i = wbase + (uint64_t)s * 32 + lane;
+    bool ok = i < n;
+    uint64_t key = ok ? keys[i] : 0;
+    k8[s] = key;
+    v8[s] = ok ? vals[i] : 0;
+    uint32_t d = ok ? (uint32_t)((key >> shift) & 255) : 256u;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    uint32_t pre = (d < 256) ? wcount[warp][d] : 0;
+    rank[s] = pre + __popc(peers & lt);
     __syncwarp();
     if (d < 256 && (peers & lt) == 0)
       wcount[warp][d] = pre + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
+  // per digit: exclusive prefix over warps, the tile's total, and where the
+  // digit's run starts in the tile and in the output
+  for (int d = threadIdx.x; d < 256; d += kSortThreads)
   {
-    // thread d: the digit's exclusive prefix over warps, its count in the
-    // tile, publication, and the look-back over earlier tiles
-    const int d = threadIdx.x;
     uint32_t run = 0;
-    for (int w = 0; w < kOsWarps; w++)
+    for (int w = 0; w < kSortWarps; w++)
     {
-      const uint32_t c = wcount[w][d];
+      uint32_t c = wcount[w][d];
       wcount[w][d] = run;
       run += c;
     }
-    localStart[d] = run;
-    unsigned long long *mine = status + tile * 256 + d;
-    unsigned long long excl = 0;
-    if (tile == 0)
-      atomicExch(mine, kOsPre | (unsigned long long)run);
-    else
-    {
-      atomicExch(mine, kOsAgg | (unsigned long long)run);
-      for (long long p = (long long)tile - 1; p >= 0; p--)
-      {
-        const volatile unsigned long long *sp = status + (uint64_t)p * 256 + d;
-        unsigned long long v = *sp;
-        long long spins = 0;
-        while ((v >> 62) == 0)
-        {
-          if (++spins > kOsSpinLimit)
-          {
-            atomicExch(err, 1);
-            v = kOsPre;
-            break;
-          }
-          __nanosleep(32);
-          v = *sp;
-        }
-        excl += v & kOsVal;
-        if ((v >> 62) == 2)
-          break;
-      }
-      atomicExch(mine, kOsPre | (excl + run));
-    }
-    globalStart[d] = base[d] + (uint32_t)excl;
+    localStart[d] = run;   // the digit's count for now
+    globalStart[d] = offsets[(uint64_t)d * numTiles + blockIdx.x];
   }
   __syncthreads();
   if (warp == 0)
   {
+    // exclusive prefix of the 256 digit counts, 8 per lane
     uint32_t c[8], sum = 0;
 #pragma unroll
     for (int q = 0; q < 8; q++)
@@ -241,39 +177,57 @@ __global__ void __launch_bounds__(kOsThreads) osPass(const uint64_t *__restrict_
       c[q] = localStart[lane * 8 + q];
       sum += c[q];
     }
-    const uint32_t inc = warpInclusive(sum);
-    uint32_t r = inc - sum;
+    uint32_t inc = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o)
+        inc += v;
+    }
+    uint32_t run = inc - sum;
 #pragma unroll
     for (int q = 0; q < 8; q++)
     {
-      localStart[lane * 8 + q] = r;
-      r += c[q];
+      localStart[lane * 8 + q] = run;
+      run += c[q];
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < kOsPerLane; q++)
+  for (int s = 0; s < kSortPerLane; s++)
   {
-    const uint64_t i = wbase + (uint64_t)q * 32 + lane;
+    uint64_t i = wbase + (uint64_t)s * 32 + lane;
     if (i < n)
     {
-      const uint32_t d = (uint32_t)((kk[q] >> shift) & 255);
-      const uint32_t lp = localStart[d] + wcount[warp][d] + rank[q];
-      skeys[lp] = kk[q];
-      svals[lp] = vv[q];
+      uint32_t d = (uint32_t)((k8[s] >> shift) & 255);
+      uint32_t lp = localStart[d] + wcount[warp][d] + rank[s];
+      skeys[lp] = k8[s];
+      svals[lp] = v8[s];
     }
   }
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < tileN; t += kOsThreads)
+  for (uint32_t t = threadIdx.x; t < tileN; t += kSortThreads)
   {
-    const uint64_t key = skeys[t];
-    const uint32_t d = (uint32_t)((key >> shift) & 255);
-    const uint64_t pos = (uint64_t)globalStart[d] + (t - localStart[d]);
+    uint64_t key = skeys[t];
+    uint32_t d = (uint32_t)((key >> shift) & 255);
+    uint32_t pos = globalStart[d] + (t - localStart[d]);
     keysOut[pos] = key;
     valsOut[pos] = svals[t];
   }
 }
 
+/* Bits that differ between any key and keys[0]. */
+__global__ void keySpread(const uint64_t *__restrict__ keys, uint64_t n, unsigned long long *orBits)
+{
+  uint64_t first = keys[0];
+  uint64_t acc = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc |= keys[i] ^ first;
+  for (int o = 16; o; o >>= 1)
+    acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc)
+    atomicOr(orBits, (unsigned long long)acc);
+}
 __global__ void pullKernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, uint64_t n16)
 {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x)
@@ -371,37 +325,32 @@ int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *k
 {
   if (n <= 1)
     return 0;
-  if (n > 0xffffffffull)
-    return wb_fail(c, WB_EINVAL, "radix sort: more than 2^32-1 pairs");
-  // aux words: histograms [0, 2048), bases [2048, 4096), tickets [4096, 4104), error at 4104
-  int rc = wb_ensure(c, c->sortAux, (4096 + 64) * 4);
+  int rc = wb_ensure(c, c->small, 4096);
   if (rc)
     return rc;
-  uint32_t *aux = (uint32_t *)c->sortAux.p;
-  uint32_t *hist = aux, *base = aux + 2048, *tickets = aux + 4096;
-  int *err = (int *)(aux + 4104);
-  const uint64_t numTiles = (n + kOsTile - 1) / kOsTile;
-  if ((rc = wb_ensure(c, c->tmp32b, numTiles * 256 * 8 + 64)))
-    return rc;
-  unsigned long long *status = (unsigned long long *)c->tmp32b.p;
-  WB_CUDA(c, cudaMemsetAsync(aux, 0, (4096 + 64) * 4, c->stream));
-  { osHistogram<<<(unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)c->sm_count * 8), 256, 0, c->stream>>>(
-        keys, n, hist); ++c->launches; }
-  { osBases<<<8, 256, 0, c->stream>>>(hist, base); ++c->launches; }
-  uint32_t h[2048];
-  WB_CUDA(c, cudaMemcpyAsync(h, hist, sizeof h, cudaMemcpyDefault, c->stream));
+  unsigned long long *dOr = (unsigned long long *)c->small.p;
+  WB_CUDA(c, cudaMemsetAsync(dOr, 0, 8, c->stream));
+  { keySpread<<<c->sm_count * 4, 256, 0, c->stream>>>(keys, n, dOr); ++c->launches; }
+  unsigned long long spread = 0;
+  WB_CUDA(c, cudaMemcpyAsync(&spread, dOr, 8, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
-  for (int shift = beginBit; shift < endBit && shift < 64; shift += 8)
+  int numTiles = (int)((n + kSortTile - 1) / kSortTile);
+  size_t cntBytes = (size_t)numTiles * 256 * sizeof(uint32_t);
+  rc = wb_ensure(c, c->tmp32b, 2 * cntBytes + 64);
+  if (rc)
+    return rc;
+  uint32_t *counts = (uint32_t *)c->tmp32b.p;
+  uint32_t *offs = counts + (size_t)numTiles * 256;
+  for (int shift = beginBit; shift < endBit; shift += 8)
   {
-    const int p = shift / 8;
-    bool constant = false;
-    for (int v = 0; v < 256 && !constant; v++)
-      constant = h[p * 256 + v] == n;
-    if (constant)
-      continue;   // every key has the same digit here: the pass would be the identity
-    WB_CUDA(c, cudaMemsetAsync(status, 0, numTiles * 256 * 8, c->stream));
-    { osPass<<<(unsigned)numTiles, kOsThreads, 0, c->stream>>>(keys, vals, n, shift, base + p * 256, status,
-                                                               tickets + p, err, keysAlt, valsAlt); ++c->launches; }
+    uint64_t mask = (shift + 8 >= 64) ? (~0ULL << shift) : (((1ULL << 8) - 1) << shift);
+    if ((spread & mask) == 0)
+      continue;   // digit identical for all keys: pass would be the identity
+    { digitCounts<<<numTiles, kSortThreads, 0, c->stream>>>(keys, n, shift, counts, numTiles); ++c->launches; }
+    rc = wb_exclusive_scan_u32(c, counts, offs, (uint64_t)numTiles * 256, nullptr);
+    if (rc)
+      return rc;
+    { digitScatter<<<numTiles, kSortThreads, 0, c->stream>>>(keys, vals, n, shift, offs, numTiles, keysAlt, valsAlt); ++c->launches; }
     WB_CUDA(c, cudaGetLastError());
     uint64_t *tk = keys;
     keys = keysAlt;
@@ -410,10 +359,5 @@ int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *k
     vals = valsAlt;
     valsAlt = tv;
   }
-  int e = 0;
-  WB_CUDA(c, cudaMemcpyAsync(&e, err, 4, cudaMemcpyDefault, c->stream));
-  WB_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (e)
-    return wb_fail(c, WB_ETIMEDOUT, "radix sort: a look-back wait ran out");
   return 0;
 }
