@@ -498,11 +498,6 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           else
             in = memberExact(a, exactHyp(a, h.j), gp, qx, qy, qz);
         }
-        // a direction outside the arc (see arcWants) changes nothing
-        if (in && fast && amode != 0)
-          in = amode == 1 ? (e0x * dy - e0y * dx >= 0.f && dx * e1y - dy * e1x >= 0.f &&
-                             (e0x + e1x) * dx + (e0y + e1y) * dy >= 0.f)
-                          : !(e1x * dy - e1y * dx > 0.f && dx * e0y - dy * e0x > 0.f);
         if (in && fast)
           u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
         else if (in)
@@ -850,6 +845,13 @@ struct GroupSmem
   float ex0[32], ey0[32], ex1[32], ey1[32];
   int amode[32];
   uint32_t gapAt[32];   /* a lane's largest gap when its point was proven surrounded */
+  /* per lane: store position, reach in column rings and super-cell rings */
+  uint32_t j[32];
+  int kmax[32], smax[32];
+  /* the warp's envelope and its column's box (the same for every lane) */
+  float apex, por2min;
+  int kmaxG, smaxG;
+  int4 cbox;
 };
 
 
@@ -956,32 +958,49 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
     // smallest polar radius, reach in rings.  It is formed again after every
     // column read, so it shrinks as lanes are decided (a tall point proven
     // surrounded no longer widens the search of the low ones).
-    float apex, por2min;
-    int kmaxG, smaxG;
-    const int offG = max(abs(ps.ci - ci0), abs(ps.cj - cj0));
+    {
+      const int offG = max(abs(ps.ci - ci0), abs(ps.cj - cj0));
+      sm.kmax[lane] = ps.kmax + offG;
+      sm.smax[lane] = ps.smax + (offG + WB_SUPER - 1) / WB_SUPER + 1;
+      sm.j[lane] = j;
+      if (lane == 0)
+        sm.cbox = cbox;
+    }
+    const float czp = ps.czp, por2 = ps.por2f;
+    // the envelope's values live in shared memory (one copy per warp)
     auto envelope = [&]() {
-      apex = !done ? (float)(me.z - oz) * sz + ps.czp : -INFINITY;
-      por2min = !done ? ps.por2f : INFINITY;
-      kmaxG = !done ? ps.kmax + offG : 0;
-      smaxG = !done ? ps.smax + (offG + WB_SUPER - 1) / WB_SUPER + 1 : 0;
+      float ap = !done ? (float)(me.z - oz) * sz + czp : -INFINITY;
+      float pm = !done ? por2 : INFINITY;
+      int km = !done ? sm.kmax[lane] : 0;
+      int sg = !done ? sm.smax[lane] : 0;
       for (int o = 16; o; o >>= 1)
       {
-        apex = fmaxf(apex, __shfl_xor_sync(0xffffffffu, apex, o));
-        por2min = fminf(por2min, __shfl_xor_sync(0xffffffffu, por2min, o));
-        kmaxG = max(kmaxG, __shfl_xor_sync(0xffffffffu, kmaxG, o));
-        smaxG = max(smaxG, __shfl_xor_sync(0xffffffffu, smaxG, o));
+        ap = fmaxf(ap, __shfl_xor_sync(0xffffffffu, ap, o));
+        pm = fminf(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+        km = max(km, __shfl_xor_sync(0xffffffffu, km, o));
+        sg = max(sg, __shfl_xor_sync(0xffffffffu, sg, o));
       }
+      __syncwarp();
+      if (lane == 0)
+      {
+        sm.apex = ap;
+        sm.por2min = pm;
+        sm.kmaxG = km;
+        sm.smaxG = sg;
+      }
+      __syncwarp();
     };
     envelope();
     bool deferred = false;
     int columnsRead = 0;
-    const float czp = ps.czp, por2 = ps.por2f;
     // envelope test of a box {x0, y0, x1, y1} with lowest point zmin
     auto envMeets = [&](const int4 &b, int32_t zmin) -> bool {
       if (b.x == INT32_MAX)
         return false;
-      float dx = (float)max(0, max(b.x - cbox.z, cbox.x - b.z)) * sx;
-      float dy = (float)max(0, max(b.y - cbox.w, cbox.y - b.w)) * sy;
+      const int4 cb0 = sm.cbox;
+      const float apex = sm.apex, por2min = sm.por2min;
+      float dx = (float)max(0, max(b.x - cb0.z, cb0.x - b.z)) * sx;
+      float dy = (float)max(0, max(b.y - cb0.w, cb0.y - b.w)) * sy;
       float zd = apex - (float)(zmin - oz) * sz;
       float r2 = s2 * (dx * dx + dy * dy);
       float mag = zd * zd + r2 + por2min;
@@ -995,8 +1014,10 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
     auto envZlim = [&](const int4 &b, const int4 &r1) -> int32_t {
       if (r1.w || !(sz > 0))
         return INT32_MAX;
-      float dx = (float)max(0, max(b.x - cbox.z, cbox.x - b.z)) * sx;
-      float dy = (float)max(0, max(b.y - cbox.w, cbox.y - b.w)) * sy;
+      const int4 cb0 = sm.cbox;
+      const float apex = sm.apex, por2min = sm.por2min;
+      float dx = (float)max(0, max(b.x - cb0.z, cb0.x - b.z)) * sx;
+      float dy = (float)max(0, max(b.y - cb0.w, cb0.y - b.w)) * sy;
       float need = sqrtf(por2min + s2 * (dx * dx + dy * dy));
       float dz = (apex - need + 1e-4f * (fabsf(apex) + need) + 1e-6f) / sz + 2.f;
       return dz > 2.1e9f ? INT32_MAX : (dz < -2.1e9f ? INT32_MIN : (int32_t)floorf(dz));
@@ -1085,21 +1106,10 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           if (!(gp & kStray) && a.fp32Only)
             in = zd > 0 && f > 0;
           else
-            in = memberExact(a, exactHyp(a, j), gp, c.x, c.y, c.z);
+            in = memberExact(a, exactHyp(a, sm.j[lane]), gp, c.x, c.y, c.z);
         }
         // dist(p,q) == 0 gives no direction (classify.cpp:142,153)
         return in && (dxi != 0 || dyi != 0);
-      };
-      // A direction outside the lane's arc lies in a gap too narrow to
-      // decide the point: it changes nothing, so it is not formed or kept.
-      auto arcHolds = [&](float dx, float dy) -> bool {
-        const int am = sm.amode[lane];
-        if (am == 0)
-          return true;
-        const float a0x = sm.ex0[lane], a0y = sm.ey0[lane], a1x = sm.ex1[lane], a1y = sm.ey1[lane];
-        if (am == 1)
-          return a0x * dy - a0y * dx >= 0.f && dx * a1y - dy * a1x >= 0.f && (a0x + a1x) * dx + (a0y + a1y) * dy >= 0.f;
-        return !(a1x * dy - a1y * dx > 0.f && dx * a0y - dy * a0x > 0.f);
       };
       auto addDir = [&](uint32_t u) {
         const int bin = (int)(u >> 28);
@@ -1122,8 +1132,10 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           keep = low;
           if (low && !((uint32_t)q.w & kStray))
           {
-            float ex = (float)max(0, max(q.x - cbox.z, cbox.x - q.x)) * sx;
-            float ey = (float)max(0, max(q.y - cbox.w, cbox.y - q.y)) * sy;
+            const int4 cb0 = sm.cbox;
+            const float apex = sm.apex, por2min = sm.por2min;
+            float ex = (float)max(0, max(q.x - cb0.z, cb0.x - q.x)) * sx;
+            float ey = (float)max(0, max(q.y - cb0.w, cb0.y - q.y)) * sy;
             float zd = apex - (float)(q.z - oz) * sz;
             float r2 = s2 * (ex * ex + ey * ey);
             float mag = zd * zd + r2 + por2min;
@@ -1148,12 +1160,16 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         {
           const int k1 = __ffs(lm) - 1;
           lm &= lm - 1;
+#ifdef WB_GROUP_SINGLE
+          const int k2 = -1;
+#else
           const int k2 = lm ? __ffs(lm) - 1 : -1;
+#endif
           if (k2 >= 0)
             lm &= lm - 1;
           float dx1, dy1, dx2 = 0.f, dy2 = 0.f;
-          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done && arcHolds(dx1, dy1);
-          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done && arcHolds(dx2, dy2);
+          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done;
+          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done;
           if (__any_sync(0xffffffffu, in1 || in2))
           {
             const uint32_t u1 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy1, dx1)) & 0x7fffffffu;
@@ -1202,13 +1218,13 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       {
         deferred = true;
         done = true;
-        a.deferList[atomicAdd(a.deferCount, 1u)] = j;
+        a.deferList[atomicAdd(a.deferCount, 1u)] = sm.j[lane];
       }
       return true;
     };
     // near field: the group's column and the ring around it
     const int kNearG = 1;
-    for (int ring = 0; ring <= kNearG && ring <= kmaxG && !allDone(); ring++)
+    for (int ring = 0; ring <= kNearG && ring <= sm.kmaxG && !allDone(); ring++)
     {
       const int ncells = ring == 0 ? 1 : 8 * ring;
       const int stride = ring == 0 ? 1 : 4 * ring - 1;
@@ -1240,7 +1256,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
     // far field: rings of super-cells, then their columns outside the near field
     const int S = WB_SUPER;
     const int si = ci0 / S, sj = cj0 / S;
-    for (int sr = 0; sr <= smaxG && kmaxG > kNearG && !allDone(); sr++)
+    for (int sr = 0; sr <= sm.smaxG && sm.kmaxG > kNearG && !allDone(); sr++)
     {
       if (si + sr < 0 || si - sr >= a.snx || sj + sr < 0 || sj - sr >= a.sny)
         continue;
@@ -1307,7 +1323,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       gst[4] = __popc(bAct);
       gst[5] = __popc(bDef);
       gst[6] = clock64() - tG;
-      gst[7] = smaxG;
+      gst[7] = sm.smaxG;
       gst[8] = __popc(bGnd);
       if (gst[2] > 1000)
       {
@@ -1321,6 +1337,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
 #endif
     if (act && !deferred)
     {
+      const uint32_t j = sm.j[lane];
       uint32_t worst = 0;
       bool amb = false;
       if (!done)
