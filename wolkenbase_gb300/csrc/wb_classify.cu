@@ -1152,7 +1152,6 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
 #ifdef WB_CLASSIFY_STATS
         const long long tCand = clock64();
 #endif
-        // two candidates per step: independent work for the scheduler
         // Every lane runs the tests (a decided lane's results are dropped), so
         // the warp does not diverge on them; the directions are formed only
         // when some lane has a candidate inside.
@@ -1160,24 +1159,13 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         {
           const int k1 = __ffs(lm) - 1;
           lm &= lm - 1;
-#ifdef WB_GROUP_SINGLE
-          const int k2 = -1;
-#else
-          const int k2 = lm ? __ffs(lm) - 1 : -1;
-#endif
-          if (k2 >= 0)
-            lm &= lm - 1;
-          float dx1, dy1, dx2 = 0.f, dy2 = 0.f;
+          float dx1, dy1;
           const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done;
-          const bool in2 = k2 >= 0 && memberOf(sm.cand[k2], dx2, dy2) && !done;
-          if (__any_sync(0xffffffffu, in1 || in2))
+          if (__any_sync(0xffffffffu, in1))
           {
             const uint32_t u1 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy1, dx1)) & 0x7fffffffu;
-            const uint32_t u2 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy2, dx2)) & 0x7fffffffu;
             if (in1)
               addDir(u1);
-            if (in2)
-              addDir(u2);
           }
         }
         __syncwarp();
@@ -1726,7 +1714,11 @@ struct WbBatch
   cudaGraphExec_t graphs[WB_N_SHAPES] = {nullptr};
 };
 
+#ifdef WB_ALT_SHAPES
+const WbShape kWbShapes[WB_N_SHAPES] = {{4, 5}, {8, 3}, {8, 2}, {4, 6}, {4, 8}, {4, 8}, {8, 4}, {2, 12}};
+#else
 const WbShape kWbShapes[WB_N_SHAPES] = {{4, 5}, {8, 3}, {8, 2}, {8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}};
+#endif
 
 namespace
 {
@@ -1745,8 +1737,13 @@ RingsFn ringsFn(int idx)
   {
   case 1: return batchGroups<8, 3>;
   case 2: return batchGroups<8, 2>;
+#ifdef WB_ALT_SHAPES
+  case 3: return batchGroups<4, 6>;
+  case 4: return batchGroups<4, 8>;
+#else
   case 3: return batchRings<0, 8, 3>;
   case 4: return batchRings<0, 4, 6>;
+#endif
   case 5: return batchRings<0, 4, 8>;
   case 6: return batchRings<0, 8, 4>;
   case 7: return batchRings<0, 2, 12>;
