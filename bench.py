@@ -345,15 +345,21 @@ def _pct(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
 
-def served_form(args, device):
+def served_form(args, device, rate=None, count=None, pool=None):
     """Poisson arrivals of tile-classify requests replayed against the plain
     per-request path (one context, one request at a time, in arrival order)
     and against the server (admission by HBM budget, overlapping scans, fused
-    classify launches).  Host buffers in and out for both."""
+    classify launches).  Host buffers in and out for both.  With pool < count
+    the requests reuse pool generated clouds in turn (their arrival times and
+    sizes follow the request stream's own seeds)."""
     import wolkenbase_gb300 as wb
     from wolkenbase_gb300 import synth
-    reqs = synth.serve_requests(args.serve_requests, rate=args.serve_rate, seed=args.seed + 5000)
-    clouds = generate([("serve", n, seed, 0.0) for _, n, seed in reqs])
+    rate = rate or args.serve_rate
+    count = count or args.serve_requests
+    pool = min(pool or count, count)
+    reqs = synth.serve_requests(count, rate=rate, seed=args.seed + 5000)
+    made = generate([("serve", n, seed, 0.0) for _, n, seed in reqs[:pool]])
+    clouds = [made[i % pool] for i in range(count)]
     arrivals = [t for t, _, _ in reqs]
     pts = sum(c.n for c in clouds)
 
@@ -400,8 +406,9 @@ def served_form(args, device):
     st = srv.stats()
     srv.close()
     batch = [s["batch_jobs"] for s in sts]
-    return {"workload": f"{len(clouds)} requests, Poisson arrivals at {args.serve_rate:g}/s, sizes log-uniform "
-                        f"10k-10M points (100 pts/m^2 tiles), {args.serve_budget_gb:g} GB HBM budget",
+    return {"workload": f"{len(clouds)} requests ({pool} distinct clouds), Poisson arrivals at {rate:g}/s, sizes "
+                        f"log-uniform 10k-10M points (100 pts/m^2 tiles), {args.serve_budget_gb:g} GB HBM budget",
+            "offered_Mpts_s": pts / max(arrivals[-1], 1e-9) / 1e6,
             "points": pts,
             "plain": {"value": pts / plain_span / 1e6, "unit": UNIT, "p50_ms": _pct(plain_lat, 50) * 1e3,
                       "p99_ms": _pct(plain_lat, 99) * 1e3, "makespan_s": plain_span},
@@ -539,6 +546,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-low-rate", type=float, default=50.0, help="arrival rate of the below-capacity run")
+    ap.add_argument("--serve-low-requests", type=int, default=256)
+    ap.add_argument("--serve-low-pool", type=int, default=64, help="distinct clouds the below-capacity run cycles through")
     ap.add_argument("--serve-budget-gb", type=float, default=80.0)
     ap.add_argument("--batch-tiles", type=int, default=256)
     ap.add_argument("--batch-slots", type=int, default=8)
@@ -660,6 +670,23 @@ def main():
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes": alg_bytes, "avg_ms": stage_ms[dom]}
+        # The kernel is bound by instruction issue and latency, not by HBM: its
+        # issue-side fraction, from the warp instructions per point of one
+        # profiled launch, over the issue rate of the GPU at the sampled clock
+        tr = json.load(open(tp)).get(dom) if os.path.exists(tp) else None
+        if tr and tr.get("inst_per_point"):
+            ck = clocks.summary() or {}
+            mhz = ck.get("sm_mhz") or ck.get("sm_max_mhz") or 2070.0
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            peak_inst = sms * 4 * mhz * 1e6
+            ach_inst = tr["inst_per_point"] * nd / (stage_ms[dom] / 1e3)
+            roof["issue"] = {"inst_per_point": tr["inst_per_point"], "achieved_Ginst_s": ach_inst / 1e9,
+                             "peak_Ginst_s": peak_inst / 1e9, "frac": ach_inst / peak_inst,
+                             "ncu_issue_active": tr.get("issue_active_pct", 0) / 100,
+                             "ncu_warps_active": tr.get("warps_active_pct", 0) / 100,
+                             "note": "warp instructions per point of the column-group fast pass (ncu, one launch "
+                                     "on 4M points) x points / the classify stage's time; peak = 4 issue slots "
+                                     "per SM per cycle at the sampled SM clock"}
     # the octree build proper (sizeFit + put of every point); the column grid is this path's own index
     build_ms = sum(v for k, v in stage_ms.items() if k in ("decode_key", "sort", "dedup", "leaves", "leaf_order",
                                                          "point_map", "nodes"))
@@ -682,6 +709,8 @@ def main():
     torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_forms:
         out["served"] = served_form(args, local)
+        out["served_below_capacity"] = served_form(args, local, rate=args.serve_low_rate,
+                                                   count=args.serve_low_requests, pool=args.serve_low_pool)
         out["batched"] = batched_form(args, local)
         out["precision"] = precision_form(args, local)
     # compact summaries last, where a reader of the line's end finds them

@@ -1714,11 +1714,7 @@ struct WbBatch
   cudaGraphExec_t graphs[WB_N_SHAPES] = {nullptr};
 };
 
-#ifdef WB_ALT_SHAPES
-const WbShape kWbShapes[WB_N_SHAPES] = {{4, 5}, {8, 3}, {8, 2}, {4, 6}, {4, 8}, {4, 8}, {8, 4}, {2, 12}};
-#else
 const WbShape kWbShapes[WB_N_SHAPES] = {{4, 5}, {8, 3}, {8, 2}, {8, 3}, {4, 6}, {4, 8}, {8, 4}, {2, 12}};
-#endif
 
 namespace
 {
@@ -1737,13 +1733,8 @@ RingsFn ringsFn(int idx)
   {
   case 1: return batchGroups<8, 3>;
   case 2: return batchGroups<8, 2>;
-#ifdef WB_ALT_SHAPES
-  case 3: return batchGroups<4, 6>;
-  case 4: return batchGroups<4, 8>;
-#else
   case 3: return batchRings<0, 8, 3>;
   case 4: return batchRings<0, 4, 6>;
-#endif
   case 5: return batchRings<0, 4, 8>;
   case 6: return batchRings<0, 8, 4>;
   case 7: return batchRings<0, 2, 12>;
