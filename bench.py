@@ -446,8 +446,20 @@ def batched_form(args, device):
     st = srv.stats()
     srv.close()
     same = all(np.array_equal(a, b) for a, b in zip(plain_ref, got))
+    # the FP32 precision mode on every tile of the batch against the exact path
+    from wolkenbase_gb300 import precision
+    clf = wb.Classifier(device)
+    reps = [precision.compare(clf, c) for c in clouds]
+    clf.close()
+    flips = sum(r["flips"] for r in reps)
+    prec = {"points": pts, "flips": flips, "agreement": 1.0 - flips / pts,
+            "slope_err": max(r["slope_err"] for r in reps),
+            "residual_abs_err_m": max(r["residual_abs_err_m"] for r in reps),
+            "residual_err": max(r["residual_err"] for r in reps),
+            "residual_err_p999_max_over_tiles_sets": max(r["residual_err_p999"] for r in reps),
+            "h_changed": sum(r["h_changed"] for r in reps), "h_rel_err": max(r["h_rel_err"] for r in reps)}
     return {"workload": f"{len(clouds)} tiles, log-uniform 50k-5M points (100 pts/m^2), slopes to 35 deg, "
-                        "nonground 5-40%",
+                        "nonground 5-40%", "precision": prec,
             "points": pts,
             "plain": {"value": pts / plain_s / 1e6, "unit": UNIT, "seconds": plain_s},
             "batched": {"value": pts / batch_s / 1e6, "unit": UNIT, "seconds": batch_s,
@@ -653,6 +665,11 @@ def main():
     las = las_measure(clf, cloud, n, stream, local) if rank == 0 else None
     paging = paging_measure(cloud, params, cls_dev, local, args) if rank == 0 and not args.no_forms else None
     info = clf.info()
+    prec_plain = None
+    if rank == 0 and not args.no_forms:
+        from wolkenbase_gb300 import precision
+        prec_plain = precision.compare(clf, cloud, built=True)
+        prec_plain["workload"] = cfg["workload"]
     stage_ms = {k: v / n_prof for k, v in stage_acc.items()}
     dom = max((k for k in stage_ms if k not in ("upload", "cls_upload", "cls_download", "classify_exact")), key=lambda k: stage_ms[k])
     peak, peak_kind = peaks()
@@ -720,6 +737,15 @@ def main():
     out["build"] = {"ms": round(build_ms, 3), "achieved_GBps": build_gbs, "frac": build_gbs / peak if build_gbs else None,
                     "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT, "peak_GBps": peak}
     out["parity"] = parity
+    if rank == 0 and world == 1 and not args.no_forms:
+        # FP32 precision mode against the exact path, per workload: label
+        # flips and the per-point fit residuals' difference (scan.cpp:74-87)
+        keys = ("points", "flips", "agreement", "slope_err", "residual_abs_err_m", "residual_err", "h_changed",
+                "h_rel_err")
+        out["precision_by_config"] = {
+            "plain_scale": {k: prec_plain.get(k) for k in keys} if prec_plain else None,
+            "batched": {k: out["batched"]["precision"].get(k) for k in keys},
+            "utm_100M": {k: out["precision"].get(k) for k in keys}}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

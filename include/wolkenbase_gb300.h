@@ -259,6 +259,14 @@ int wb_set_precision(wb_ctx *ctx, int mode);
  * measured from the tile centre); NaN where the fit is singular.  With
  * WB_PRECISION_FP32 this is the FP32-sum fit. */
 int wb_tile_planes(wb_ctx *ctx, double *abc, uint64_t capacity);
+
+/* The per-point fit residuals of every tile (no reference counterpart: the
+ * precision report).  r = z - (a*x + b*y + c) over the tile's points, x and y
+ * from the tile centre, under the planes of the last wb_scan_tiles and under
+ * abc_ref (3 doubles per tile, e.g. wb_tile_planes of an exact scan):
+ * max_diff[k] = max |r - r_ref|, max_ref[k] = max |r_ref| (NaN where either
+ * plane is singular).  Host arrays of the tile count.  Synchronous. */
+int wb_tile_residuals(wb_ctx *ctx, const double *abc_ref, double *max_diff, double *max_ref);
 int wb_get_tuning(wb_ctx *ctx, wb_tuning *t);
 int wb_autotune(wb_ctx *ctx, const wb_params *params);
 

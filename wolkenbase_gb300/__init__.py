@@ -235,6 +235,18 @@ class Classifier:
         self._check(self.L.wb_tile_planes(self.ctx, out.ctypes.data, T))
         return out
 
+    def residuals(self, ref_planes):
+        """Per tile, max |r - r_ref| and max |r_ref| of the points' fit residuals
+        r = z - (a*x + b*y + c) under the last scan's planes and under ref_planes."""
+        ref = np.ascontiguousarray(ref_planes, dtype=np.float64)
+        T = self.info()["n_tiles"]
+        if ref.shape != (T, 3):
+            raise ValueError("ref_planes must be (n_tiles, 3)")
+        d = np.zeros(T)
+        r = np.zeros(T)
+        self._check(self.L.wb_tile_residuals(self.ctx, ref.ctypes.data, d.ctypes.data, r.ctypes.data))
+        return d, r
+
     def set_paging(self, host_budget):
         """Lets buffers beyond the HBM budget live in pinned host memory (0 turns it off)."""
         self._check(self.L.wb_set_paging(self.ctx, int(host_budget)))

@@ -147,6 +147,7 @@ SIGNATURES = {
     "wb_autotune": (C.c_int, [C.c_void_p, C.POINTER(wb_params)]),
     "wb_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "wb_tile_planes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wb_tile_residuals": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "wb_class_totals": (C.c_int, [C.c_void_p, C.c_void_p]),
     "wb_duplicates": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_void_p]),
     "wb_las_write_classes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_void_p]),

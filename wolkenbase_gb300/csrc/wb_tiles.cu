@@ -1274,6 +1274,45 @@ static int sortHugeTiles(wb_ctx *c, uint32_t nh, const uint32_t *tileStart)
   return 0;
 }
 
+/* Per tile, over its points (x, y from the tile centre, z as decoded): the
+ * largest |r - r_ref| and |r_ref| of the fit residuals r = z - (a x + b y + c)
+ * under the last scan's plane and r_ref under a given plane (NaN where
+ * either plane is singular).  One warp per tile. */
+__global__ void residualKernel(ScanArgs s, const TileRes *__restrict__ res, const double *__restrict__ ref,
+                               double *__restrict__ maxDiff, double *__restrict__ maxRef)
+{
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < s.t.T; k += warps)
+  {
+    double cx, cy;
+    tileCenter(s.t, k, cx, cy);
+    const double a = res[k].plane[0], b = res[k].plane[1], c = res[k].plane[2];
+    const double ar = ref[3 * k], br = ref[3 * k + 1], cr = ref[3 * k + 2];
+    double md = 0, mr = 0;
+    const uint32_t base = s.tileStart[k], n = s.tileN[k];
+    for (uint32_t t = lane; t < n; t += 32)
+    {
+      const uint32_t j = s.tilePts[base + t];
+      const double x = dec(s.t, 0, s.t.sx[j]) - cx, y = dec(s.t, 1, s.t.sy[j]) - cy, z = dec(s.t, 2, s.t.sz[j]);
+      const double r = z - (a * x + b * y + c), rr = z - (ar * x + br * y + cr);
+      md = fmax(md, fabs(r - rr));
+      mr = fmax(mr, fabs(rr));
+    }
+    for (int o = 16; o; o >>= 1)
+    {
+      md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+      mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    }
+    if (lane == 0)
+    {
+      const bool bad = !(a == a && b == b && c == c && ar == ar && br == br && cr == cr);
+      maxDiff[k] = bad ? NAN : md;
+      maxRef[k] = bad ? NAN : mr;
+    }
+  }
+}
+
 /* Sum of the tiles' room bounds in 64 bits. */
 __global__ void boundTotal64(const uint32_t *bound, uint64_t T, unsigned long long *tot)
 {
@@ -1383,5 +1422,36 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "postscan");
   c->stage = 2;
+  return 0;
+}
+
+int wb_tile_residuals(wb_ctx *c, const double *abc_ref, double *max_diff, double *max_ref)
+{
+  if (!c || !abc_ref || !max_diff || !max_ref)
+    return WB_EINVAL;
+  if (c->stage < 2)
+    return wb_fail(c, WB_ESTATE, "wb_tile_residuals: scan the tiles first");
+  WbDeviceGuard deviceGuard(c->device);
+  const uint64_t T = c->n_tiles;
+  if (T == 0)
+    return 0;
+  WbScratch ref(c), out(c);
+  int rc;
+  if ((rc = wb_ensure(c, ref.b, T * 24 + 64)) || (rc = wb_ensure(c, out.b, T * 16 + 64)))
+    return rc;
+  WB_CUDA(c, cudaMemcpyAsync(ref.b.p, abc_ref, T * 24, cudaMemcpyDefault, c->stream));
+  ScanArgs s;
+  s.t = tileArgs(c);
+  s.tileStart = (const uint32_t *)c->tileStart.p;
+  s.tileN = (const uint32_t *)c->tileN.p;
+  s.tilePts = (const uint32_t *)c->tilePts.p;
+  s.minH = c->params.min_hyp_size;
+  double *md = (double *)out.b.p, *mr = md + T;
+  { residualKernel<<<(unsigned)std::min<uint64_t>((T * 32 + 255) / 256, (uint64_t)c->sm_count * 32), 256, 0,
+                     c->stream>>>(s, (const TileRes *)c->tileRes.p, (const double *)ref.b.p, md, mr); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  WB_CUDA(c, cudaMemcpyAsync(max_diff, md, T * 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaMemcpyAsync(max_ref, mr, T * 8, cudaMemcpyDefault, c->stream));
+  WB_CUDA(c, cudaStreamSynchronize(c->stream));
   return 0;
 }

@@ -8,13 +8,17 @@ exact FP64 path on the same cloud.
                percentile: a fit of a few nearly collinear points is
                ill-conditioned in any precision)
   residual_err max over tiles of max_i |r32_i - r64_i| / max(max_i |r64_i|, q),
-               where r = z - (a*x + b*y + c) is a point's fit residual and q
-               the height quantum (scale * unit).  The difference of two
-               planes is linear in x and y, so over the tile cylinder
-               (radius R) it is at most |da|R + |db|R + |dc|; max_i |r64_i| is
-               at least half the tile's untilted height range.  The ratio of
-               the two bounds is reported.
-  h_rel_err    max relative difference of the tiles' hyperboloid sizes
+               where r = z - (a*x + b*y + c) is point i's fit residual under
+               each mode's plane (x, y from the tile centre; the residuals of
+               scanCylinder's untilting, scan.cpp:74-87) and q the height
+               quantum (scale * unit); also its 99.9th percentile and the
+               largest absolute difference in metres
+  h_changed    tiles whose hyperboloid size differs, and h_rel_err the largest
+               relative difference: the size follows integer counts of the
+               points below a height threshold (scan.cpp:88-112), so a plane
+               that moves by rounding can move one point across the threshold
+               and change a size by a whole count -- a threshold effect, not
+               an accumulated error
 """
 from __future__ import annotations
 
@@ -42,17 +46,18 @@ def compare(clf, cloud, params=None, built=False):
         t2 = time.perf_counter()
         res[name] = (cls, clf.planes(), clf.tiles())
         out[name + "_ms"] = {"scan": (t1 - t0) * 1e3, "classify": (t2 - t1) * 1e3}
+        if name == "fp32":
+            rdiff, rref = clf.residuals(res["fp64"][1])
     clf.set_precision(_lib.WB_PRECISION_EXACT)
     c64, p64, t64 = res["fp64"]
     c32, p32, t32 = res["fp32"]
     flips = int(np.count_nonzero(c64 != c32))
     n = int(c64.size)
     ok = (t64["n_points"] >= 3) & np.all(np.isfinite(p64), axis=1) & np.all(np.isfinite(p32), axis=1)
+    ok &= np.isfinite(rdiff) & np.isfinite(rref)
     d = np.abs(p32 - p64)[ok]
-    R = clf.info()["spacing"] * 41.0 / 71.0
-    bound = d[:, 0] * R + d[:, 1] * R + d[:, 2]
     q = abs(cloud.scale[2] * cloud.unit)
-    half = np.maximum(t64["height"][ok] / 2, q)
+    rel = rdiff[ok] / np.maximum(rref[ok], q)
     h64, h32 = t64["hyperboloid_size"], t32["hyperboloid_size"]
     hm = (t64["n_points"] > 0) & (h64 > 0)
     out.update({
@@ -60,10 +65,11 @@ def compare(clf, cloud, params=None, built=False):
         "tiles_compared": int(ok.sum()),
         "slope_err": float(np.max(np.hypot(d[:, 0], d[:, 1]))) if len(d) else 0.0,
         "slope_err_p999": float(np.percentile(np.hypot(d[:, 0], d[:, 1]), 99.9)) if len(d) else 0.0,
-        "residual_abs_err_m": float(np.max(bound)) if len(d) else 0.0,
-        "residual_err": float(np.max(bound / half)) if len(d) else 0.0,
-        "residual_err_p999": float(np.percentile(bound / half, 99.9)) if len(d) else 0.0,
+        "residual_abs_err_m": float(np.max(rdiff[ok])) if len(d) else 0.0,
+        "residual_err": float(np.max(rel)) if len(d) else 0.0,
+        "residual_err_p999": float(np.percentile(rel, 99.9)) if len(d) else 0.0,
         "h_rel_err": float(np.max(np.abs(h32[hm] - h64[hm]) / h64[hm])) if hm.any() else 0.0,
+        "h_changed": int(np.count_nonzero(h32[hm] != h64[hm])),
         "tree_flag_changes": int(np.count_nonzero(t64["tree_flags"] != t32["tree_flags"])),
     })
     return out
