@@ -273,55 +273,68 @@ __global__ void leafCountKernel(uint64_t L, uint64_t nd, const uint32_t *__restr
 }
 
 /* One block per leaf: bitonic sort of the leaf's input indices (<= 537, padded
- * to 1024), gather of X/Y/Z into store order, integer bounding box. */
-__global__ void __launch_bounds__(512) leafSortKernel(KeyArgs a, const uint32_t *__restrict__ first,
-                                                      const uint32_t *__restrict__ count,
-                                                      const uint32_t *__restrict__ didx, uint32_t *__restrict__ sidx,
-                                                      int32_t *__restrict__ sx, int32_t *__restrict__ sy,
-                                                      int32_t *__restrict__ sz, int32_t *__restrict__ box,
-                                                      uint64_t L)
+ * to a power of two, at most 1024), gather of X/Y/Z into store order, integer
+ * bounding box, and each stored record's store slot and leaf.  Each thread is
+ * one comparator of a stage (kLeafThreads comparators per pass).  A stage
+ * whose partners lie at most 32 apart touches only its warp's own 64-element
+ * window, so between two such stages a warp barrier is enough. */
+constexpr int kLeafThreads = 256;
+__global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const uint32_t *__restrict__ first,
+                                                               const uint32_t *__restrict__ count,
+                                                               const uint32_t *__restrict__ didx,
+                                                               uint32_t *__restrict__ sidx, int32_t *__restrict__ sx,
+                                                               int32_t *__restrict__ sy, int32_t *__restrict__ sz,
+                                                               int32_t *__restrict__ box, uint32_t *__restrict__ storeOf,
+                                                               uint32_t *__restrict__ pointLeaf, uint64_t L)
 {
   __shared__ uint32_t v[1024];
-  __shared__ int32_t red[6][16];
-  uint64_t l = blockIdx.x;
+  __shared__ int32_t red[6][kLeafThreads / 32];
+  const uint64_t l = blockIdx.x;
   if (l >= L)
     return;
-  uint32_t f = first[l], cnt = count[l];
-  int P = 32;
+  const uint32_t f = first[l], cnt = count[l];
+  int P = 64;
   while (P < (int)cnt)
     P <<= 1;
-  for (int t = threadIdx.x; t < P; t += blockDim.x)
+  for (int t = threadIdx.x; t < P; t += kLeafThreads)
     v[t] = t < (int)cnt ? didx[f + t] : 0xffffffffu;
   __syncthreads();
+  const int half = P >> 1;
   for (int k = 2; k <= P; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1)
     {
-      for (int t = threadIdx.x; t < P; t += blockDim.x)
+      for (int t = threadIdx.x; t < half; t += kLeafThreads)
       {
-        int u = t ^ j;
-        if (u > t)
+        const int i = (t / j) * 2 * j + (t % j), u = i + j;
+        const bool up = (i & k) == 0;
+        const uint32_t x = v[i], y = v[u];
+        if ((x > y) == up)
         {
-          bool up = (t & k) == 0;
-          uint32_t x = v[t], y = v[u];
-          if ((x > y) == up)
-          {
-            v[t] = y;
-            v[u] = x;
-          }
+          v[i] = y;
+          v[u] = x;
         }
       }
-      __syncthreads();
+      // a warp barrier suffices when this stage and the next both stay in
+      // the warps' own 64-element windows
+      const int jNext = j > 1 ? j >> 1 : k;
+      if (j <= 32 && jNext <= 32 && half <= kLeafThreads)
+        __syncwarp();
+      else
+        __syncthreads();
     }
+  __syncthreads();
   int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
-  for (int t = threadIdx.x; t < (int)cnt; t += blockDim.x)
+  for (int t = threadIdx.x; t < (int)cnt; t += kLeafThreads)
   {
-    uint32_t id = v[t];
+    const uint32_t id = v[t];
     int32_t q[3];
     loadXYZ(a.rec, a.stride, id, q[0], q[1], q[2]);
     sidx[f + t] = id;
     sx[f + t] = q[0];
     sy[f + t] = q[1];
     sz[f + t] = q[2];
+    storeOf[id] = f + t;
+    pointLeaf[id] = (uint32_t)l;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++)
     {
@@ -336,7 +349,7 @@ __global__ void __launch_bounds__(512) leafSortKernel(KeyArgs a, const uint32_t 
       mn[ax] = min(mn[ax], __shfl_xor_sync(0xffffffffu, mn[ax], o));
       mx[ax] = max(mx[ax], __shfl_xor_sync(0xffffffffu, mx[ax], o));
     }
-  int w = threadIdx.x >> 5;
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
     for (int ax = 0; ax < 3; ax++)
     {
@@ -346,18 +359,12 @@ __global__ void __launch_bounds__(512) leafSortKernel(KeyArgs a, const uint32_t 
   __syncthreads();
   if (threadIdx.x < 6)
   {
-    int ax = threadIdx.x;
+    const int ax = threadIdx.x;
     int32_t r = ax < 3 ? INT32_MAX : INT32_MIN;
-    for (int k = 0; k < (int)(blockDim.x >> 5); k++)
-      r = ax < 3 ? min(r, red[ax][k]) : max(r, red[ax][k]);
+    for (int q = 0; q < kLeafThreads / 32; q++)
+      r = ax < 3 ? min(r, red[ax][q]) : max(r, red[ax][q]);
     box[(uint64_t)ax * L + l] = r;
   }
-}
-
-__global__ void storeOfKernel(uint64_t nd, const uint32_t *__restrict__ sidx, uint32_t *__restrict__ storeOf)
-{
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
-    storeOf[sidx[j]] = (uint32_t)j;
 }
 
 /* Records overwritten by a later duplicate point at the survivor's slot. */
@@ -653,15 +660,18 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   { leafCountKernel<<<gridFor(c, L), 256, 0, c->stream>>>(L, nd, first, count); ++c->launches; }
   wb_mark(c, "leaves");
   int32_t *box = (int32_t *)c->leafBox.p;
-  { leafSortKernel<<<(unsigned)L, 512, 0, c->stream>>>(a, first, count, didx, (uint32_t *)c->sidx.p, (int32_t *)c->sx.p,
-                                                     (int32_t *)c->sy.p, (int32_t *)c->sz.p, box, L); ++c->launches; }
+  uint32_t *storeOf = (uint32_t *)c->storeOf.p;
+  { leafSortKernel<<<(unsigned)L, kLeafThreads, 0, c->stream>>>(a, first, count, didx, (uint32_t *)c->sidx.p,
+                                                               (int32_t *)c->sx.p, (int32_t *)c->sy.p, (int32_t *)c->sz.p,
+                                                               box, storeOf, (uint32_t *)c->pointLeaf.p, L); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "leaf_order");
-  uint32_t *storeOf = (uint32_t *)c->storeOf.p;
-  { storeOfKernel<<<gridFor(c, nd), 256, 0, c->stream>>>(nd, (uint32_t *)c->sidx.p, storeOf); ++c->launches; }
+  // records a later identical point overwrote take their survivor's slot and leaf
   if (nd != n)
+  {
     { dupMapKernel<<<gridFor(c, n), 256, 0, c->stream>>>(a, keys, idx, surv, storeOf); ++c->launches; }
-  { pointLeafKernel<<<gridFor(c, n), 256, 0, c->stream>>>(n, storeOf, leafId, (uint32_t *)c->pointLeaf.p); ++c->launches; }
+    { pointLeafKernel<<<gridFor(c, n), 256, 0, c->stream>>>(n, storeOf, leafId, (uint32_t *)c->pointLeaf.p); ++c->launches; }
+  }
   { maxLevelKernel<<<gridFor(c, L), 256, 0, c->stream>>>(L, leafLev, dMax); ++c->launches; }
   int maxLev = 0;
   WB_CUDA(c, cudaMemcpyAsync(&maxLev, dMax, 4, cudaMemcpyDefault, c->stream));

@@ -1147,41 +1147,27 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         unsigned lm = __ballot_sync(0xffffffffu, keep);
         WB_STAT(gst[2], __popc(lm));
         WB_STAT(gst[3], __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)));
-        // the kept candidates, packed to the front in lane order
-        if (keep)
-          sm.cand[__popc(lm & ((1u << lane) - 1))] = q;
+        sm.cand[lane] = q;
         __syncwarp();
 #ifdef WB_CLASSIFY_STATS
         const long long tCand = clock64();
 #endif
-        // Two phases.  First every lane tests every kept candidate against its
-        // own point: the tests are independent of one another (no warp
-        // intrinsic between them), so their latencies overlap.  Then the
-        // directions of the candidates some lane holds are formed by every
-        // lane (the warp does not diverge) and kept by the lanes that hold
-        // them.  A decided lane tests nothing.
-        const int nk = __popc(lm);
-        unsigned inMask = 0;
-        if (!done)
+        // Every lane runs the tests (a decided lane's results are dropped), so
+        // the warp does not diverge on them; the directions are formed only
+        // when some lane has a candidate inside.  (Testing a whole chunk first
+        // and forming the directions afterwards measured 40% slower.)
+        while (lm)
         {
-#pragma unroll 4
-          for (int k = 0; k < nk; k++)
+          const int k1 = __ffs(lm) - 1;
+          lm &= lm - 1;
+          float dx1, dy1;
+          const bool in1 = memberOf(sm.cand[k1], dx1, dy1) && !done;
+          if (__any_sync(0xffffffffu, in1))
           {
-            float dxk, dyk;
-            if (memberOf(sm.cand[k], dxk, dyk))
-              inMask |= 1u << k;
+            const uint32_t u1 = (uint32_t)__float2int_rn(wb_dir_units_f32(dy1, dx1)) & 0x7fffffffu;
+            if (in1)
+              addDir(u1);
           }
-        }
-        unsigned anyIn = __reduce_or_sync(0xffffffffu, inMask);
-        while (anyIn)
-        {
-          const int k = __ffs(anyIn) - 1;
-          anyIn &= anyIn - 1;
-          const int4 c = sm.cand[k];
-          const float dx = (float)(c.x - me.x) * sx, dy = (float)(c.y - me.y) * sy;
-          const uint32_t u = (uint32_t)__float2int_rn(wb_dir_units_f32(dy, dx)) & 0x7fffffffu;
-          if ((inMask >> k) & 1)
-            addDir(u);
         }
         __syncwarp();
 #ifdef WB_CLASSIFY_STATS
