@@ -111,6 +111,138 @@ __global__ void gatherRecordsKernel(const uint8_t *__restrict__ in, uint8_t *__r
   }
 }
 
+/* Stable partition of records by class byte, in two passes over tiles of
+ * kPartTile records: partCount writes each tile's class counts (class-major,
+ * so one scan gives every (class, tile) its first output record), and
+ * partScatter re-reads the tile, ranks its records within their class in
+ * input order (warps walk their records in order with match_any), and copies
+ * them word by word into the class runs of the output: consecutive threads
+ * write consecutive words of a run. */
+constexpr int kPartThreads = 256, kPartPer = 8, kPartTile = kPartThreads * kPartPer;
+
+__global__ void __launch_bounds__(kPartThreads) partCount(const uint8_t *__restrict__ rec, uint64_t n,
+                                                          uint32_t stride, int format, uint32_t numTiles,
+                                                          uint32_t *__restrict__ counts,
+                                                          unsigned long long *__restrict__ hist)
+{
+  __shared__ unsigned int h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    h[i] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)blockIdx.x * kPartTile;
+  for (int k = 0; k < kPartPer; k++)
+  {
+    const uint64_t i = base + (uint64_t)k * kPartThreads + threadIdx.x;
+    if (i < n)
+      atomicAdd(&h[classOf(rec + i * stride, format)], 1u);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < 256; c += blockDim.x)
+  {
+    counts[(uint64_t)c * numTiles + blockIdx.x] = h[c];
+    if (h[c])
+      atomicAdd(&hist[c], (unsigned long long)h[c]);
+  }
+}
+
+__global__ void __launch_bounds__(kPartThreads) partScatter(const uint8_t *__restrict__ rec, uint64_t n,
+                                                            uint32_t stride, int format, uint32_t numTiles,
+                                                            const uint32_t *__restrict__ offs,
+                                                            uint8_t *__restrict__ out)
+{
+  constexpr int W = kPartThreads / 32;
+  __shared__ uint32_t wcount[W][256];
+  __shared__ uint32_t localStart[256], globalStart[256];
+  __shared__ uint32_t order[kPartTile];   // tile record of each local (class-sorted) position
+  __shared__ uint8_t clsOf[kPartTile];    // class of each local position
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < W * 256; i += kPartThreads)
+    (&wcount[0][0])[i] = 0;
+  __syncthreads();
+  const uint64_t tbase = (uint64_t)blockIdx.x * kPartTile;
+  const uint32_t tileN = (uint32_t)(n - tbase < (uint64_t)kPartTile ? n - tbase : (uint64_t)kPartTile);
+  uint32_t rank[kPartPer];
+  uint8_t cl[kPartPer];
+  const unsigned lt = (1u << lane) - 1;
+  // warp w takes records [w*256, (w+1)*256) of the tile, 32 at a time, in order
+#pragma unroll
+  for (int q = 0; q < kPartPer; q++)
+  {
+    const uint32_t r = (uint32_t)warp * (kPartPer * 32) + q * 32 + lane;
+    const bool ok = r < tileN;
+    const uint32_t d = ok ? classOf(rec + (tbase + r) * stride, format) : 256u;
+    cl[q] = (uint8_t)d;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t pre = d < 256 ? wcount[warp][d] : 0;
+    rank[q] = pre + __popc(peers & lt);
+    __syncwarp();
+    if (d < 256 && (peers & lt) == 0)
+      wcount[warp][d] = pre + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += kPartThreads)
+  {
+    uint32_t run = 0;
+    for (int w = 0; w < W; w++)
+    {
+      const uint32_t c = wcount[w][d];
+      wcount[w][d] = run;
+      run += c;
+    }
+    localStart[d] = run;
+    globalStart[d] = offs[(uint64_t)d * numTiles + blockIdx.x];
+  }
+  __syncthreads();
+  if (warp == 0)
+  {
+    uint32_t c[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      c[q] = localStart[lane * 8 + q];
+      sum += c[q];
+    }
+    uint32_t inc = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o)
+        inc += v;
+    }
+    uint32_t run = inc - sum;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      localStart[lane * 8 + q] = run;
+      run += c[q];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < kPartPer; q++)
+  {
+    const uint32_t r = (uint32_t)warp * (kPartPer * 32) + q * 32 + lane;
+    if (r < tileN)
+    {
+      const uint32_t lp = localStart[cl[q]] + wcount[warp][cl[q]] + rank[q];
+      order[lp] = r;
+      clsOf[lp] = cl[q];
+    }
+  }
+  __syncthreads();
+  // copy: word w of the tile's class-ordered records goes to its class run
+  const uint32_t words = stride / 4;
+  const uint64_t total = (uint64_t)tileN * words;
+  for (uint64_t w = threadIdx.x; w < total; w += kPartThreads)
+  {
+    const uint32_t lp = (uint32_t)(w / words), k = (uint32_t)(w % words);
+    const uint32_t d = clsOf[lp];
+    const uint64_t dst = (uint64_t)globalStart[d] + (lp - localStart[d]);
+    ((uint32_t *)out)[dst * words + k] = ((const uint32_t *)rec)[(tbase + order[lp]) * words + k];
+  }
+}
+
 unsigned gridOf(const wb_ctx *c, uint64_t n)
 {
   return (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, (uint64_t)c->sm_count * 16);
@@ -236,12 +368,43 @@ int wb_las_split_by_class(wb_ctx *c, const void *records, uint64_t n, uint32_t s
     din = (const uint8_t *)rin.b.p;
     dout = (uint8_t *)rout.b.p;
   }
-  if ((rc = wb_ensure(c, hist.b, 256 * 8)) || (rc = wb_ensure(c, c->key0, n * 8)) ||
-      (rc = wb_ensure(c, c->key1, n * 8)) || (rc = wb_ensure(c, c->idx0, n * 4)) || (rc = wb_ensure(c, c->idx1, n * 4)))
+  if ((rc = wb_ensure(c, hist.b, 256 * 8)))
+    return rc;
+  WB_CUDA(c, cudaMemsetAsync(hist.b.p, 0, 256 * 8, c->stream));
+  if (stride % 4 == 0 && ((uintptr_t)din % 4 == 0) && ((uintptr_t)dout % 4 == 0))
+  {
+    // the stable partition: records read twice in order, written once
+    const uint64_t numTiles = (n + kPartTile - 1) / kPartTile;
+    WbScratch cnt(c), off(c);
+    if ((rc = wb_ensure(c, cnt.b, numTiles * 256 * 4 + 64)) || (rc = wb_ensure(c, off.b, numTiles * 256 * 4 + 64)))
+      return rc;
+    { partCount<<<(unsigned)numTiles, kPartThreads, 0, c->stream>>>(din, n, stride, point_format, (uint32_t)numTiles,
+                                                                   (uint32_t *)cnt.b.p,
+                                                                   (unsigned long long *)hist.b.p); ++c->launches; }
+    if ((rc = wb_exclusive_scan_u32(c, (const uint32_t *)cnt.b.p, (uint32_t *)off.b.p, numTiles * 256, nullptr)))
+      return rc;
+    { partScatter<<<(unsigned)numTiles, kPartThreads, 0, c->stream>>>(din, n, stride, point_format, (uint32_t)numTiles,
+                                                                     (const uint32_t *)off.b.p, dout); ++c->launches; }
+    uint64_t h[256];
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h, hist.b.p, sizeof h, cudaMemcpyDefault, c->stream);
+    if (e == cudaSuccess && !on_device)
+      e = cudaMemcpyAsync(out, dout, n * stride, cudaMemcpyDefault, c->stream);
+    if (e == cudaSuccess)
+      e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+      return wb_fail(c, WB_ECUDA, std::string("wb_las_split_by_class: ") + cudaGetErrorString(e));
+    for (int k = 0; k < 256; k++)
+      offsets[k + 1] = offsets[k] + h[k];
+    return 0;
+  }
+  // strides or bases that are not word multiples: class keys, one radix pass, a record gather
+  if ((rc = wb_ensure(c, c->key0, n * 8)) || (rc = wb_ensure(c, c->key1, n * 8)) ||
+      (rc = wb_ensure(c, c->idx0, n * 4)) || (rc = wb_ensure(c, c->idx1, n * 4)))
     return rc;
   uint64_t *keys = (uint64_t *)c->key0.p;
   uint32_t *idx = (uint32_t *)c->idx0.p;
-  WB_CUDA(c, cudaMemsetAsync(hist.b.p, 0, 256 * 8, c->stream));
   { classKeysKernel<<<gridOf(c, n), 256, 0, c->stream>>>(din, n, stride, point_format, keys, idx,
                                                          (unsigned long long *)hist.b.p); ++c->launches; }
   // one stable pass of the 8-bit digit: records keep their order within a class

@@ -465,7 +465,7 @@ struct WriteArgs
   uint8_t *out;
   uint64_t nLeaves;
   const uint32_t *leafFirst, *leafCount, *sidx;
-  const uint8_t *cls;
+  const uint8_t *cls;            /* class byte per stored point, in store order */
   uint32_t nSets;
   uint16_t setOf[256];           /* class byte -> set of files */
   unsigned long long *base;      /* per (block, set): next output record */
@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kBlock) setCountKernel(const WriteArgs a, uint
       const unsigned act = __ballot_sync(0xffffffffu, valid);
       if (valid)
       {
-        const uint32_t s = a.setOf[a.cls[a.sidx[first + c0 + lane]]];
+        const uint32_t s = a.setOf[a.cls[first + c0 + lane]];
         const unsigned gm = __match_any_sync(act, s);
         if (lane == __ffs(gm) - 1)
           counts[leaf * a.nSets + s] += __popc(gm);
@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(kBlock) writeKernel(const WriteArgs a)
       if (valid)
       {
         const uint32_t idx = a.sidx[first + c0 + lane];
-        const uint8_t cl = a.cls[idx];
+        const uint8_t cl = a.cls[first + c0 + lane];
         const uint32_t s = a.setOf[cl];
         loadRecord(si, a.rec + (uint64_t)idx * a.stride, Li.len, a.inWords);
         LasPt p;
@@ -616,15 +616,25 @@ __global__ void statInit(FileStat *st, uint32_t n)
   }
 }
 
-__global__ void storedTotals(uint64_t nd, const uint32_t *__restrict__ sidx, const uint8_t *__restrict__ cls,
-                             unsigned long long *__restrict__ totals)
+/* The class byte of every stored point in store order: from the last
+ * classify's store-order labels where a tile decided the point (sequential
+ * reads), else from the per-record class bytes (recCls). */
+__global__ void storeClassKernel(uint64_t nd, const uint32_t *__restrict__ sidx, const int32_t *__restrict__ owner,
+                                 const uint8_t *__restrict__ label, const uint8_t *__restrict__ recCls,
+                                 uint8_t *__restrict__ out)
+{
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
+    out[j] = (owner && owner[j] >= 0) ? label[j] : recCls[sidx[j]];
+}
+
+__global__ void storedTotals(uint64_t nd, const uint8_t *__restrict__ cls, unsigned long long *__restrict__ totals)
 {
   __shared__ unsigned int h[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x)
     h[i] = 0;
   __syncthreads();
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
-    atomicAdd(&h[cls[sidx[j]]], 1u);
+    atomicAdd(&h[cls[j]], 1u);
   __syncthreads();
   for (int i = threadIdx.x; i < 256; i += blockDim.x)
     if (h[i])
@@ -997,7 +1007,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   const uint64_t n = c->n, nd = c->nd, L = c->n_leaves;
   const Layout Li = layoutOf(in_format), Lo = layoutOf(opt->point_format);
   int rc;
-  WbScratch rin(c), cin(c), dout(c), tot(c), counts(c), bases(c), fileOf(c), stats(c);
+  WbScratch rin(c), cin(c), cstore(c), dout(c), tot(c), counts(c), bases(c), fileOf(c), stats(c);
 
   WriteArgs a;
   a.stride = cloud->stride;
@@ -1054,18 +1064,27 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
   else
     a.rec = nullptr;
   a.inWords = ((uintptr_t)a.rec % 4 == 0) && (a.stride % 4 == 0);
+  const uint8_t *recCls;
   if (!cls)
-    a.cls = c->clsFinal;
+    recCls = c->clsFinal;
   else if (cloud->device_resident)
-    a.cls = cls;
+    recCls = cls;
   else
   {
     if ((rc = wb_ensure(c, cin.b, n + 16)))
       return rc;
     WB_CUDA(c, cudaMemcpyAsync(cin.b.p, cls, n, cudaMemcpyDefault, c->stream));
-    a.cls = (const uint8_t *)cin.b.p;
+    recCls = (const uint8_t *)cin.b.p;
   }
   a.sidx = (const uint32_t *)c->sidx.p;
+  // class bytes in store order, read sequentially by every pass below
+  if ((rc = wb_ensure(c, cstore.b, nd + 16)))
+    return rc;
+  if (nd)
+    { storeClassKernel<<<gridOf(c, nd), kBlock, 0, c->stream>>>(
+          nd, a.sidx, (!cls && c->stage >= 3) ? (const int32_t *)c->owner.p : nullptr, (const uint8_t *)c->label.p, recCls,
+          (uint8_t *)cstore.b.p); ++c->launches; }
+  a.cls = (const uint8_t *)cstore.b.p;
   a.leafFirst = (const uint32_t *)c->leafFirst.p;
   a.leafCount = (const uint32_t *)c->leafCount.p;
   a.nLeaves = L;
@@ -1075,7 +1094,7 @@ int wb_las_write_output(wb_ctx *c, const wb_cloud *cloud, int in_format, const u
     return rc;
   WB_CUDA(c, cudaMemsetAsync(tot.b.p, 0, 256 * 8, c->stream));
   if (nd)
-    { storedTotals<<<gridOf(c, nd), kBlock, 0, c->stream>>>(nd, a.sidx, a.cls, (unsigned long long *)tot.b.p); ++c->launches; }
+    { storedTotals<<<gridOf(c, nd), kBlock, 0, c->stream>>>(nd, a.cls, (unsigned long long *)tot.b.p); ++c->launches; }
   uint64_t T[256];
   WB_CUDA(c, cudaMemcpyAsync(T, tot.b.p, sizeof T, cudaMemcpyDefault, c->stream));
   WB_CUDA(c, cudaStreamSynchronize(c->stream));
