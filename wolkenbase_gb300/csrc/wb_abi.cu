@@ -122,7 +122,7 @@ void wb_release_buffers(wb_ctx *c)
                    &c->leafLevel, &c->leafKey, &c->leafBox, &c->sidx, &c->sx, &c->sy, &c->sz, &c->pointLeaf,
                    &c->storeOf, &c->survivorOf, &c->nodeChild, &c->nodeBox, &c->nodeStart, &c->nodeIdLevel,
                    &c->tileEx, &c->tileEy, &c->tileLookup, &c->tileStart, &c->tilePts, &c->owner, &c->tileRes,
-                   &c->tileHuge, &c->hugePre,
+                   &c->tileHuge, &c->hugePre, &c->scanTot,
                    &c->tileH, &c->tileN, &c->tileNg, &c->label, &c->clsDev, &c->ambiguous, &c->deferred, &c->angleT,
                    &c->flowCache, &c->gKey0, &c->gKey1, &c->gVal0, &c->gVal1, &c->stray, &c->cellStart,
                    &c->gpt, &c->cellRec, &c->superRec, &c->ptSetup, &c->groups, &c->groupCnt, &c->lasAngles,

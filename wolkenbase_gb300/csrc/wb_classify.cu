@@ -117,6 +117,7 @@ struct ClsArgs
   uint8_t *label;
   /* grid */
   double gx0, gy0, cell;
+  double invSlope2, invCell, invSuper;   /* 1/slope^2, 1/cell, 1/(WB_SUPER cell): reach bounds only */
   int nx, ny;
   uint64_t ncell;
   const int4 *col;     /* two int4 per column: {x0, y0, x1, y1}, {zmin, begin, end, flags} */
@@ -361,13 +362,15 @@ __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
   s.por2f = (float)por2;
   // horizontal reach of the hyperboloid at the lowest point of the cloud
   double zdMax = cz - a.zmin;
-  double reach2 = (zdMax * zdMax - por2) / (a.slope * a.slope);
+  // (products with reciprocals: reach carries a 1e-6 margin, far above their
+  // rounding, so the ring counts still cover it)
+  double reach2 = (zdMax * zdMax - por2) * a.invSlope2;
   double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
   double fi = floor((px - a.gx0) / a.cell), fj = floor((py - a.gy0) / a.cell);
   s.ci = (int32_t)fmax(fmin(fi, 1e9), -1e9);
   s.cj = (int32_t)fmax(fmin(fj, 1e9), -1e9);
-  s.kmax = (int32_t)fmin(ceil(reach / a.cell) + 1, 1e9);
-  s.smax = (int32_t)fmin(ceil(reach / (WB_SUPER * a.cell)) + 1, 1e9);
+  s.kmax = (int32_t)fmin(ceil(reach * a.invCell) + 1, 1e9);
+  s.smax = (int32_t)fmin(ceil(reach * a.invSuper) + 1, 1e9);
   a.setup[j] = s;
 }
 
@@ -1155,9 +1158,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         // when some lane has a candidate inside.  Two candidates a step: their
         // FP32 tests and directions are independent, so their latencies
         // overlap (31% faster than one a step; the bins are minima and maxima,
-        // so the order of the two updates does not matter).  Testing a whole
-        // chunk first and forming the directions afterwards measured 40%
-        // slower than one a step.
+        // so the order of the two updates does not matter).  Four a step
+        // measured 35% slower than two (register spills), and testing a whole
+        // chunk first and forming the directions afterwards 40% slower than one.
         while (lm)
         {
           const int k1 = __ffs(lm) - 1;
@@ -1450,6 +1453,9 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.gx0 = c->grid.x0;
   a.gy0 = c->grid.y0;
   a.cell = c->grid.cell;
+  a.invSlope2 = 1.0 / (p->max_slope * p->max_slope);
+  a.invCell = 1.0 / c->grid.cell;
+  a.invSuper = 1.0 / (WB_SUPER * c->grid.cell);
   a.nx = c->grid.nx;
   a.ny = c->grid.ny;
   a.ncell = c->grid.ncell;
@@ -1654,10 +1660,12 @@ __global__ void batchPrefix(const BatchHdr *__restrict__ h, BatchOut *__restrict
   out[h->k] = s;
 }
 
-__global__ void batchZeroGround(const BatchHdr *__restrict__ h)
+__global__ void batchZeroGround(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
 {
   const int k = h->k;
   const uint64_t total = h->startT[k];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < k; q += gridDim.x * blockDim.x)
+    o->ground[q] = 0;
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
   {
     int q = batchJob(h->startT, k, g);
@@ -1665,43 +1673,38 @@ __global__ void batchZeroGround(const BatchHdr *__restrict__ h)
   }
 }
 
-__global__ void batchGroundCount(const BatchHdr *__restrict__ h)
+__global__ void batchGroundCount(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
 {
   const int k = h->k;
   const uint64_t total = h->startNd[k];
-  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x)
+  const int lane = threadIdx.x & 31;
+  // whole warps step together, so the ground points of a warp are counted
+  // with one atomic per tile and one per job
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < total; w0 += stride)
   {
-    int q = batchJob(h->startNd, k, g);
-    const ClsArgs &a = h->jobs[q];
-    uint64_t j = g - h->startNd[q];
-    int32_t t = a.owner[j];
-    if (t >= 0 && a.label[j] == 2)
-      atomicAdd(&((TileRes *)a.tiles)[t].nGround, 1);
-  }
-}
-
-/* Block q sums job q's per-tile ground counts. */
-__global__ void batchGroundTotal(const BatchHdr *__restrict__ h, BatchOut *__restrict__ o)
-{
-  __shared__ unsigned long long part[8];
-  const int q = blockIdx.x;
-  if (q >= h->k)
-    return;
-  const ClsArgs &a = h->jobs[q];
-  unsigned long long s = 0;
-  for (uint64_t t = threadIdx.x; t < a.nTiles; t += blockDim.x)
-    s += (unsigned)a.tiles[t].nGround;
-  for (int d = 16; d; d >>= 1)
-    s += __shfl_down_sync(0xffffffffu, s, d);
-  if ((threadIdx.x & 31) == 0)
-    part[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0)
-  {
-    unsigned long long tot = 0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
-      tot += part[i];
-    o->ground[q] = tot;
+    const uint64_t g = w0 + lane;
+    bool gnd = false;
+    int q = 0;
+    int32_t t = -1;
+    if (g < total)
+    {
+      q = batchJob(h->startNd, k, g);
+      const ClsArgs &a = h->jobs[q];
+      const uint64_t j = g - h->startNd[q];
+      t = a.owner[j];
+      gnd = t >= 0 && a.label[j] == 2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, gnd);
+    if (gnd)
+    {
+      const unsigned sameT = __match_any_sync(m, ((unsigned long long)q << 32) | (uint32_t)t);
+      if (lane == __ffs(sameT) - 1)
+        atomicAdd(&((TileRes *)h->jobs[q].tiles)[t].nGround, __popc(sameT));
+      const unsigned sameQ = __match_any_sync(m, q);
+      if (lane == __ffs(sameQ) - 1)
+        atomicAdd(&o->ground[q], (unsigned long long)__popc(sameQ));
+    }
   }
 }
 
@@ -1797,9 +1800,9 @@ cudaError_t ringsGrid(WbBatch *b, int shape, unsigned *grid)
 }
 
 /* The fused classify on stream s: upload of the job table, set-up, the
- * persistent fast pass, the ambiguous prefix, the persistent exact pass,
- * ground counts, the class-byte scatter and the read-back of the per-job
- * totals (8 kernels).  With mark, stage events go on mark's stream. */
+ * persistent fast pass, the deferred prefix and one-point pass, the ambiguous
+ * prefix and exact pass, ground counts (per tile and per job), the
+ * class-byte scatter and the read-back of the per-job totals (9 kernels).  With mark, stage events go on mark's stream. */
 cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned grids[3], wb_ctx *mark)
 {
   const unsigned grid = (unsigned)b->sm * 8;
@@ -1816,9 +1819,8 @@ cudaError_t enqueueBatch(WbBatch *b, cudaStream_t s, int shape, const unsigned g
   ringsFn(kExactPass)<<<grids[2], 32 * ringsWarps(kExactPass), 0, s>>>(b->dIn, b->dOut);
   if (mark)
     wb_mark(mark, "classify_exact");
-  batchZeroGround<<<grid, 256, 0, s>>>(b->dIn);
-  batchGroundCount<<<grid, 256, 0, s>>>(b->dIn);
-  batchGroundTotal<<<WB_BATCH_MAX, 256, 0, s>>>(b->dIn, b->dOut);
+  batchZeroGround<<<grid, 256, 0, s>>>(b->dIn, b->dOut);
+  batchGroundCount<<<grid, 256, 0, s>>>(b->dIn, b->dOut);
   batchScatter<<<grid, 256, 0, s>>>(b->dIn);
   e = cudaMemcpyAsync(b->hOut, b->dOut, sizeof(BatchOut), cudaMemcpyDefault, s);
   if (e == cudaSuccess)
@@ -2036,7 +2038,7 @@ int wb_batch_launch(WbBatch *b, wb_ctx *const *jobs, int k, cudaStream_t s, int 
     return WB_ECUDA;
   }
   if (launches)
-    *launches += 10;   /* kernel nodes of the graph */
+    *launches += 9;   /* kernel nodes of the graph */
   return 0;
 }
 
@@ -2072,7 +2074,7 @@ int wb_classify_impl(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDevice)
   unsigned grids[3];
   WB_CUDA(c, batchGrids(b, shape, grids));
   WB_CUDA(c, enqueueBatch(b, c->stream, shape, grids, c));
-  c->launches += 10;
+  c->launches += 9;
   ClsArgs *a = (ClsArgs *)c->clsArgs;
   if (!onDevice && c->n)
     WB_CUDA(c, cudaMemcpyAsync(cls, a->cls, c->n, cudaMemcpyDefault, c->stream));

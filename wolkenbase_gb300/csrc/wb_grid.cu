@@ -35,18 +35,27 @@ struct GridArgs
 
 __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                            const int32_t *__restrict__ sz, uint64_t *__restrict__ key, uint32_t *__restrict__ val,
-                           uint8_t *__restrict__ stray, unsigned long long *__restrict__ nStray)
+                           uint8_t *__restrict__ stray, unsigned long long *__restrict__ nStray,
+                           int *__restrict__ ext)
 {
+  // record-integer extent of the points ({min x, y, z}, {max x, y, z})
+  int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.nd; j += (uint64_t)gridDim.x * blockDim.x)
   {
-    double x = wb_decode(sx[j], g.off[0], g.scale[0], g.unit);
-    double y = wb_decode(sy[j], g.off[1], g.scale[1], g.unit);
-    double z = wb_decode(sz[j], g.off[2], g.scale[2], g.unit);
+    const int q[3] = {sx[j], sy[j], sz[j]};
+    for (int a = 0; a < 3; a++)
+    {
+      mn[a] = min(mn[a], q[a]);
+      mx[a] = max(mx[a], q[a]);
+    }
+    double x = wb_decode(q[0], g.off[0], g.scale[0], g.unit);
+    double y = wb_decode(q[1], g.off[1], g.scale[1], g.unit);
+    double z = wb_decode(q[2], g.off[2], g.scale[2], g.unit);
     int cx = (int)floor((x - g.x0) / g.cell), cy = (int)floor((y - g.y0) / g.cell);
     cx = min(max(cx, 0), g.nx - 1);
     cy = min(max(cy, 0), g.ny - 1);
     // column in the high 32 bits, height (order-preserving int32 -> uint32) below
-    key[j] = (((uint64_t)cy * g.nx + cx) << 32) | (uint32_t)(sz[j] ^ (int32_t)0x80000000);
+    key[j] = (((uint64_t)cy * g.nx + cx) << 32) | (uint32_t)(q[2] ^ (int32_t)0x80000000);
     val[j] = (uint32_t)j;
     bool sxy = x < g.rootLo[0] || y < g.rootLo[1] || x >= g.rootHi[0] || y >= g.rootHi[1];
     bool s = sxy || z < g.rootLo[2] || z >= g.rootHi[2];
@@ -54,6 +63,18 @@ __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int
     if (s)
       atomicAdd(nStray, 1ull);
   }
+  for (int a = 0; a < 3; a++)
+    for (int o = 16; o; o >>= 1)
+    {
+      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; a++)
+    {
+      atomicMin(&ext[a], mn[a]);
+      atomicMax(&ext[3 + a], mx[a]);
+    }
 }
 
 __global__ void cellStartKernel(uint64_t nd, uint64_t ncell, const uint64_t *__restrict__ key,
@@ -141,33 +162,6 @@ __global__ void groupFillKernel(uint64_t ncell, const int4 *__restrict__ rec, co
 }
 
 /* Record-integer extent of the cloud: out[0..2] minima, out[3..5] maxima. */
-__global__ void extentKernel(uint64_t nd, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
-                             const int32_t *__restrict__ sz, int *__restrict__ out)
-{
-  int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nd; j += (uint64_t)gridDim.x * blockDim.x)
-  {
-    int q[3] = {sx[j], sy[j], sz[j]};
-    for (int a = 0; a < 3; a++)
-    {
-      mn[a] = min(mn[a], q[a]);
-      mx[a] = max(mx[a], q[a]);
-    }
-  }
-  for (int a = 0; a < 3; a++)
-    for (int o = 16; o; o >>= 1)
-    {
-      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-    }
-  if ((threadIdx.x & 31) == 0)
-    for (int a = 0; a < 3; a++)
-    {
-      atomicMin(&out[a], mn[a]);
-      atomicMax(&out[3 + a], mx[a]);
-    }
-}
-
 /* Records of each block of WB_SUPER x WB_SUPER columns (the column record
  * layout; begin/end unused). */
 __global__ void superKernel(int nx, int ny, int snx, int sny, const int4 *__restrict__ rec, int4 *__restrict__ srec)
@@ -247,9 +241,8 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   uint64_t *key = (uint64_t *)c->gKey0.p;
   uint32_t *val = (uint32_t *)c->gVal0.p;
   { cellKernel<<<blocks, 256, 0, c->stream>>>(a, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
-                                              (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray); ++c->launches; }
-  { extentKernel<<<blocks, 256, 0, c->stream>>>(nd, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
-                                                (const int32_t *)c->sz.p, dExt); ++c->launches; }
+                                              (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray,
+                                              dExt); ++c->launches; }
   int bits = 1;
   while ((1ull << bits) < ncell)
     bits++;

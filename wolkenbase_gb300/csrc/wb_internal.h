@@ -74,7 +74,8 @@ struct wb_ctx
   DevBuf leafFirst, leafCount, leafLevel, leafKey, leafBox;
   DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
-  DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre;
+  DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre,
+      scanTot;
   DevBuf label, clsDev, ambiguous, deferred, angleT;
   /* column grid (wb_grid.cu): gpt holds one int4 {X, Y, Z, store position |
      stray bit} per point in column order; cellRec two int4 per column,

@@ -407,7 +407,7 @@ struct ScanArgs
 
 constexpr int kQ = 8;   // summed quantities: xx, yx, yy, x, y, xz, yz, z
 constexpr int kScanCache = 224;   // tile points whose coordinates stay in shared memory
-constexpr int kScanWarps = 6;     // tiles per block of the exact scan (one solve lane each); 41 KB of shared memory
+constexpr int kScanWarps = 6;     // tiles (one warp each) per block of the exact scan's sums and shape passes
 
 __device__ __forceinline__ void counterMergeGroup(double *part, uint64_t i, double g)
 {
@@ -559,7 +559,7 @@ __device__ void rowOp3(double m[3][3], double b[3], int row0, int row1, int piv)
   }
 }
 
-/* The histogram sector of a bottom point (scan.cpp:96-106): 0 inside the
+/* The histogram sector of a bottom point (scan.cpp:93-101): 0 inside the
  * inner circle hypot(x, y) < rin, else 1 + (rint(atan2(y, x) * 3 / pi) mod 6).
  * FP32 decides wherever it is at least 1e-5 (relative) away from the circle
  * and from a sector boundary (a half-integer of atan2 * 3 / pi); the rest is
@@ -589,27 +589,197 @@ __device__ __forceinline__ int sectorOf(double x, double y, double rin)
   return (sector % 6) + 1;
 }
 
-__global__ void __launch_bounds__(32 * kScanWarps) scanKernel(ScanArgs s, TileRes *__restrict__ res)
+/* scanCylinder in five kernels.  The FP64 pipe bounds this stage, and an
+ * FP64 instruction costs the same whether one lane or 32 run it, so each part
+ * runs at the width that keeps its lanes busy: the per-point passes one warp
+ * per tile (lanes over points), everything done once per tile (centre, the
+ * reference's 3x3 Gauss-Jordan, the slope clamp, density and height) one
+ * thread per tile.  A tile's intermediate values live in one ScanWork slot. */
+union ScanWork
+{
+  double sums[kQ];   // scanSums -> scanSolve: the eight normal-equation sums
+  struct
+  {
+    double sx, sy;          // scanSolve -> scanShape: the slope clamped to length 1
+    double top, bottom;     // scanShape -> scanFinish
+    uint32_t histo[7], nBottom;
+  } s;
+};
+
+/* Tile centres (Flowsnake::cyl), one thread per tile. */
+__global__ void scanPrep(TileArgs a, double2 *__restrict__ ctr)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    double cx, cy;
+    tileCenter(a, k, cx, cy);
+    ctr[k] = make_double2(cx, cy);
+  }
+}
+
+/* Pass 1: the eight sums of the normal equations that linearLeastSquares
+ * forms from the tile's points (scan.cpp:60-68, matrix.cpp:194, 211) in the
+ * reference's pairwise order (pairwisesum's binary counter over the points in
+ * store order). */
+__global__ void __launch_bounds__(32 * kScanWarps) scanSums(ScanArgs s, const double2 *__restrict__ ctr,
+                                                             ScanWork *__restrict__ work)
 {
   __shared__ double part[kScanWarps][kQ][kLevels];
   __shared__ double tail[kScanWarps][kQ][8];
-  // tile-local coordinates of tiles up to kScanCache points, decoded once
-  __shared__ double cxy[kScanWarps][3][kScanCache];
-  // the block's solves: sums in, plane and clamped slope out
-  __shared__ double tots[kScanWarps][kQ];
-  __shared__ double planes[kScanWarps][5];
-  __shared__ uint32_t counts[kScanWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const TileArgs &a = s.t;
-  uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
-  const bool live = k < a.T;
-  uint32_t b0 = live ? s.tileStart[k] : 0, M = live ? s.tileN[k] : 0;
-  TileRes r{};
-  double cx = 0, cy = 0;
-  if (live)
-    tileCenter(a, k, cx, cy);
-  uint64_t G = M / 8;   // complete groups of eight
+  const uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
+  if (k >= a.T)
+    return;
+  const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
+  if (M == 0)
+    return;
+  const double cx = ctr[k].x, cy = ctr[k].y;
+  const uint64_t G = M / 8;   // complete groups of eight
+  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  {
+    uint32_t i = c0 + lane;
+    double q[kQ];
+    if (i < M)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      q[0] = x * x;
+      q[1] = y * x;
+      q[2] = y * y;
+      q[3] = 1.0 * x;
+      q[4] = 1.0 * y;
+      q[5] = x * z;
+      q[6] = y * z;
+      q[7] = 1.0 * z;
+    }
+    else
+      for (int u = 0; u < kQ; u++)
+        q[u] = 0;
+    uint64_t grp = i / 8;
+    // fixed tree inside each group of eight, ((a0+a1)+(a2+a3))+((a4+a5)+(a6+a7)),
+    // for the eight quantities of the chunk's four groups: 224 additions in
+    // seven FP64 instructions.  At each level a lane and its partner split
+    // the quantities they both hold, so every lane's addition is a useful
+    // one (addition commutes exactly; only the grouping is fixed).
+    const bool l0 = lane & 1, l1 = (lane >> 1) & 1, l2 = (lane >> 2) & 1;
+    double s1[4], s2[2], g;
+#pragma unroll
+    for (int r = 0; r < 4; r++)   // pairs: quantity 4*l0 + r
+    {
+      const double give = l0 ? q[r] : q[4 + r];
+      s1[r] = (l0 ? q[4 + r] : q[r]) + __shfl_xor_sync(0xffffffffu, give, 1);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; t++)   // quads: quantity 4*l0 + 2*l1 + t
+    {
+      const double give = l1 ? s1[t] : s1[2 + t];
+      s2[t] = (l1 ? s1[2 + t] : s1[t]) + __shfl_xor_sync(0xffffffffu, give, 2);
+    }
+    {                             // groups: quantity 4*l0 + 2*l1 + l2
+      const double give = l2 ? s2[0] : s2[1];
+      g = (l2 ? s2[1] : s2[0]) + __shfl_xor_sync(0xffffffffu, give, 4);
+    }
+    // lanes 0-7 merge their quantity for the up-to-4 complete groups of the
+    // chunk, in group order (lane l + 8 gq holds group gq of the same quantity)
+    const int uq = 4 * l0 + 2 * l1 + l2;
+    for (int gq = 0; gq < 4; gq++)
+    {
+      const uint64_t gi = (uint64_t)c0 / 8 + gq;
+      const double gv = __shfl_sync(0xffffffffu, g, (lane & 7) + 8 * gq);
+      if (gi < G && lane < 8)
+        counterMergeGroup(part[w][uq], gi * 8, gv);
+    }
+    // stash the trailing incomplete group's values
+    if (i < M && grp == G)
+      for (int u = 0; u < kQ; u++)
+        tail[w][u][i - G * 8] = q[u];
+    __syncwarp();
+  }
+  if (lane < kQ)
+  {
+    for (uint64_t i = G * 8; i < M; i++)
+      counterMergeOne(part[w][lane], i, tail[w][lane][i - G * 8]);
+    work[k].sums[lane] = pairwiseFinish(part[w][lane], M);
+  }
+}
+
+/* The normal equations of each tile solved by one thread (matrix.cpp:262-422):
+ * the plane goes into the tile's result, the slope clamped to length 1
+ * (scan.cpp:69-73) into its work slot. */
+__global__ void scanSolve(uint64_t T, const uint32_t *__restrict__ tileN, ScanWork *__restrict__ work,
+                          TileRes *__restrict__ res)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const uint32_t M = tileN[k];
+    if (M == 0)
+      continue;
+    double t[kQ];
+    for (int u = 0; u < kQ; u++)
+      t[u] = work[k].sums[u];
+    double m[3][3] = {{t[0], t[1], t[3]}, {t[1], t[2], t[4]}, {t[3], t[4], (double)M}};
+    double bv[3] = {t[5], t[6], t[7]};
+    for (int i = 0; i < 3; i++)
+    {
+      findPivot3(m, bv, i, i);
+      for (int j = 0; j < 3; j++)
+        rowOp3(m, bv, i, j, i);
+    }
+    for (int i = 2; i >= 0; i--)
+      for (int j = 0; j < i; j++)
+        rowOp3(m, bv, i, j, i);
+    const double v0 = m[0][0] == 0 ? NAN : bv[0], v1 = m[1][1] == 0 ? NAN : bv[1];
+    res[k].plane[0] = v0;
+    res[k].plane[1] = v1;
+    res[k].plane[2] = m[2][2] == 0 ? NAN : bv[2];
+    double sx = v0, sy = v1;
+    const double len = wb_hypot(sx, sy);
+    if (len > 1)
+    {
+      sx /= len;
+      sy /= len;
+    }
+    if (isnan(sx) || isnan(sy))
+      sx = sy = 0;
+    work[k].s.sx = sx;
+    work[k].s.sy = sy;
+  }
+}
+
+/* Passes 2-4 of scanCylinder (scan.cpp:74-102): untilt by the clamped
+ * slope, bottom (first minimum), bottom2 (minimum before it), top and the
+ * sector histogram of the bottom points.  Each lane keeps its own minimum (with its first index), maximum
+ * and bottom2 over its points and the warp combines them once per tile:
+ * the first minimum is the least (height, index) pair whatever the order,
+ * and fmin / fmax give the same value in any order (they order -0 below +0). */
+__global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const double2 *__restrict__ ctr,
+                                                              ScanWork *__restrict__ work)
+{
+  // tile-local coordinates and untilted heights of tiles up to kScanCache
+  // points, computed once
+  __shared__ double cxy[kScanWarps][4][kScanCache];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const TileArgs &a = s.t;
+  const uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
+  if (k >= a.T)
+    return;
+  const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
+  if (M == 0)
+    return;
+  const double cx = ctr[k].x, cy = ctr[k].y;
   const bool cached = M <= kScanCache;
+  if (cached)
+  {
+    for (uint32_t i = lane; i < M; i += 32)
+    {
+      uint32_t j = s.tilePts[b0 + i];
+      cxy[w][0][i] = dec(a, 0, a.sx[j]) - cx;
+      cxy[w][1][i] = dec(a, 1, a.sy[j]) - cy;
+      cxy[w][2][i] = dec(a, 2, a.sz[j]) - 0.0;
+    }
+    __syncwarp();
+  }
   // coordinates of tile point i: from the cache, or decoded again
   auto coords = [&](uint32_t i, double &x, double &y, double &z) {
     if (cached)
@@ -626,192 +796,67 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanKernel(ScanArgs s, TileRe
       z = dec(a, 2, a.sz[j]) - 0.0;
     }
   };
-  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  const double sx = work[k].s.sx, sy = work[k].s.sy;
+  // untilted height of tile point i (cached tiles: from the cache once pass 2 stored it)
+  auto untilted = [&](uint32_t i) -> double {
+    if (cached)
+      return cxy[w][3][i];
+    double x, y, z;
+    coords(i, x, y, z);
+    return z - (sy * y + sx * x);
+  };
+  // untilt: bottom (first minimum), top
+  double mv = INFINITY, top = -INFINITY;
+  uint32_t mi = 0xffffffffu;
+  for (uint32_t i = lane; i < M; i += 32)
   {
-    uint32_t i = c0 + lane;
-    double q[kQ];
-    if (i < M)
+    double x, y, z;
+    coords(i, x, y, z);
+    const double uz = z - (sy * y + sx * x);
+    if (cached)
+      cxy[w][3][i] = uz;
+    if (uz < mv)
     {
-      uint32_t j = s.tilePts[b0 + i];
-      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
-      if (cached)
-      {
-        cxy[w][0][i] = x;
-        cxy[w][1][i] = y;
-        cxy[w][2][i] = z;
-      }
-      q[0] = x * x;
-      q[1] = y * x;
-      q[2] = y * y;
-      q[3] = 1.0 * x;
-      q[4] = 1.0 * y;
-      q[5] = x * z;
-      q[6] = y * z;
-      q[7] = 1.0 * z;
+      mv = uz;
+      mi = i;
     }
-    else
-      for (int u = 0; u < kQ; u++)
-        q[u] = 0;
-    uint64_t grp = i / 8;
-    // fixed tree inside each group of eight: ((a0+a1)+(a2+a3))+((a4+a5)+(a6+a7))
-    double gs[kQ];
-    for (int u = 0; u < kQ; u++)
-    {
-      double v = q[u];
-      v = v + __shfl_xor_sync(0xffffffffu, v, 1);
-      v = v + __shfl_xor_sync(0xffffffffu, v, 2);
-      v = v + __shfl_xor_sync(0xffffffffu, v, 4);
-      gs[u] = v;
-    }
-    // lane u (< kQ) merges quantity u for the up-to-4 complete groups of the chunk
-    for (int gq = 0; gq < 4; gq++)
-    {
-      uint64_t gi = (uint64_t)c0 / 8 + gq;
-      double gv[kQ];
-      for (int u = 0; u < kQ; u++)
-        gv[u] = __shfl_sync(0xffffffffu, gs[u], gq * 8);
-      if (gi < G && lane < kQ)
-      {
-        double g = gv[0];
-        for (int u = 1; u < kQ; u++)
-          if (lane == u)
-            g = gv[u];
-        counterMergeGroup(part[w][lane], gi * 8, g);
-      }
-    }
-    // stash the trailing incomplete group's values
-    if (i < M && grp == G)
-      for (int u = 0; u < kQ; u++)
-        tail[w][u][i - G * 8] = q[u];
-    __syncwarp();
+    top = fmax(top, uz);
   }
-  if (lane < kQ)
+  for (int o = 16; o; o >>= 1)
   {
-    for (uint64_t i = G * 8; i < M; i++)
-      counterMergeOne(part[w][lane], i, tail[w][lane][i - G * 8]);
+    const double ov = __shfl_xor_sync(0xffffffffu, mv, o);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
+    if (ov < mv || (ov == mv && oi < mi))
+    {
+      mv = ov;
+      mi = oi;
+    }
+    top = fmax(top, __shfl_xor_sync(0xffffffffu, top, o));
   }
+  const double bottom = mv < INFINITY ? mv : INFINITY;
+  const uint32_t argmin = mv < INFINITY ? mi : 0xffffffffu;
   __syncwarp();
-  if (lane < kQ)
-    tots[w][lane] = pairwiseFinish(part[w][lane], M);
-  if (lane == 0)
-    counts[w] = M;
-  __syncthreads();
-  // one lane per tile solves the block's normal equations (matrix.cpp:262-422)
-  if (w == 0 && lane < kScanWarps && counts[lane] > 0)
-  {
-    const double *tot = tots[lane];
-    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)counts[lane]}};
-    double bv[3] = {tot[5], tot[6], tot[7]};
-    for (int i = 0; i < 3; i++)
-    {
-      findPivot3(m, bv, i, i);
-      for (int j = 0; j < 3; j++)
-        rowOp3(m, bv, i, j, i);
-    }
-    for (int i = 2; i >= 0; i--)
-      for (int j = 0; j < i; j++)
-        rowOp3(m, bv, i, j, i);
-    double v0 = bv[0], v1 = bv[1];
-    if (m[0][0] == 0)
-      v0 = NAN;
-    if (m[1][1] == 0)
-      v1 = NAN;
-    double px = v0, py = v1;
-    double len = wb_hypot(px, py);
-    if (len > 1)
-    {
-      px /= len;
-      py /= len;
-    }
-    if (isnan(px) || isnan(py))
-      px = py = 0;
-    planes[lane][0] = v0;
-    planes[lane][1] = v1;
-    planes[lane][2] = m[2][2] == 0 ? NAN : bv[2];
-    planes[lane][3] = px;
-    planes[lane][4] = py;
-  }
-  __syncthreads();
-  if (!live)
-    return;
-  if (M == 0)
-  {
-    if (lane == 0)
-      res[k] = r;
-    return;
-  }
-  r.plane[0] = planes[w][0];
-  r.plane[1] = planes[w][1];
-  r.plane[2] = planes[w][2];
-  const double sx = planes[w][3], sy = planes[w][4];
-  // untilt: bottom (first minimum), bottom2 (running minimum before it), top
-  double bottom = INFINITY, top = -INFINITY;
-  uint32_t argmin = 0xffffffffu;
-  for (uint32_t c0 = 0; c0 < M; c0 += 32)
-  {
-    uint32_t i = c0 + lane;
-    double uz = INFINITY, ut = -INFINITY;
-    if (i < M)
-    {
-      double x, y, z;
-      coords(i, x, y, z);
-      double zz = sy * y + sx * x;
-      uz = z - zz;
-      ut = uz;
-    }
-    // chunk minimum with first index
-    double mv = uz;
-    uint32_t mi = (i < M && uz < INFINITY) ? i : 0xffffffffu;
-    for (int o = 16; o; o >>= 1)
-    {
-      double ov = __shfl_xor_sync(0xffffffffu, mv, o);
-      uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
-      if (ov < mv || (ov == mv && oi < mi))
-      {
-        mv = ov;
-        mi = oi;
-      }
-    }
-    if (mv < bottom)
-    {
-      bottom = mv;
-      argmin = mi;
-    }
-    double tv = ut;
-    for (int o = 16; o; o >>= 1)
-      tv = fmax(tv, __shfl_xor_sync(0xffffffffu, tv, o));
-    top = fmax(top, tv);
-  }
+  // bottom2: the lowest untilted height before the first minimum
   double bottom2 = INFINITY;
+  for (uint32_t i = lane; i < M && i < argmin; i += 32)
+    bottom2 = fmin(bottom2, untilted(i));
+  for (int o = 16; o; o >>= 1)
+    bottom2 = fmin(bottom2, __shfl_xor_sync(0xffffffffu, bottom2, o));
+  if (isinf(bottom2))
+    bottom2 = bottom;
+  // sector histogram of the points within 2 rad of bottom2
+  const double zcut = bottom2 + 2 * a.rad, rin = a.rad / 2.6457513110645905905016;
   uint32_t nBottom = 0;
   int histo[7] = {0, 0, 0, 0, 0, 0, 0};
   for (uint32_t c0 = 0; c0 < M; c0 += 32)
   {
     uint32_t i = c0 + lane;
-    double v = INFINITY;
-    if (i < M && i < argmin)
-    {
-      double x, y, z;
-      coords(i, x, y, z);
-      v = z - (sy * y + sx * x);
-    }
-    for (int o = 16; o; o >>= 1)
-      v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    bottom2 = fmin(bottom2, v);
-  }
-  if (isinf(bottom2))
-    bottom2 = bottom;
-  for (uint32_t c0 = 0; c0 < M; c0 += 32)
-  {
-    uint32_t i = c0 + lane;
     int sector = -1;
-    if (i < M)
+    if (i < M && untilted(i) < zcut)
     {
       double x, y, z;
       coords(i, x, y, z);
-      double uz = z - (sy * y + sx * x);
-      if (uz < bottom2 + 2 * a.rad)
-        sector = sectorOf(x, y, a.rad / 2.6457513110645905905016);
+      sector = sectorOf(x, y, rin);
     }
     for (int sct = 0; sct < 7; sct++)
       histo[sct] += __popc(__ballot_sync(0xffffffffu, sector == sct));
@@ -819,23 +864,50 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanKernel(ScanArgs s, TileRe
   }
   if (lane == 0)
   {
+    ScanWork &o = work[k];
+    o.s.top = top;
+    o.s.bottom = bottom;
+    for (int i = 0; i < 7; i++)
+      o.s.histo[i] = (uint32_t)histo[i];
+    o.s.nBottom = nBottom;
+  }
+}
+
+/* Density, tree flags, h and height of each tile (scan.cpp:103-120), one
+ * thread per tile. */
+__global__ void scanFinish(uint64_t T, const uint32_t *__restrict__ tileN, const ScanWork *__restrict__ work,
+                           double rad, double minH, TileRes *__restrict__ res)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const uint32_t M = tileN[k];
+    TileRes r{};
+    if (M == 0)
+    {
+      res[k] = r;
+      continue;
+    }
+    const ScanWork &o = work[k];
+    r.plane[0] = res[k].plane[0];
+    r.plane[1] = res[k].plane[1];
+    r.plane[2] = res[k].plane[2];
     double density = 0;
     int treeFlags = 0;
     for (int i = 0; i < 7; i++)
-      density += (double)histo[i] * (double)histo[i];
-    if (M > nBottom && density < 7)
+      density += (double)(int)o.s.histo[i] * (double)(int)o.s.histo[i];
+    if (M > o.s.nBottom && density < 7)
       treeFlags = 1;
-    density = sqrt(density) * 2.6457513110645905905016 / (a.rad * a.rad) / M_PI;
-    if (M > nBottom && density < 0.5)
+    density = sqrt(density) * 2.6457513110645905905016 / (rad * rad) / M_PI;
+    if (M > o.s.nBottom && density < 0.5)
       treeFlags = 1;
-    if (top - bottom > 1.5)
+    if (o.s.top - o.s.bottom > 1.5)
       treeFlags = 1;
     r.nPoints = (int32_t)M;
     r.nGround = 0;
     r.treeFlags = treeFlags;
     r.density = density;
-    r.hScan = r.h = sqrt(1 / density + s.minH * s.minH);
-    r.height = top - bottom;
+    r.hScan = r.h = sqrt(1 / density + minH * minH);
+    r.height = o.s.top - o.s.bottom;
     res[k] = r;
   }
 }
@@ -1412,7 +1484,20 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   if (c->precision == WB_PRECISION_FP32 && a.fast)
     { scanKernel32<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
   else
-    { scanKernel<<<(unsigned)((T + kScanWarps - 1) / kScanWarps), 32 * kScanWarps, 0, c->stream>>>(s, res); ++c->launches; }
+  {
+    // per tile: centre (16 B) and one ScanWork slot (64 B)
+    if ((rc = wb_ensure(c, c->scanTot, T * (sizeof(double2) + sizeof(ScanWork)) + 64)))
+      return rc;
+    double2 *ctr = (double2 *)c->scanTot.p;
+    ScanWork *work = (ScanWork *)(ctr + T);
+    const unsigned sb = (unsigned)((T + kScanWarps - 1) / kScanWarps);
+    const unsigned tb = (unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32);
+    { scanPrep<<<tb, 128, 0, c->stream>>>(a, ctr); ++c->launches; }
+    { scanSums<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, ctr, work); ++c->launches; }
+    { scanSolve<<<tb, 128, 0, c->stream>>>(T, tileN, work, res); ++c->launches; }
+    { scanShape<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, ctr, work); ++c->launches; }
+    { scanFinish<<<tb, 128, 0, c->stream>>>(T, tileN, work, a.rad, p->min_hyp_size, res); ++c->launches; }
+  }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "scan");
   unsigned pb = (unsigned)std::min<uint64_t>((T + 255) / 256, (uint64_t)c->sm_count * 16);
