@@ -285,7 +285,8 @@ __global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const 
                                                                uint32_t *__restrict__ sidx, int32_t *__restrict__ sx,
                                                                int32_t *__restrict__ sy, int32_t *__restrict__ sz,
                                                                int32_t *__restrict__ box, uint32_t *__restrict__ storeOf,
-                                                               uint32_t *__restrict__ pointLeaf, uint64_t L)
+                                                               uint32_t *__restrict__ pointLeaf, uint64_t L,
+                                                               double *__restrict__ xyzd, uint64_t nd)
 {
   __shared__ uint32_t v[1024];
   __shared__ int32_t red[6][kLeafThreads / 32];
@@ -333,6 +334,9 @@ __global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const 
     sx[f + t] = q[0];
     sy[f + t] = q[1];
     sz[f + t] = q[2];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++)
+      xyzd[(uint64_t)ax * nd + f + t] = wb_decode(q[ax], a.off[ax], a.scale[ax], a.unit);
     storeOf[id] = f + t;
     pointLeaf[id] = (uint32_t)l;
 #pragma unroll
@@ -520,10 +524,10 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if (cl->n > 0xfffffff0ull)
     return wb_fail(c, WB_EINVAL, "wb_octree_build: at most 2^32-16 points per cloud");
   uint64_t n = cl->n;
-  // with paging, a cloud whose working set (about 300 B per point plus the
+  // with paging, a cloud whose working set (about 330 B per point plus the
   // records) is above the HBM budget keeps its scratch buffers in host memory
   c->spill_cold = c->host_budget && c->budget &&
-                  n * (300ull + (cl->device_resident ? 0 : cl->stride)) > c->budget;
+                  n * (330ull + (cl->device_resident ? 0 : cl->stride)) > c->budget;
   WbGeom &g = c->g;
   for (int a = 0; a < 3; a++)
   {
@@ -651,7 +655,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
       (rc = wb_ensure(c, c->leafLevel, L + 64)) || (rc = wb_ensure(c, c->leafKey, L * 8 + 64)) ||
       (rc = wb_ensure(c, c->leafBox, L * 24 + 64)) || (rc = wb_ensure(c, c->sidx, nd * 4 + 64)) ||
       (rc = wb_ensure(c, c->sx, nd * 4 + 64)) || (rc = wb_ensure(c, c->sy, nd * 4 + 64)) ||
-      (rc = wb_ensure(c, c->sz, nd * 4 + 64)))
+      (rc = wb_ensure(c, c->sz, nd * 4 + 64)) || (rc = wb_ensure(c, c->xyzd, nd * 24 + 64)))
     return rc;
   uint32_t *leafId = (uint32_t *)c->leafId.p, *first = (uint32_t *)c->leafFirst.p, *count = (uint32_t *)c->leafCount.p;
   uint8_t *leafLev = (uint8_t *)c->leafLevel.p;
@@ -663,7 +667,8 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   uint32_t *storeOf = (uint32_t *)c->storeOf.p;
   { leafSortKernel<<<(unsigned)L, kLeafThreads, 0, c->stream>>>(a, first, count, didx, (uint32_t *)c->sidx.p,
                                                                (int32_t *)c->sx.p, (int32_t *)c->sy.p, (int32_t *)c->sz.p,
-                                                               box, storeOf, (uint32_t *)c->pointLeaf.p, L); ++c->launches; }
+                                                               box, storeOf, (uint32_t *)c->pointLeaf.p, L,
+                                                               (double *)c->xyzd.p, nd); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "leaf_order");
   // records a later identical point overwrote take their survivor's slot and leaf

@@ -111,6 +111,7 @@ struct ClsArgs
   const uint32_t *leafId;
   double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
+  const double *xyzd;   /* decoded x, y, z planes of nd doubles */
   const int32_t *owner;
   const TileRes *tiles;
   const double *tanT, *sinT, *cosT;
@@ -353,7 +354,7 @@ __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
   if (k < 0)
     return;
   double hs = a.tiles[k].h;
-  double px = decA(a, 0, a.sx[j]), py = decA(a, 1, a.sy[j]), pz = decA(a, 2, a.sz[j]);
+  const double px = a.xyzd[j], py = a.xyzd[a.nd + j], pz = a.xyzd[2 * a.nd + j];
   double por = hs * (a.slope * a.slope);
   double por2 = por * por;
   double cz = (pz - a.thickness) + por;
@@ -1444,6 +1445,7 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;
+  a.xyzd = (const double *)c->xyzd.p;
   a.owner = (const int32_t *)c->owner.p;
   a.tiles = (const TileRes *)c->tileRes.p;
   a.tanT = tab;

@@ -36,7 +36,7 @@ struct GridArgs
 __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                            const int32_t *__restrict__ sz, uint64_t *__restrict__ key, uint32_t *__restrict__ val,
                            uint8_t *__restrict__ stray, unsigned long long *__restrict__ nStray,
-                           int *__restrict__ ext)
+                           int *__restrict__ ext, const double *__restrict__ xyzd)
 {
   // record-integer extent of the points ({min x, y, z}, {max x, y, z})
   int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
@@ -48,9 +48,7 @@ __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int
       mn[a] = min(mn[a], q[a]);
       mx[a] = max(mx[a], q[a]);
     }
-    double x = wb_decode(q[0], g.off[0], g.scale[0], g.unit);
-    double y = wb_decode(q[1], g.off[1], g.scale[1], g.unit);
-    double z = wb_decode(q[2], g.off[2], g.scale[2], g.unit);
+    const double x = xyzd[j], y = xyzd[g.nd + j], z = xyzd[2 * g.nd + j];
     int cx = (int)floor((x - g.x0) / g.cell), cy = (int)floor((y - g.y0) / g.cell);
     cx = min(max(cx, 0), g.nx - 1);
     cy = min(max(cy, 0), g.ny - 1);
@@ -242,7 +240,7 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   uint32_t *val = (uint32_t *)c->gVal0.p;
   { cellKernel<<<blocks, 256, 0, c->stream>>>(a, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
                                               (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray,
-                                              dExt); ++c->launches; }
+                                              dExt, (const double *)c->xyzd.p); ++c->launches; }
   int bits = 1;
   while ((1ull << bits) < ncell)
     bits++;

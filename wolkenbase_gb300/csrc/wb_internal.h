@@ -73,9 +73,12 @@ struct wb_ctx
   DevBuf lev, cpl, pre, suf, leafId;
   DevBuf leafFirst, leafCount, leafLevel, leafKey, leafBox;
   DevBuf sidx, sx, sy, sz, pointLeaf, storeOf, survivorOf;
+  /* decoded coordinates of the stored points, three planes of nd doubles
+     (x, y, z), each the reference's (offset + scale * X) * unit */
+  DevBuf xyzd;
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre,
-      scanTot;
+      scanTot, tileFrm;
   DevBuf label, clsDev, ambiguous, deferred, angleT;
   /* column grid (wb_grid.cu): gpt holds one int4 {X, Y, Z, store position |
      stray bit} per point in column order; cellRec two int4 per column,

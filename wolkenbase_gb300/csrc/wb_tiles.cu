@@ -37,6 +37,8 @@ struct TileArgs
   const uint8_t *leafLev;
   double rootLo[3], rootSide;
   const int32_t *sx, *sy, *sz;
+  const double *xyzd;   /* decoded x, y, z planes of nd doubles */
+  uint64_t nd;
   int fast;   /* FP32 filter allowed: decode strictly increasing, 32-bit record differences exact */
 };
 
@@ -145,6 +147,23 @@ __device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const int4 &box,
   return dx * dx + dy * dy <= r * r;
 }
 
+/* The same column test in the tile's FP32 frame, with the radius widened by
+ * 2e-4 (relative) and 1e-4 (absolute, squared units): a superset of the FP64
+ * test (the frame's rounding is about 1e-7 relative), so no column with a
+ * member is skipped; an extra column only costs its points' tests.  The
+ * bound and both fills use this one test, so a tile never gathers more
+ * points than its bound counted. */
+__device__ __forceinline__ bool cellMeets(const TileArgs &a, const TileFrame &f, const int4 &box)
+{
+  if (!a.fast)
+    return cellMeetsCyl(a, box, f.cx, f.cy);
+  const float x0 = ((float)(box.x - f.qx0) - f.fx) * f.sx, x1 = ((float)(box.z - f.qx0) - f.fx) * f.sx;
+  const float y0 = ((float)(box.y - f.qy0) - f.fy) * f.sy, y1 = ((float)(box.w - f.qy0) - f.fy) * f.sy;
+  const float dx = x0 > 0 ? x0 : (x1 < 0 ? -x1 : 0.f);
+  const float dy = y0 > 0 ? y0 : (y1 < 0 ? -y1 : 0.f);
+  return dx * dx + dy * dy <= f.r2hi * 1.0002f + 1e-8f;
+}
+
 /* Entries of the huge tiles as sort keys: (huge tile rank << 32) | store
  * position, huge tile h owning entries [pre[h], pre[h+1]). */
 __global__ void hugeKeysKernel(uint32_t nh, const uint32_t *__restrict__ hugeList, const uint32_t *__restrict__ tileStart,
@@ -186,18 +205,19 @@ __global__ void hugeBackKernel(uint32_t nh, const uint32_t *__restrict__ hugeLis
 /* Room for each tile's points: the points of the grid columns its cylinder
  * meets (an upper bound of the tile's count), one thread per tile.  The fill
  * passes write a tile's points from tileStart[k] on and its count to tileN. */
-__global__ void gridBound(TileArgs a, GridDev gd, uint32_t *__restrict__ bound)
+__global__ void gridBound(TileArgs a, GridDev gd, uint32_t *__restrict__ bound, TileFrame *__restrict__ frames)
 {
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.T; k += (uint64_t)gridDim.x * blockDim.x)
   {
-    TileFrame f = tileFrame(a, gd, k);
+    const TileFrame f = tileFrame(a, gd, k);
+    frames[k] = f;
     uint32_t room = 0;
     for (int j = f.j0; j <= f.j1; j++)
       for (int i = f.i0; i <= f.i1; i++)
       {
         uint64_t c = (uint64_t)j * gd.nx + i;
         int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
-        if (r1.y != r1.z && cellMeetsCyl(a, box, f.cx, f.cy))
+        if (r1.y != r1.z && cellMeets(a, f, box))
           room += (uint32_t)(r1.z - r1.y);
       }
     bound[k] = room;
@@ -217,7 +237,8 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
                                                                 const uint32_t *__restrict__ tileStart,
                                                                 uint32_t *__restrict__ tileN,
                                                                 uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
-                                                                uint32_t *__restrict__ bigList, uint32_t *__restrict__ bigCount)
+                                                                uint32_t *__restrict__ bigList, uint32_t *__restrict__ bigCount,
+                                                                const TileFrame *__restrict__ frames)
 {
   __shared__ uint32_t buf[kTileWarps][kWarpFill];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -233,7 +254,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
   }
   uint32_t *b = buf[w];
   const unsigned lt = (1u << lane) - 1;
-  TileFrame f = tileFrame(a, gd, k);
+  const TileFrame f = frames[k];
   uint32_t n = 0;
   for (int j = f.j0; j <= f.j1; j++)
     for (int i = f.i0; i <= f.i1; i++)
@@ -241,7 +262,7 @@ __global__ void __launch_bounds__(32 * kTileWarps) gridFillWarp(TileArgs a, Grid
       uint64_t c = (uint64_t)j * gd.nx + i;
       int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
       uint32_t cb = (uint32_t)r1.y, ce = (uint32_t)r1.z;
-      if (cb == ce || !cellMeetsCyl(a, box, f.cx, f.cy))
+      if (cb == ce || !cellMeets(a, f, box))
         continue;
       for (uint32_t t0 = cb; t0 < ce; t0 += 32)
       {
@@ -313,7 +334,8 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
                                                          uint32_t *__restrict__ tilePts, int32_t *__restrict__ owner,
                                                          int *__restrict__ overflow, const uint32_t *__restrict__ bigList,
                                                          const uint32_t *__restrict__ bigCount,
-                                                         uint32_t *__restrict__ hugeList)
+                                                         uint32_t *__restrict__ hugeList,
+                                                         const TileFrame *__restrict__ frames)
 {
   __shared__ uint32_t buf[kFillMax];
   __shared__ uint32_t cnt;
@@ -330,14 +352,14 @@ __global__ void __launch_bounds__(kFillThreads) gridFill(TileArgs a, GridDev gd,
       hugeList[atomicAdd(overflow, 1)] = (uint32_t)k;
   }
   __syncthreads();
-  TileFrame f = tileFrame(a, gd, k);
+  const TileFrame f = frames[k];
   for (int j = f.j0; j <= f.j1; j++)
     for (int i = f.i0; i <= f.i1; i++)
     {
       uint64_t c = (uint64_t)j * gd.nx + i;
       int4 box = gd.cell2[2 * c], r1 = gd.cell2[2 * c + 1];
       uint32_t b = (uint32_t)r1.y, e = (uint32_t)r1.z;
-      if (b == e || !cellMeetsCyl(a, box, f.cx, f.cy))
+      if (b == e || !cellMeets(a, f, box))
         continue;
       for (uint32_t t = b + threadIdx.x; t < e; t += kFillThreads)
       {
@@ -589,12 +611,13 @@ __device__ __forceinline__ int sectorOf(double x, double y, double rin)
   return (sector % 6) + 1;
 }
 
-/* scanCylinder in five kernels.  The FP64 pipe bounds this stage, and an
+/* scanCylinder in four kernels.  The FP64 pipe bounds this stage, and an
  * FP64 instruction costs the same whether one lane or 32 run it, so each part
  * runs at the width that keeps its lanes busy: the per-point passes one warp
  * per tile (lanes over points), everything done once per tile (centre, the
  * reference's 3x3 Gauss-Jordan, the slope clamp, density and height) one
- * thread per tile.  A tile's intermediate values live in one ScanWork slot. */
+ * thread per tile.  A tile's intermediate values live in one ScanWork slot;
+ * its centre comes from the frame the gather's bound pass stored. */
 union ScanWork
 {
   double sums[kQ];   // scanSums -> scanSolve: the eight normal-equation sums
@@ -606,22 +629,11 @@ union ScanWork
   } s;
 };
 
-/* Tile centres (Flowsnake::cyl), one thread per tile. */
-__global__ void scanPrep(TileArgs a, double2 *__restrict__ ctr)
-{
-  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.T; k += (uint64_t)gridDim.x * blockDim.x)
-  {
-    double cx, cy;
-    tileCenter(a, k, cx, cy);
-    ctr[k] = make_double2(cx, cy);
-  }
-}
-
 /* Pass 1: the eight sums of the normal equations that linearLeastSquares
  * forms from the tile's points (scan.cpp:60-68, matrix.cpp:194, 211) in the
  * reference's pairwise order (pairwisesum's binary counter over the points in
  * store order). */
-__global__ void __launch_bounds__(32 * kScanWarps) scanSums(ScanArgs s, const double2 *__restrict__ ctr,
+__global__ void __launch_bounds__(32 * kScanWarps) scanSums(ScanArgs s, const TileFrame *__restrict__ frames,
                                                              ScanWork *__restrict__ work)
 {
   __shared__ double part[kScanWarps][kQ][kLevels];
@@ -634,7 +646,7 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanSums(ScanArgs s, const do
   const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
   if (M == 0)
     return;
-  const double cx = ctr[k].x, cy = ctr[k].y;
+  const double cx = frames[k].cx, cy = frames[k].cy;
   const uint64_t G = M / 8;   // complete groups of eight
   for (uint32_t c0 = 0; c0 < M; c0 += 32)
   {
@@ -643,7 +655,7 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanSums(ScanArgs s, const do
     if (i < M)
     {
       uint32_t j = s.tilePts[b0 + i];
-      double x = dec(a, 0, a.sx[j]) - cx, y = dec(a, 1, a.sy[j]) - cy, z = dec(a, 2, a.sz[j]) - 0.0;
+      double x = a.xyzd[j] - cx, y = a.xyzd[a.nd + j] - cy, z = a.xyzd[2 * a.nd + j] - 0.0;
       q[0] = x * x;
       q[1] = y * x;
       q[2] = y * y;
@@ -753,7 +765,7 @@ __global__ void scanSolve(uint64_t T, const uint32_t *__restrict__ tileN, ScanWo
  * and bottom2 over its points and the warp combines them once per tile:
  * the first minimum is the least (height, index) pair whatever the order,
  * and fmin / fmax give the same value in any order (they order -0 below +0). */
-__global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const double2 *__restrict__ ctr,
+__global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const TileFrame *__restrict__ frames,
                                                               ScanWork *__restrict__ work)
 {
   // tile-local coordinates and untilted heights of tiles up to kScanCache
@@ -767,16 +779,16 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const d
   const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
   if (M == 0)
     return;
-  const double cx = ctr[k].x, cy = ctr[k].y;
+  const double cx = frames[k].cx, cy = frames[k].cy;
   const bool cached = M <= kScanCache;
   if (cached)
   {
     for (uint32_t i = lane; i < M; i += 32)
     {
       uint32_t j = s.tilePts[b0 + i];
-      cxy[w][0][i] = dec(a, 0, a.sx[j]) - cx;
-      cxy[w][1][i] = dec(a, 1, a.sy[j]) - cy;
-      cxy[w][2][i] = dec(a, 2, a.sz[j]) - 0.0;
+      cxy[w][0][i] = a.xyzd[j] - cx;
+      cxy[w][1][i] = a.xyzd[a.nd + j] - cy;
+      cxy[w][2][i] = a.xyzd[2 * a.nd + j] - 0.0;
     }
     __syncwarp();
   }
@@ -791,9 +803,9 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const d
     else
     {
       uint32_t j = s.tilePts[b0 + i];
-      x = dec(a, 0, a.sx[j]) - cx;
-      y = dec(a, 1, a.sy[j]) - cy;
-      z = dec(a, 2, a.sz[j]) - 0.0;
+      x = a.xyzd[j] - cx;
+      y = a.xyzd[a.nd + j] - cy;
+      z = a.xyzd[2 * a.nd + j] - 0.0;
     }
   };
   const double sx = work[k].s.sx, sy = work[k].s.sy;
@@ -1306,6 +1318,8 @@ static TileArgs tileArgs(wb_ctx *c)
   a.sx = (const int32_t *)c->sx.p;
   a.sy = (const int32_t *)c->sy.p;
   a.sz = (const int32_t *)c->sz.p;
+  a.xyzd = (const double *)c->xyzd.p;
+  a.nd = c->nd;
   return a;
 }
 
@@ -1432,8 +1446,11 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   if ((rc = wb_ensure(c, c->tileNg, T * 4 + 64)))
     return rc;
   uint32_t *bound = (uint32_t *)c->tileNg.p;
+  if ((rc = wb_ensure(c, c->tileFrm, T * sizeof(TileFrame) + 64)))
+    return rc;
+  TileFrame *frames = (TileFrame *)c->tileFrm.p;
   { gridBound<<<(unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32), 128, 0, c->stream>>>(
-        a, gd, bound); ++c->launches; }
+        a, gd, bound, frames); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   uint32_t *dTot = (uint32_t *)((char *)c->small.p + 64);
   // Cylinders overlap, so the rooms add up to more than the points; their sum
@@ -1461,12 +1478,12 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   // huge-tile count and big-tile count (bytes 384..395 of the scratch block)
   WB_CUDA(c, cudaMemsetAsync(dOvf, 0, 16, c->stream));
   { gridFillWarp<<<blocks, 32 * kTileWarps, 0, c->stream>>>(a, gd, tileStart, tileN, (uint32_t *)c->tilePts.p, owner,
-                                                           (uint32_t *)c->tileNg.p, dBig); ++c->launches; }
+                                                           (uint32_t *)c->tileNg.p, dBig, frames); ++c->launches; }
   if ((rc = wb_ensure(c, c->tileHuge, T * 4 + 64)))
     return rc;
   { gridFill<<<(unsigned)c->sm_count, kFillThreads, 0, c->stream>>>(a, gd, tileStart, tileN, (uint32_t *)c->tilePts.p,
                                                                    owner, dOvf, (const uint32_t *)c->tileNg.p, dBig,
-                                                                   (uint32_t *)c->tileHuge.p); ++c->launches; }
+                                                                   (uint32_t *)c->tileHuge.p, frames); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   int nHuge = 0;
   WB_CUDA(c, cudaMemcpyAsync(&nHuge, dOvf, 4, cudaMemcpyDefault, c->stream));
@@ -1485,17 +1502,15 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
     { scanKernel32<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
   else
   {
-    // per tile: centre (16 B) and one ScanWork slot (64 B)
-    if ((rc = wb_ensure(c, c->scanTot, T * (sizeof(double2) + sizeof(ScanWork)) + 64)))
+    // one ScanWork slot (64 B) per tile; the centres come from the tile frames
+    if ((rc = wb_ensure(c, c->scanTot, T * sizeof(ScanWork) + 64)))
       return rc;
-    double2 *ctr = (double2 *)c->scanTot.p;
-    ScanWork *work = (ScanWork *)(ctr + T);
+    ScanWork *work = (ScanWork *)c->scanTot.p;
     const unsigned sb = (unsigned)((T + kScanWarps - 1) / kScanWarps);
     const unsigned tb = (unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32);
-    { scanPrep<<<tb, 128, 0, c->stream>>>(a, ctr); ++c->launches; }
-    { scanSums<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, ctr, work); ++c->launches; }
+    { scanSums<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, frames, work); ++c->launches; }
     { scanSolve<<<tb, 128, 0, c->stream>>>(T, tileN, work, res); ++c->launches; }
-    { scanShape<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, ctr, work); ++c->launches; }
+    { scanShape<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, frames, work); ++c->launches; }
     { scanFinish<<<tb, 128, 0, c->stream>>>(T, tileN, work, a.rad, p->min_hyp_size, res); ++c->launches; }
   }
   WB_CUDA(c, cudaGetLastError());
