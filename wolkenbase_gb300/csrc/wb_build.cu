@@ -524,10 +524,10 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if (cl->n > 0xfffffff0ull)
     return wb_fail(c, WB_EINVAL, "wb_octree_build: at most 2^32-16 points per cloud");
   uint64_t n = cl->n;
-  // with paging, a cloud whose working set (about 330 B per point plus the
+  // with paging, a cloud whose working set (about 340 B per point plus the
   // records) is above the HBM budget keeps its scratch buffers in host memory
   c->spill_cold = c->host_budget && c->budget &&
-                  n * (330ull + (cl->device_resident ? 0 : cl->stride)) > c->budget;
+                  n * (340ull + (cl->device_resident ? 0 : cl->stride)) > c->budget;
   WbGeom &g = c->g;
   for (int a = 0; a < 3; a++)
   {

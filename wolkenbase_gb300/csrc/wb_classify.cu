@@ -118,7 +118,9 @@ struct ClsArgs
   uint8_t *label;
   /* grid */
   double gx0, gy0, cell;
-  double invSlope2, invCell, invSuper;   /* 1/slope^2, 1/cell, 1/(WB_SUPER cell): reach bounds only */
+  double invSlope2;          /* 1/slope^2, for the reach bound */
+  float invCellF, invSuperF; /* 1/cell, 1/(WB_SUPER cell) in FP32, for the ring counts */
+  const int2 *colOf;         /* column of each stored point, from the grid build */
   int nx, ny;
   uint64_t ncell;
   const int4 *col;     /* two int4 per column: {x0, y0, x1, y1}, {zmin, begin, end, flags} */
@@ -354,7 +356,7 @@ __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
   if (k < 0)
     return;
   double hs = a.tiles[k].h;
-  const double px = a.xyzd[j], py = a.xyzd[a.nd + j], pz = a.xyzd[2 * a.nd + j];
+  const double pz = a.xyzd[2 * a.nd + j];
   double por = hs * (a.slope * a.slope);
   double por2 = por * por;
   double cz = (pz - a.thickness) + por;
@@ -363,15 +365,16 @@ __device__ __forceinline__ void setupPoint(const ClsArgs &a, uint64_t j)
   s.por2f = (float)por2;
   // horizontal reach of the hyperboloid at the lowest point of the cloud
   double zdMax = cz - a.zmin;
-  // (products with reciprocals: reach carries a 1e-6 margin, far above their
-  // rounding, so the ring counts still cover it)
-  double reach2 = (zdMax * zdMax - por2) * a.invSlope2;
-  double reach = reach2 > 0 ? sqrt(reach2) * (1 + 1e-6) + 1e-6 : 0.0;
-  double fi = floor((px - a.gx0) / a.cell), fj = floor((py - a.gy0) / a.cell);
-  s.ci = (int32_t)fmax(fmin(fi, 1e9), -1e9);
-  s.cj = (int32_t)fmax(fmin(fj, 1e9), -1e9);
-  s.kmax = (int32_t)fmin(ceil(reach * a.invCell) + 1, 1e9);
-  s.smax = (int32_t)fmin(ceil(reach * a.invSuper) + 1, 1e9);
+  // The ring counts only bound the search (columns beyond the reach hold no
+  // member), so they are formed in FP32 with a 1e-5 margin, far above the
+  // 1e-7 rounding of the FP32 root and products.
+  const float r2f = (float)((zdMax * zdMax - por2) * a.invSlope2);
+  const float reach = r2f > 0 ? sqrtf(r2f) * (1 + 1e-5f) + 1e-5f : 0.f;
+  const int2 col = a.colOf[j];
+  s.ci = col.x;
+  s.cj = col.y;
+  s.kmax = (int32_t)fminf(ceilf(reach * a.invCellF) + 1, 1e9f);
+  s.smax = (int32_t)fminf(ceilf(reach * a.invSuperF) + 1, 1e9f);
   a.setup[j] = s;
 }
 
@@ -1456,8 +1459,9 @@ static int classifyPrepare(wb_ctx *c, const wb_params *p, uint8_t *cls, int onDe
   a.gy0 = c->grid.y0;
   a.cell = c->grid.cell;
   a.invSlope2 = 1.0 / (p->max_slope * p->max_slope);
-  a.invCell = 1.0 / c->grid.cell;
-  a.invSuper = 1.0 / (WB_SUPER * c->grid.cell);
+  a.invCellF = (float)(1.0 / c->grid.cell);
+  a.invSuperF = (float)(1.0 / (WB_SUPER * c->grid.cell));
+  a.colOf = (const int2 *)c->colOf.p;
   a.nx = c->grid.nx;
   a.ny = c->grid.ny;
   a.ncell = c->grid.ncell;

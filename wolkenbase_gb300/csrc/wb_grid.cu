@@ -36,7 +36,7 @@ struct GridArgs
 __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                            const int32_t *__restrict__ sz, uint64_t *__restrict__ key, uint32_t *__restrict__ val,
                            uint8_t *__restrict__ stray, unsigned long long *__restrict__ nStray,
-                           int *__restrict__ ext, const double *__restrict__ xyzd)
+                           int *__restrict__ ext, const double *__restrict__ xyzd, int2 *__restrict__ colOf)
 {
   // record-integer extent of the points ({min x, y, z}, {max x, y, z})
   int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
@@ -49,9 +49,12 @@ __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int
       mx[a] = max(mx[a], q[a]);
     }
     const double x = xyzd[j], y = xyzd[g.nd + j], z = xyzd[2 * g.nd + j];
-    int cx = (int)floor((x - g.x0) / g.cell), cy = (int)floor((y - g.y0) / g.cell);
-    cx = min(max(cx, 0), g.nx - 1);
-    cy = min(max(cy, 0), g.ny - 1);
+    // the point's column as the classify set-up needs it (unclamped, within
+    // +-1e9), and clamped into the grid for the sort key
+    const int ci = (int)fmax(fmin(floor((x - g.x0) / g.cell), 1e9), -1e9);
+    const int cj = (int)fmax(fmin(floor((y - g.y0) / g.cell), 1e9), -1e9);
+    colOf[j] = make_int2(ci, cj);
+    const int cx = min(max(ci, 0), g.nx - 1), cy = min(max(cj, 0), g.ny - 1);
     // column in the high 32 bits, height (order-preserving int32 -> uint32) below
     key[j] = (((uint64_t)cy * g.nx + cx) << 32) | (uint32_t)(q[2] ^ (int32_t)0x80000000);
     val[j] = (uint32_t)j;
@@ -213,7 +216,8 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   if ((rc = wb_ensure(c, c->gKey0, nd * 8 + 64)) || (rc = wb_ensure(c, c->gKey1, nd * 8 + 64)) ||
       (rc = wb_ensure(c, c->gVal0, nd * 4 + 64)) || (rc = wb_ensure(c, c->gVal1, nd * 4 + 64)) ||
       (rc = wb_ensure(c, c->stray, nd + 64)) || (rc = wb_ensure(c, c->cellStart, (ncell + 1) * 4 + 64)) ||
-      (rc = wb_ensure(c, c->gpt, nd * 16 + 64)) || (rc = wb_ensure(c, c->cellRec, ncell * 32 + 64)))
+      (rc = wb_ensure(c, c->gpt, nd * 16 + 64)) || (rc = wb_ensure(c, c->cellRec, ncell * 32 + 64)) ||
+      (rc = wb_ensure(c, c->colOf, nd * 8 + 64)))
     return rc;
   GridArgs a;
   a.nd = nd;
@@ -240,7 +244,7 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   uint32_t *val = (uint32_t *)c->gVal0.p;
   { cellKernel<<<blocks, 256, 0, c->stream>>>(a, (const int32_t *)c->sx.p, (const int32_t *)c->sy.p,
                                               (const int32_t *)c->sz.p, key, val, (uint8_t *)c->stray.p, dStray,
-                                              dExt, (const double *)c->xyzd.p); ++c->launches; }
+                                              dExt, (const double *)c->xyzd.p, (int2 *)c->colOf.p); ++c->launches; }
   int bits = 1;
   while ((1ull << bits) < ncell)
     bits++;

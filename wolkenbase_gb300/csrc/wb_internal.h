@@ -76,6 +76,7 @@ struct wb_ctx
   /* decoded coordinates of the stored points, three planes of nd doubles
      (x, y, z), each the reference's (offset + scale * X) * unit */
   DevBuf xyzd;
+  DevBuf colOf;   /* column {i, j} of each stored point (unclamped, within +-1e9) */
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre,
       scanTot, tileFrm;

@@ -45,13 +45,13 @@ struct JobRec
 };
 
 /* Device bytes a job of n records is expected to hold: the pipeline's buffers
- * come to about 280 bytes per point (sort keys and values twice, the leaf
- * store, the column grid, the tile lists and the classify set-up, each grown
- * with 1/8 slack), plus the uploaded records. */
+ * come to about 310 bytes per point (sort keys and values twice, the leaf
+ * store and its decoded coordinates, the column grid, the tile lists and the
+ * classify set-up, each grown with 1/8 slack), plus the uploaded records. */
 uint64_t estimateBytes(const wb_job &j)
 {
   uint64_t n = j.cloud.n;
-  uint64_t per = 300 + (j.cloud.device_resident ? 0 : j.cloud.stride);
+  uint64_t per = 340 + (j.cloud.device_resident ? 0 : j.cloud.stride);
   return n * per + (64ull << 20);
 }
 }  // namespace
