@@ -837,8 +837,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
  * its hyperboloid.  Clouds whose record differences do not fit FP32 send
  * every point to the exact pass instead. */
 constexpr int kGroupBins = 8;
-constexpr int kDefer = 6;          // undecided lanes at or below which a group hands its points over
-constexpr int kGroupColumns = 256; // columns a group reads before it hands its undecided points over
+constexpr int kGroupColumns = 128;   // columns a group reads before it hands its undecided points over
 
 struct GroupSmem
 {
@@ -1254,15 +1253,14 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       gst[13] += clock64() - tEnv;
 #endif
     };
-    // When few lanes remain undecided the warp would run at a fraction of its
-    // width, and a group whose neighbourhood is very large would hold one warp
-    // while the rest of the GPU idles: in both cases the undecided points go
-    // to the one-point kernel (kDefer lanes or fewer, or more than
-    // kGroupColumns columns read).
+    // A group whose neighbourhood is very large would hold one warp while the
+    // rest of the GPU idles: after kGroupColumns columns its undecided points
+    // go to the one-point kernel.  (Handing over a group with few lanes left
+    // as well measured 11% slower with these limits: 6 lanes, 256 columns.)
     auto allDone = [&]() {
       if (__all_sync(0xffffffffu, done))
         return true;
-      if (__popc(__ballot_sync(0xffffffffu, !done)) > kDefer && columnsRead <= kGroupColumns)
+      if (columnsRead <= kGroupColumns)
         return false;
       if (!done)
       {
