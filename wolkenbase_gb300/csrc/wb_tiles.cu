@@ -887,7 +887,13 @@ __global__ void __launch_bounds__(32 * kScanWarps) scanShape(ScanArgs s, const T
 
 /* Density, tree flags, h and height of each tile (scan.cpp:103-120), one
  * thread per tile. */
-__global__ void scanFinish(uint64_t T, const uint32_t *__restrict__ tileN, const ScanWork *__restrict__ work,
+__device__ __forceinline__ const ScanWork &asWork(const ScanWork &x)
+{
+  return x;
+}
+
+template <typename Slot>
+__global__ void scanFinish(uint64_t T, const uint32_t *__restrict__ tileN, const Slot *__restrict__ work,
                            double rad, double minH, TileRes *__restrict__ res)
 {
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T; k += (uint64_t)gridDim.x * blockDim.x)
@@ -899,7 +905,7 @@ __global__ void scanFinish(uint64_t T, const uint32_t *__restrict__ tileN, const
       res[k] = r;
       continue;
     }
-    const ScanWork &o = work[k];
+    const ScanWork &o = asWork(work[k]);
     r.plane[0] = res[k].plane[0];
     r.plane[1] = res[k].plane[1];
     r.plane[2] = res[k].plane[2];
@@ -933,96 +939,100 @@ __device__ __forceinline__ void twoSumF(float a, float b, float &s, float &e)
 }
 
 /* scanCylinder in the precision mode: coordinates are FP32 in a tile-local
- * frame.  The normal-equation sums are taken about the points' centroid
- * (found exactly in record integers), accumulated per lane with Kahan
- * compensation and merged across the warp with two-sums; the sums of the
- * tile-centre frame are rebuilt from them in FP64, and only the 3x3 solve
- * (the reference's Gauss-Jordan with ratio pivoting) runs in FP64.  The
- * untilting, bottom, bottom2, top and the sector histogram run in FP32 with
- * coordinates from an integer anchor next to the tile centre.  Untilting, bottom,
- * bottom2, top and the sector histogram run in FP32 in the same frame. */
-__global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, TileRes *__restrict__ res)
+ * frame (record integers minus an integer anchor next to the tile centre,
+ * times the scale).  The normal-equation sums are taken about the points'
+ * centroid in record integers, accumulated per lane with Kahan compensation
+ * and merged across the warp with two-sums; the untilting, bottom, bottom2,
+ * top and the sector histogram run in FP32 in the anchor frame.  As in the
+ * exact mode, everything done once per tile runs one thread per tile: the
+ * rebuild of the tile-centre sums in FP64, the 3x3 solve (the reference's
+ * Gauss-Jordan with ratio pivoting), the slope clamp, density and height. */
+struct Scan32Sums
+{
+  float hi[kQ], lo[kQ];       // compensated sums about the centroid, hi + lo
+  int32_t cX, cY, cZ, az;     // centroid and the height anchor, record integers
+};
+union ScanWork32
+{
+  Scan32Sums p;   // scan32Sums -> scan32Solve
+  ScanWork w;     // scan32Solve -> scan32Shape -> scanFinish (az stays in p)
+};
+
+__device__ __forceinline__ const ScanWork &asWork(const ScanWork32 &x)
+{
+  return x.w;
+}
+
+/* The tile-local FP32 frame: anchor (qx0, qy0) of the tile frame, the anchor's
+ * offset from the centre in metres, heights from az. */
+struct Frame32
+{
+  int32_t ax, ay, az;
+  float fx, fy, ssx, ssy, ssz;
+};
+
+__device__ __forceinline__ Frame32 frame32(const TileArgs &a, const TileFrame &f, int32_t az)
+{
+  Frame32 g;
+  g.ax = f.qx0;
+  g.ay = f.qy0;
+  g.az = az;
+  g.ssx = f.sx;
+  g.ssy = f.sy;
+  g.ssz = (float)(a.scale[2] * a.unit);
+  g.fx = -__fmul_rn(f.fx, f.sx);
+  g.fy = -__fmul_rn(f.fy, f.sy);
+  return g;
+}
+
+__device__ __forceinline__ void local32(const TileArgs &a, const Frame32 &g, uint32_t j, float &x, float &y, float &z)
+{
+  x = __fadd_rn(__fmul_rn((float)(a.sx[j] - g.ax), g.ssx), g.fx);
+  y = __fadd_rn(__fmul_rn((float)(a.sy[j] - g.ay), g.ssy), g.fy);
+  z = __fmul_rn((float)(a.sz[j] - g.az), g.ssz);
+}
+
+/* Pass 1 of the precision mode, one warp per tile: the centroid in record
+ * integers (exact int64 sums) and the compensated sums of the products of
+ * u = X - centroid (exact in FP32), which are exact while a product stays
+ * below 2^24 (|u| * |v| of a 1.5 m tile at 1 mm is below 2^20). */
+__global__ void __launch_bounds__(32 * kScanWarps) scan32Sums(ScanArgs s, ScanWork32 *__restrict__ work)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const TileArgs &a = s.t;
-  uint64_t k = (uint64_t)blockIdx.x * kTileWarps + w;
+  const uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
   if (k >= a.T)
     return;
-  uint32_t b0 = s.tileStart[k], M = s.tileN[k];
-  TileRes r{};
+  const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
   if (M == 0)
-  {
-    if (lane == 0)
-      res[k] = r;
     return;
-  }
-  double cx, cy;
-  tileCenter(a, k, cx, cy);
-  // integer anchor next to the centre and the FP32 offset of the centre from it
-  int32_t ax = (int32_t)llrint((cx / a.unit - a.off[0]) / a.scale[0]);
-  int32_t ay = (int32_t)llrint((cy / a.unit - a.off[1]) / a.scale[1]);
-  const float fx = (float)(dec(a, 0, ax) - cx), fy = (float)(dec(a, 1, ay) - cy);
-  const float ssx = (float)(a.scale[0] * a.unit), ssy = (float)(a.scale[1] * a.unit), ssz = (float)(a.scale[2] * a.unit);
-  const int32_t az = a.sz[s.tilePts[b0]];
-  const double z0 = dec(a, 2, az);
-  auto local = [&](uint32_t j, float &x, float &y, float &z) {
-    x = __fadd_rn(__fmul_rn((float)(a.sx[j] - ax), ssx), fx);
-    y = __fadd_rn(__fmul_rn((float)(a.sy[j] - ay), ssy), fy);
-    z = __fmul_rn((float)(a.sz[j] - az), ssz);
-  };
-  // Compensated sums of n quantities per lane (Kahan), merged across the warp
-  // with two-sums; every lane receives the totals as doubles.
-  auto warpSum = [&](auto quantities, double *tot, int n) {
-    float sum[kQ], cmp[kQ];
-    for (int u = 0; u < n; u++)
-      sum[u] = cmp[u] = 0.f;
-    for (uint32_t i = lane; i < M; i += 32)
-    {
-      float q[kQ];
-      quantities(s.tilePts[b0 + i], q);
-      for (int u = 0; u < n; u++)
-      {
-        float yv = __fsub_rn(q[u], cmp[u]);
-        float t = __fadd_rn(sum[u], yv);
-        cmp[u] = __fsub_rn(__fsub_rn(t, sum[u]), yv);
-        sum[u] = t;
-      }
-    }
-    for (int u = 0; u < n; u++)
-    {
-      float hi = sum[u], lo = -cmp[u];
-      for (int o = 16; o; o >>= 1)
-      {
-        float ohi = __shfl_xor_sync(0xffffffffu, hi, o), olo = __shfl_xor_sync(0xffffffffu, lo, o);
-        float sh, se;
-        twoSumF(hi, ohi, sh, se);
-        hi = sh;
-        lo = __fadd_rn(__fadd_rn(lo, olo), se);
-      }
-      tot[u] = (double)hi + (double)lo;
-    }
-  };
-  // Pass 1: the centroid in record integers (exact int64 sums).  Pass 2:
-  // FP32 coordinates about it in record units, u = X - centroid (exact in
-  // FP32), and the compensated sums of their products, which are exact while
-  // a product stays below 2^24 (|u| * |v| of a 1.5 m tile at 1 mm is below
-  // 2^20); the scales are applied in FP64.
+  // the first point as the origin of the integer sums (the cloud spans less
+  // than 2^30 record units, so the differences fit)
+  const uint32_t j0 = s.tilePts[b0];
+  const int32_t ox = a.sx[j0], oy = a.sy[j0], az = a.sz[j0];
   long long isum[3] = {0, 0, 0};
   for (uint32_t i = lane; i < M; i += 32)
   {
-    uint32_t j = s.tilePts[b0 + i];
-    isum[0] += a.sx[j] - ax;
-    isum[1] += a.sy[j] - ay;
+    const uint32_t j = s.tilePts[b0 + i];
+    isum[0] += a.sx[j] - ox;
+    isum[1] += a.sy[j] - oy;
     isum[2] += a.sz[j] - az;
   }
   for (int d = 0; d < 3; d++)
     for (int o = 16; o; o >>= 1)
       isum[d] += __shfl_xor_sync(0xffffffffu, isum[d], o);
-  const int32_t cX = ax + (int32_t)llrint((double)isum[0] / M), cY = ay + (int32_t)llrint((double)isum[1] / M),
-                cZ = az + (int32_t)llrint((double)isum[2] / M);
-  double cs[kQ];
-  warpSum([&](uint32_t j, float *q) {
-    float u = (float)(a.sx[j] - cX), v = (float)(a.sy[j] - cY), t = (float)(a.sz[j] - cZ);
+  // an integer next to the centroid (truncated quotient): only the origin of
+  // the FP32 products, so any nearby integer will do
+  const int32_t cX = ox + (int32_t)(isum[0] / (long long)M), cY = oy + (int32_t)(isum[1] / (long long)M),
+                cZ = az + (int32_t)(isum[2] / (long long)M);
+  float sum[kQ], cmp[kQ];
+  for (int u = 0; u < kQ; u++)
+    sum[u] = cmp[u] = 0.f;
+  for (uint32_t i = lane; i < M; i += 32)
+  {
+    const uint32_t j = s.tilePts[b0 + i];
+    const float u = (float)(a.sx[j] - cX), v = (float)(a.sy[j] - cY), t = (float)(a.sz[j] - cZ);
+    float q[kQ];
     q[0] = __fmul_rn(u, u);
     q[1] = __fmul_rn(v, u);
     q[2] = __fmul_rn(v, v);
@@ -1031,26 +1041,67 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
     q[5] = __fmul_rn(u, t);
     q[6] = __fmul_rn(v, t);
     q[7] = t;
-  }, cs, kQ);
-  // the sums of the tile-centre frame (heights from z0), rebuilt in FP64:
-  // x = u*kx + X, y = v*ky + Y, z - z0 = t*kz + Z
-  const double kx = a.scale[0] * a.unit, ky = a.scale[1] * a.unit, kz = a.scale[2] * a.unit;
-  const double X = dec(a, 0, cX) - cx, Y = dec(a, 1, cY) - cy, Z = dec(a, 2, cZ) - z0, Md = (double)M;
-  const double uu = cs[0] * kx * kx, uv = cs[1] * kx * ky, vv = cs[2] * ky * ky, su = cs[3] * kx, sv = cs[4] * ky,
-               ut = cs[5] * kx * kz, vt = cs[6] * ky * kz, st = cs[7] * kz;
-  double tot[kQ];
-  tot[0] = uu + 2 * X * su + Md * X * X;
-  tot[1] = uv + X * sv + Y * su + Md * X * Y;
-  tot[2] = vv + 2 * Y * sv + Md * Y * Y;
-  tot[3] = su + Md * X;
-  tot[4] = sv + Md * Y;
-  tot[5] = ut + Z * su + X * st + Md * X * Z;
-  tot[6] = vt + Z * sv + Y * st + Md * Y * Z;
-  tot[7] = st + Md * Z;
-  double sx = 0, sy = 0;
-  if (lane == 0)
+    for (int e = 0; e < kQ; e++)
+    {
+      const float yv = __fsub_rn(q[e], cmp[e]);
+      const float tt = __fadd_rn(sum[e], yv);
+      cmp[e] = __fsub_rn(__fsub_rn(tt, sum[e]), yv);
+      sum[e] = tt;
+    }
+  }
+  Scan32Sums out;
+  for (int e = 0; e < kQ; e++)
   {
-    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], (double)M}};
+    float hi = sum[e], lo = -cmp[e];
+    for (int o = 16; o; o >>= 1)
+    {
+      const float ohi = __shfl_xor_sync(0xffffffffu, hi, o), olo = __shfl_xor_sync(0xffffffffu, lo, o);
+      float sh, se;
+      twoSumF(hi, ohi, sh, se);
+      hi = sh;
+      lo = __fadd_rn(__fadd_rn(lo, olo), se);
+    }
+    out.hi[e] = hi;
+    out.lo[e] = lo;
+  }
+  out.cX = cX;
+  out.cY = cY;
+  out.cZ = cZ;
+  out.az = az;
+  if (lane == 0)
+    work[k].p = out;
+}
+
+/* The tile-centre sums rebuilt in FP64 from the centroid sums (x = u kx + X,
+ * y = v ky + Y, z - z0 = t kz + Z), the solve and the slope clamp, one
+ * thread per tile. */
+__global__ void scan32Solve(TileArgs a, const uint32_t *__restrict__ tileN, const TileFrame *__restrict__ frames,
+                            ScanWork32 *__restrict__ work, TileRes *__restrict__ res)
+{
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.T; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const uint32_t M = tileN[k];
+    if (M == 0)
+      continue;
+    const Scan32Sums p = work[k].p;
+    double cs[kQ];
+    for (int e = 0; e < kQ; e++)
+      cs[e] = (double)p.hi[e] + (double)p.lo[e];
+    const double cx = frames[k].cx, cy = frames[k].cy, z0 = dec(a, 2, p.az);
+    const double kx = a.scale[0] * a.unit, ky = a.scale[1] * a.unit, kz = a.scale[2] * a.unit;
+    const double X = dec(a, 0, p.cX) - cx, Y = dec(a, 1, p.cY) - cy, Z = dec(a, 2, p.cZ) - z0, Md = (double)M;
+    const double uu = cs[0] * kx * kx, uv = cs[1] * kx * ky, vv = cs[2] * ky * ky, su = cs[3] * kx, sv = cs[4] * ky,
+                 ut = cs[5] * kx * kz, vt = cs[6] * ky * kz, st = cs[7] * kz;
+    double tot[kQ];
+    tot[0] = uu + 2 * X * su + Md * X * X;
+    tot[1] = uv + X * sv + Y * su + Md * X * Y;
+    tot[2] = vv + 2 * Y * sv + Md * Y * Y;
+    tot[3] = su + Md * X;
+    tot[4] = sv + Md * Y;
+    tot[5] = ut + Z * su + X * st + Md * X * Z;
+    tot[6] = vt + Z * sv + Y * st + Md * Y * Z;
+    tot[7] = st + Md * Z;
+    double m[3][3] = {{tot[0], tot[1], tot[3]}, {tot[1], tot[2], tot[4]}, {tot[3], tot[4], Md}};
     double bv[3] = {tot[5], tot[6], tot[7]};
     for (int i = 0; i < 3; i++)
     {
@@ -1061,17 +1112,12 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
     for (int i = 2; i >= 0; i--)
       for (int j = 0; j < i; j++)
         rowOp3(m, bv, i, j, i);
-    double v0 = bv[0], v1 = bv[1];
-    if (m[0][0] == 0)
-      v0 = NAN;
-    if (m[1][1] == 0)
-      v1 = NAN;
-    r.plane[0] = v0;
-    r.plane[1] = v1;
-    r.plane[2] = m[2][2] == 0 ? NAN : bv[2] + z0;
-    sx = v0;
-    sy = v1;
-    double len = wb_hypot(sx, sy);
+    const double v0 = m[0][0] == 0 ? NAN : bv[0], v1 = m[1][1] == 0 ? NAN : bv[1];
+    res[k].plane[0] = v0;
+    res[k].plane[1] = v1;
+    res[k].plane[2] = m[2][2] == 0 ? NAN : bv[2] + z0;
+    double sx = v0, sy = v1;
+    const double len = wb_hypot(sx, sy);
     if (len > 1)
     {
       sx /= len;
@@ -1079,57 +1125,63 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
     }
     if (isnan(sx) || isnan(sy))
       sx = sy = 0;
+    work[k].w.s.sx = sx;
+    work[k].w.s.sy = sy;
   }
-  const float fsx = (float)__shfl_sync(0xffffffffu, sx, 0), fsy = (float)__shfl_sync(0xffffffffu, sy, 0);
+}
+
+/* Passes 2-4 of the precision mode, one warp per tile, in FP32: untilt,
+ * bottom (first minimum), bottom2, top and the sector histogram. */
+__global__ void __launch_bounds__(32 * kScanWarps) scan32Shape(ScanArgs s, const TileFrame *__restrict__ frames,
+                                                               ScanWork32 *__restrict__ work)
+{
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const TileArgs &a = s.t;
+  const uint64_t k = (uint64_t)blockIdx.x * kScanWarps + w;
+  if (k >= a.T)
+    return;
+  const uint32_t b0 = s.tileStart[k], M = s.tileN[k];
+  if (M == 0)
+    return;
+  const Frame32 g = frame32(a, frames[k], work[k].p.az);
+  const float fsx = (float)work[k].w.s.sx, fsy = (float)work[k].w.s.sy;
   auto untilt = [&](float x, float y, float z) { return __fsub_rn(z, __fadd_rn(__fmul_rn(fsy, y), __fmul_rn(fsx, x))); };
-  float bottom = INFINITY, top = -INFINITY;
-  uint32_t argmin = 0xffffffffu;
-  for (uint32_t c0 = 0; c0 < M; c0 += 32)
+  float mv = INFINITY, top = -INFINITY;
+  uint32_t mi = 0xffffffffu;
+  for (uint32_t i = lane; i < M; i += 32)
   {
-    uint32_t i = c0 + lane;
-    float uz = INFINITY, ut = -INFINITY;
-    if (i < M)
+    float x, y, z;
+    local32(a, g, s.tilePts[b0 + i], x, y, z);
+    const float uz = untilt(x, y, z);
+    if (uz < mv)
     {
-      float x, y, z;
-      local(s.tilePts[b0 + i], x, y, z);
-      uz = ut = untilt(x, y, z);
+      mv = uz;
+      mi = i;
     }
-    float mv = uz;
-    uint32_t mi = i < M ? i : 0xffffffffu;
-    for (int o = 16; o; o >>= 1)
-    {
-      float ov = __shfl_xor_sync(0xffffffffu, mv, o);
-      uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
-      if (ov < mv || (ov == mv && oi < mi))
-      {
-        mv = ov;
-        mi = oi;
-      }
-    }
-    if (mv < bottom)
-    {
-      bottom = mv;
-      argmin = mi;
-    }
-    for (int o = 16; o; o >>= 1)
-      ut = fmaxf(ut, __shfl_xor_sync(0xffffffffu, ut, o));
-    top = fmaxf(top, ut);
+    top = fmaxf(top, uz);
   }
+  for (int o = 16; o; o >>= 1)
+  {
+    const float ov = __shfl_xor_sync(0xffffffffu, mv, o);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, mi, o);
+    if (ov < mv || (ov == mv && oi < mi))
+    {
+      mv = ov;
+      mi = oi;
+    }
+    top = fmaxf(top, __shfl_xor_sync(0xffffffffu, top, o));
+  }
+  const float bottom = mv;
+  const uint32_t argmin = mi;
   float bottom2 = INFINITY;
-  for (uint32_t c0 = 0; c0 < M && c0 < argmin; c0 += 32)
+  for (uint32_t i = lane; i < M && i < argmin; i += 32)
   {
-    uint32_t i = c0 + lane;
-    float v = INFINITY;
-    if (i < M && i < argmin)
-    {
-      float x, y, z;
-      local(s.tilePts[b0 + i], x, y, z);
-      v = untilt(x, y, z);
-    }
-    for (int o = 16; o; o >>= 1)
-      v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    bottom2 = fminf(bottom2, v);
+    float x, y, z;
+    local32(a, g, s.tilePts[b0 + i], x, y, z);
+    bottom2 = fminf(bottom2, untilt(x, y, z));
   }
+  for (int o = 16; o; o >>= 1)
+    bottom2 = fminf(bottom2, __shfl_xor_sync(0xffffffffu, bottom2, o));
   if (isinf(bottom2))
     bottom2 = bottom;
   const float lim = __fadd_rn(bottom2, (float)(2 * a.rad)), inner = (float)(a.rad / 2.6457513110645905905016);
@@ -1137,12 +1189,12 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
   int histo[7] = {0, 0, 0, 0, 0, 0, 0};
   for (uint32_t c0 = 0; c0 < M; c0 += 32)
   {
-    uint32_t i = c0 + lane;
+    const uint32_t i = c0 + lane;
     int sector = -1;
     if (i < M)
     {
       float x, y, z;
-      local(s.tilePts[b0 + i], x, y, z);
+      local32(a, g, s.tilePts[b0 + i], x, y, z);
       if (untilt(x, y, z) < lim)
       {
         sector = (int)rintf(atan2f(y, x) * 0.954929658551372f);   // 3 / pi
@@ -1159,24 +1211,12 @@ __global__ void __launch_bounds__(32 * kTileWarps) scanKernel32(ScanArgs s, Tile
   }
   if (lane == 0)
   {
-    double density = 0;
-    int treeFlags = 0;
-    for (int i = 0; i < 7; i++)
-      density += (double)histo[i] * (double)histo[i];
-    if (M > nBottom && density < 7)
-      treeFlags = 1;
-    density = sqrt(density) * 2.6457513110645905905016 / (a.rad * a.rad) / M_PI;
-    if (M > nBottom && density < 0.5)
-      treeFlags = 1;
-    if ((double)top - (double)bottom > 1.5)
-      treeFlags = 1;
-    r.nPoints = (int32_t)M;
-    r.nGround = 0;
-    r.treeFlags = treeFlags;
-    r.density = density;
-    r.hScan = r.h = sqrt(1 / density + s.minH * s.minH);
-    r.height = (double)top - (double)bottom;
-    res[k] = r;
+    ScanWork &o = work[k].w;
+    o.s.top = (double)top;
+    o.s.bottom = (double)bottom;
+    for (int e = 0; e < 7; e++)
+      o.s.histo[e] = (uint32_t)histo[e];
+    o.s.nBottom = nBottom;
   }
 }
 
@@ -1498,16 +1538,23 @@ int wb_scan_impl(wb_ctx *c, const wb_params *p)
   s.tilePts = (const uint32_t *)c->tilePts.p;
   s.minH = p->min_hyp_size;
   TileRes *res = (TileRes *)c->tileRes.p;
+  // one work slot per tile (64 B, 80 B in the precision mode); the centres
+  // come from the tile frames
+  if ((rc = wb_ensure(c, c->scanTot, T * sizeof(ScanWork32) + 64)))
+    return rc;
+  const unsigned sb = (unsigned)((T + kScanWarps - 1) / kScanWarps);
+  const unsigned tb = (unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32);
   if (c->precision == WB_PRECISION_FP32 && a.fast)
-    { scanKernel32<<<blocks, 32 * kTileWarps, 0, c->stream>>>(s, res); ++c->launches; }
+  {
+    ScanWork32 *work = (ScanWork32 *)c->scanTot.p;
+    { scan32Sums<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, work); ++c->launches; }
+    { scan32Solve<<<tb, 128, 0, c->stream>>>(a, tileN, frames, work, res); ++c->launches; }
+    { scan32Shape<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, frames, work); ++c->launches; }
+    { scanFinish<<<tb, 128, 0, c->stream>>>(T, tileN, work, a.rad, p->min_hyp_size, res); ++c->launches; }
+  }
   else
   {
-    // one ScanWork slot (64 B) per tile; the centres come from the tile frames
-    if ((rc = wb_ensure(c, c->scanTot, T * sizeof(ScanWork) + 64)))
-      return rc;
     ScanWork *work = (ScanWork *)c->scanTot.p;
-    const unsigned sb = (unsigned)((T + kScanWarps - 1) / kScanWarps);
-    const unsigned tb = (unsigned)std::min<uint64_t>((T + 127) / 128, (uint64_t)c->sm_count * 32);
     { scanSums<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, frames, work); ++c->launches; }
     { scanSolve<<<tb, 128, 0, c->stream>>>(T, tileN, work, res); ++c->launches; }
     { scanShape<<<sb, 32 * kScanWarps, 0, c->stream>>>(s, frames, work); ++c->launches; }
