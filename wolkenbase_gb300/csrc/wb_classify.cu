@@ -858,6 +858,11 @@ struct GroupSmem
   float apex, por2min;
   int kmaxG, smaxG;
   int4 cbox;
+  /* the columns / super-cells the lanes hold while the warp walks them, and
+     their boxes (read by every lane from shared memory, not kept in registers) */
+  int4 nbox[32], sbox[32];
+  unsigned long long ncol[32];
+  int2 sij[32];
 };
 
 
@@ -1063,16 +1068,12 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         sm.amode[lane] = 0;
       return dec;
     };
-    // whether any undecided lane's arc meets the box that lane src holds
+    // whether any undecided lane's arc meets box src of boxes (shared memory)
     // (record integers); true at once while no undecided lane has an arc
-    auto boxWanted = [&](const int4 &mine, int src) -> bool {
+    auto boxWanted = [&](const int4 *boxes, int src) -> bool {
       if (!__any_sync(0xffffffffu, !done && sm.amode[lane] != 0))
         return true;
-      int4 b;
-      b.x = __shfl_sync(0xffffffffu, mine.x, src);
-      b.y = __shfl_sync(0xffffffffu, mine.y, src);
-      b.z = __shfl_sync(0xffffffffu, mine.z, src);
-      b.w = __shfl_sync(0xffffffffu, mine.w, src);
+      const int4 b = boxes[src];
       bool want = false;
       if (!done)
         want = arcMeetsBox(sm, lane, (float)(b.x - me.x) * sx, (float)(b.z - me.x) * sx, (float)(b.y - me.y) * sy,
@@ -1292,12 +1293,16 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, ok);
+      __syncwarp();
+      sm.nbox[lane] = cb;
+      sm.ncol[lane] = c;
+      __syncwarp();
       while (mask && !allDone())
       {
         const int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        const uint64_t cc = __shfl_sync(0xffffffffu, c, src);
-        if (boxWanted(cb, src))
+        const uint64_t cc = sm.ncol[src];
+        if (boxWanted(sm.nbox, src))
           scanColumn(cc);
       }
     }
@@ -1329,12 +1334,16 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           }
         }
         unsigned mask = __ballot_sync(0xffffffffu, ok);
+        __syncwarp();
+        sm.sbox[lane] = sb;
+        sm.sij[lane] = make_int2(SI, SJ);
+        __syncwarp();
         while (mask && !allDone())
         {
           const int src = __ffs(mask) - 1;
           mask &= mask - 1;
-          const int SIs = __shfl_sync(0xffffffffu, SI, src), SJs = __shfl_sync(0xffffffffu, SJ, src);
-          if (!boxWanted(sb, src))
+          const int SIs = sm.sij[src].x, SJs = sm.sij[src].y;
+          if (!boxWanted(sm.sbox, src))
             continue;
           const int bi = SIs * S, bj = SJs * S;
           uint64_t c = 0;
@@ -1351,12 +1360,16 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
             }
           }
           unsigned cm = __ballot_sync(0xffffffffu, cok);
+          __syncwarp();
+          sm.nbox[lane] = cb;
+          sm.ncol[lane] = c;
+          __syncwarp();
           while (cm && !allDone())
           {
             const int cs = __ffs(cm) - 1;
             cm &= cm - 1;
-            const uint64_t cc = __shfl_sync(0xffffffffu, c, cs);
-            if (boxWanted(cb, cs))
+            const uint64_t cc = sm.ncol[cs];
+            if (boxWanted(sm.nbox, cs))
               scanColumn(cc);
           }
         }
