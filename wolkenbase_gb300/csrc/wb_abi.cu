@@ -119,7 +119,7 @@ void wb_release_buffers(wb_ctx *c)
 {
   DevBuf *all[] = {&c->rec, &c->key0, &c->key1, &c->idx0, &c->idx1, &c->tmp32, &c->tmp32b, &c->tmp8, &c->scanTmp,
                    &c->small, &c->lev, &c->cpl, &c->pre, &c->suf, &c->leafId, &c->leafFirst, &c->leafCount,
-                   &c->leafLevel, &c->leafKey, &c->leafBox, &c->sidx, &c->sx, &c->sy, &c->sz, &c->xyzd, &c->colOf, &c->pointLeaf,
+                   &c->leafLevel, &c->leafKey, &c->leafBox, &c->sidx, &c->sx, &c->sy, &c->sz, &c->xyzd, &c->colOf, &c->gridBounds, &c->pointLeaf,
                    &c->storeOf, &c->survivorOf, &c->nodeChild, &c->nodeBox, &c->nodeStart, &c->nodeIdLevel,
                    &c->tileEx, &c->tileEy, &c->tileLookup, &c->tileStart, &c->tilePts, &c->owner, &c->tileRes,
                    &c->tileHuge, &c->hugePre, &c->scanTot, &c->tileFrm,

@@ -31,7 +31,72 @@ struct GridArgs
   double x0, y0, cell;
   int nx, ny;
   double rootLo[3], rootHi[3];
+  /* integer thresholds (thr = 1: the decode increases with the record integer
+     on every axis): xb[0..nx], yb[0..ny], then the root cube's faces
+     {x, y, z lo, x, y, z hi} */
+  const long long *bounds;
+  int thr;
+  float colPerUnit[2];
 };
+
+/* Smallest record integer X in [-2^31, 2^31) with pred(X), for a predicate
+ * that is false then true as X grows; 2^31 when it never holds. */
+template <typename P>
+__device__ long long firstTrue(P pred)
+{
+  long long lo = -2147483648LL, hi = 2147483648LL;   // pred(lo) false, pred(hi) taken as true
+  if (pred(lo))
+    return lo;
+  while (hi - lo > 1)
+  {
+    const long long mid = lo + (hi - lo) / 2;
+    if (pred(mid))
+      hi = mid;
+    else
+      lo = mid;
+  }
+  return hi;
+}
+
+/* The record-integer thresholds of the column boundaries and the root cube's
+ * faces, one thread each, found with the same FP64 arithmetic the per-point
+ * tests use: with a decode that increases with X, floor((dec(X) - x0) / cell)
+ * >= i exactly when X >= xb[i], and dec(X) < lo exactly when X < xlo. */
+__global__ void gridBoundsKernel(GridArgs g, long long *__restrict__ bounds)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = (g.nx + 1) + (g.ny + 1);
+  if (t <= g.nx)
+    bounds[t] = firstTrue([&](long long X) {
+      return floor((wb_decode((int32_t)X, g.off[0], g.scale[0], g.unit) - g.x0) / g.cell) >= (double)t;
+    });
+  else if (t < nb)
+  {
+    const int i = t - (g.nx + 1);
+    bounds[t] = firstTrue([&](long long X) {
+      return floor((wb_decode((int32_t)X, g.off[1], g.scale[1], g.unit) - g.y0) / g.cell) >= (double)i;
+    });
+  }
+  else if (t < nb + 6)
+  {
+    const int ax = (t - nb) % 3;
+    const double lim = (t - nb) < 3 ? g.rootLo[ax] : g.rootHi[ax];
+    bounds[t] = firstTrue([&](long long X) { return wb_decode((int32_t)X, g.off[ax], g.scale[ax], g.unit) >= lim; });
+  }
+}
+
+/* Column of record integer X on an axis with thresholds b[0..n]: X lies in
+ * [b[0], b[n]); a guess from the mean column width, then the thresholds. */
+__device__ __forceinline__ int columnOf(const long long *__restrict__ b, int n, long long X, float perUnit)
+{
+  int k = (int)((float)(X - b[0]) * perUnit);
+  k = min(max(k, 0), n - 1);
+  while (k > 0 && X < b[k])
+    k--;
+  while (k < n - 1 && X >= b[k + 1])
+    k++;
+  return k;
+}
 
 __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int32_t *__restrict__ sy,
                            const int32_t *__restrict__ sz, uint64_t *__restrict__ key, uint32_t *__restrict__ val,
@@ -48,18 +113,39 @@ __global__ void cellKernel(GridArgs g, const int32_t *__restrict__ sx, const int
       mn[a] = min(mn[a], q[a]);
       mx[a] = max(mx[a], q[a]);
     }
-    const double x = xyzd[j], y = xyzd[g.nd + j], z = xyzd[2 * g.nd + j];
     // the point's column as the classify set-up needs it (unclamped, within
-    // +-1e9), and clamped into the grid for the sort key
-    const int ci = (int)fmax(fmin(floor((x - g.x0) / g.cell), 1e9), -1e9);
-    const int cj = (int)fmax(fmin(floor((y - g.y0) / g.cell), 1e9), -1e9);
+    // +-1e9), and clamped into the grid for the sort key; from the integer
+    // thresholds where they apply, else in FP64
+    int ci, cj;
+    bool sxy, s;
+    if (g.thr)
+    {
+      const long long *xb = g.bounds, *yb = g.bounds + g.nx + 1, *face = g.bounds + g.nx + g.ny + 2;
+      const long long X = q[0], Y = q[1], Z = q[2];
+      if (X >= xb[0] && X < xb[g.nx])
+        ci = columnOf(xb, g.nx, X, g.colPerUnit[0]);
+      else
+        ci = (int)fmax(fmin(floor((xyzd[j] - g.x0) / g.cell), 1e9), -1e9);
+      if (Y >= yb[0] && Y < yb[g.ny])
+        cj = columnOf(yb, g.ny, Y, g.colPerUnit[1]);
+      else
+        cj = (int)fmax(fmin(floor((xyzd[g.nd + j] - g.y0) / g.cell), 1e9), -1e9);
+      sxy = X < face[0] || Y < face[1] || X >= face[3] || Y >= face[4];
+      s = sxy || Z < face[2] || Z >= face[5];
+    }
+    else
+    {
+      const double x = xyzd[j], y = xyzd[g.nd + j], z = xyzd[2 * g.nd + j];
+      ci = (int)fmax(fmin(floor((x - g.x0) / g.cell), 1e9), -1e9);
+      cj = (int)fmax(fmin(floor((y - g.y0) / g.cell), 1e9), -1e9);
+      sxy = x < g.rootLo[0] || y < g.rootLo[1] || x >= g.rootHi[0] || y >= g.rootHi[1];
+      s = sxy || z < g.rootLo[2] || z >= g.rootHi[2];
+    }
     colOf[j] = make_int2(ci, cj);
     const int cx = min(max(ci, 0), g.nx - 1), cy = min(max(cj, 0), g.ny - 1);
     // column in the high 32 bits, height (order-preserving int32 -> uint32) below
     key[j] = (((uint64_t)cy * g.nx + cx) << 32) | (uint32_t)(q[2] ^ (int32_t)0x80000000);
     val[j] = (uint32_t)j;
-    bool sxy = x < g.rootLo[0] || y < g.rootLo[1] || x >= g.rootHi[0] || y >= g.rootHi[1];
-    bool s = sxy || z < g.rootLo[2] || z >= g.rootHi[2];
     stray[j] = (uint8_t)((s ? 1 : 0) | (sxy ? 2 : 0));
     if (s)
       atomicAdd(nStray, 1ull);
@@ -234,6 +320,20 @@ int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1)
   a.cell = cell;
   a.nx = nx;
   a.ny = ny;
+  // integer thresholds where every axis decodes increasingly
+  a.thr = 0;
+  a.bounds = nullptr;
+  if (g.scale[0] * g.unit > 0 && g.scale[1] * g.unit > 0 && g.scale[2] * g.unit > 0)
+  {
+    const int nb = (nx + 1) + (ny + 1) + 6;
+    if ((rc = wb_ensure(c, c->gridBounds, (size_t)nb * 8 + 64)))
+      return rc;
+    a.thr = 1;
+    a.bounds = (const long long *)c->gridBounds.p;
+    a.colPerUnit[0] = (float)(g.scale[0] * g.unit / cell);
+    a.colPerUnit[1] = (float)(g.scale[1] * g.unit / cell);
+    { gridBoundsKernel<<<(unsigned)((nb + 127) / 128), 128, 0, c->stream>>>(a, (long long *)c->gridBounds.p); ++c->launches; }
+  }
   unsigned long long *dStray = (unsigned long long *)((char *)c->small.p + 256);
   int *dExt = (int *)((char *)c->small.p + 512);
   static const int kExtInit[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};

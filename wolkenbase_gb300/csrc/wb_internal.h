@@ -77,6 +77,7 @@ struct wb_ctx
      (x, y, z), each the reference's (offset + scale * X) * unit */
   DevBuf xyzd;
   DevBuf colOf;   /* column {i, j} of each stored point (unclamped, within +-1e9) */
+  DevBuf gridBounds;   /* record-integer column boundaries and root-cube faces */
   DevBuf nodeChild, nodeBox, nodeStart, nodeIdLevel;
   DevBuf tileEx, tileEy, tileLookup, tileStart, tilePts, owner, tileRes, tileH, tileN, tileNg, tileHuge, hugePre,
       scanTot, tileFrm;
