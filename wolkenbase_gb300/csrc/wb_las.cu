@@ -234,13 +234,25 @@ __global__ void __launch_bounds__(kPartThreads) partScatter(const uint8_t *__res
   // copy: word w of the tile's class-ordered records goes to its class run
   const uint32_t words = stride / 4;
   const uint64_t total = (uint64_t)tileN * words;
-  for (uint64_t w = threadIdx.x; w < total; w += kPartThreads)
-  {
-    const uint32_t lp = (uint32_t)(w / words), k = (uint32_t)(w % words);
+  auto copyWord = [&](uint32_t lp, uint32_t k) {
     const uint32_t d = clsOf[lp];
     const uint64_t dst = (uint64_t)globalStart[d] + (lp - localStart[d]);
     ((uint32_t *)out)[dst * words + k] = ((const uint32_t *)rec)[(tbase + order[lp]) * words + k];
+  };
+  if (words > 1 && total * words < (1ull << 32))
+  {
+    // w / words as the high half of w * ceil(2^32 / words): exact while
+    // w * words < 2^32 (the rounding of the reciprocal stays below 1 / words)
+    const uint32_t magic = (uint32_t)(((1ull << 32) + words - 1) / words);
+    for (uint32_t w = threadIdx.x; w < (uint32_t)total; w += kPartThreads)
+    {
+      const uint32_t lp = __umulhi(w, magic);
+      copyWord(lp, w - lp * words);
+    }
   }
+  else
+    for (uint64_t w = threadIdx.x; w < total; w += kPartThreads)
+      copyWord((uint32_t)(w / words), (uint32_t)(w % words));
 }
 
 unsigned gridOf(const wb_ctx *c, uint64_t n)
