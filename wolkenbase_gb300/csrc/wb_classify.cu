@@ -427,7 +427,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
   uint32_t occLo = 0, occHi = 0;
   uint32_t gapNow = 0;   // the largest gap at the last surround test that formed it
   bool gapValid = false;
-  // The fast pass's arc (see setArc): directions outside the one gap that can
+  // The point's arc (see setArc): directions outside the one gap that can
   // still decide the point change nothing, so boxes outside it are skipped.
   int amode = 0;
   float e0x = 0.f, e0y = 0.f, e1x = 0.f, e1y = 0.f;
@@ -594,26 +594,28 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
     WB_STAT(stat[12], clock64() - tc);
     return got;
   };
-  // Surround test.  A circular run of 27 empty bins (151.9 degrees) already
-  // proves a gap above 144 degrees plus both margins; only otherwise is the
-  // exact largest gap formed from the bin extremes.
+  // Surround test from the bin extremes; it also gives the arc.  The fast
+  // pass decides two margins away from 144 degrees, exact directions (the
+  // exact pass, clouds without exact 32-bit differences) and the precision
+  // mode at 144 degrees.  The arc is as sound with exact directions: only a
+  // direction inside the one gap at or above the threshold can change the
+  // label or the largest gap.
   auto decideBody = [&]() {
     WB_STAT(stat[6], 1);
     uint64_t occ = ((uint64_t)occHi << 32) | occLo;
     if (__popcll(occ) < 2)
       return;
-    if (fast)
     {
-      // the fast pass always forms the gaps: they give the arc
       __syncwarp();
       int nocc, nbig;
       uint32_t u0, w;
-      const uint32_t thr = a.fp32Only ? (uint32_t)WB_DEG144 : (uint32_t)WB_DEG144 - 2 * kMargin;
+      const bool at144 = !fast || a.fp32Only;
+      const uint32_t thr = at144 ? (uint32_t)WB_DEG144 : (uint32_t)WB_DEG144 - 2 * kMargin;
       uint32_t gap = largestGapArc(bminW, bmaxW, lane, thr, nocc, nbig, u0, w);
       gapNow = gap;
       gapValid = nocc >= 2;
       if (nocc >= 2)
-        surrounded = a.fp32Only ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
+        surrounded = at144 ? gap < (uint32_t)WB_DEG144 : gap + 2 * kMargin < (uint32_t)WB_DEG144;
       amode = 0;
       if (!surrounded && nbig == 1)
       {
@@ -632,23 +634,7 @@ __device__ __forceinline__ void classifyPoint(const ClsArgs &a, uint64_t j, int 
           amode = W < 3.14159f ? 1 : 2;
         }
       }
-      return;
     }
-    uint64_t r = ~occ;
-    r &= (r << 1) | (r >> 63);
-    r &= (r << 2) | (r >> 62);
-    r &= (r << 4) | (r >> 60);
-    r &= (r << 8) | (r >> 56);
-    r &= (r << 11) | (r >> 53);
-    if (r)
-      return;
-    __syncwarp();
-    int nocc;
-    uint32_t gap = largestGap(bminW, bmaxW, lane, nocc);
-    gapNow = gap;
-    gapValid = nocc >= 2;
-    if (nocc >= 2)
-      surrounded = gap < (uint32_t)WB_DEG144;
   };
   auto decide = [&]() {
 #ifdef WB_CLASSIFY_STATS
