@@ -990,6 +990,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
     envelope();
     bool deferred = false;
     int columnsRead = 0;
+#ifdef WB_CLASSIFY_STATS
+    bool farField = false;   // lane tests beyond the near field (instrumented builds)
+#endif
     // envelope test of a box {x0, y0, x1, y1} with lowest point zmin
     auto envMeets = [&](const int4 &b, int32_t zmin) -> bool {
       if (b.x == INT32_MAX)
@@ -1137,7 +1140,7 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
           break;
         unsigned lm = __ballot_sync(0xffffffffu, keep);
         WB_STAT(gst[2], __popc(lm));
-        WB_STAT(gst[11], 1);
+        WB_STAT(gst[11], farField ? __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)) : 0);
         WB_STAT(gst[3], __popc(lm) * __popc(__ballot_sync(0xffffffffu, !done)));
         sm.cand[lane] = q;
         __syncwarp();
@@ -1293,6 +1296,9 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
       }
     }
     // far field: rings of super-cells, then their columns outside the near field
+#ifdef WB_CLASSIFY_STATS
+    farField = true;
+#endif
     const int S = WB_SUPER;
     const int si = ci0 / S, sj = cj0 / S;
     for (int sr = 0; sr <= sm.smaxG && sm.kmaxG > kNearG && !allDone(); sr++)
