@@ -335,7 +335,7 @@ def generate(specs, procs=None):
 
 def _tuned(st):
     from wolkenbase_gb300 import _lib
-    shapes = ["groups 4 warps/5 blocks", "groups 8/3", "groups 8/2", "points 8/3", "points 4/6", "points 4/8",
+    shapes = ["groups 8 warps/3 blocks", "groups 4/5", "groups 8/2", "points 8/3", "points 4/6", "points 4/8",
               "points 8/4", "points 2/12"]
     return {"shape": shapes[st["shape"]], "chunk": st["chunk"], "grid_points": st["grid_points"],
             "tune_ms": st["tune_ms"]}
