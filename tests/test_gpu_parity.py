@@ -126,6 +126,32 @@ def test_random_tiles_match_oracle(classifier, oracle_mod, seed, n):
     assert np.array_equal(r["cs"][r["pleaf"]], o["leaves"][o["leaf"]])
 
 
+def test_negative_scales_match_oracle(classifier, oracle_mod):
+    """x and z record integers that run against the coordinates (negative
+    scales; the same decoded points as a positive-scale cloud): the tile
+    gather's column tests and the classify's box bounds must not take a box's
+    low record integer as its low coordinate, and the cell kernel's integer
+    thresholds do not apply."""
+    from wolkenbase_gb300 import synth
+    import wolkenbase_gb300 as wb
+    base = synth.density_tile(20000, 404)
+    xyz = base.xyz.copy()
+    xyz[:, 0] = -xyz[:, 0]
+    xyz[:, 2] = -xyz[:, 2]
+    cloud = synth.Cloud(xyz=xyz, scale=(-base.scale[0], base.scale[1], -base.scale[2]), offset=base.offset,
+                        unit=base.unit, minc=base.minc, maxc=base.maxc)
+    assert np.array_equal(cloud.decoded(), base.decoded())
+    r = _gpu_run(classifier, cloud, wb.Params())
+    o = oracle_mod.run(cloud, canonical_order=True, threads=16)
+    assert np.array_equal(r["tiles"]["n_points"], o["tiles"]["n_points"])
+    assert np.array_equal(r["tiles"]["hyperboloid_size"], o["tiles"]["h_final"])
+    bad = np.nonzero(r["cls"] != o["cls"])[0]
+    assert bad.size == 0, f"{bad.size} labels differ from the oracle, e.g. {bad[:10].tolist()}"
+    # the same decoded points as the positive-scale cloud: the same labels
+    r0 = _gpu_run(classifier, base, wb.Params())
+    assert np.array_equal(r0["cls"], r["cls"])
+
+
 def test_large_cloud_properties(classifier):
     """Size-independent checks at 4M points: determinism, leaf invariants,
     input-order independence of the octree."""

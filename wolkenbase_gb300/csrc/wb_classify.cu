@@ -224,6 +224,10 @@ __device__ __forceinline__ bool boxMeets(const Hyp &h, const int4 &b, int32_t zm
 {
   if (b.x == INT32_MAX)
     return false;   // empty block
+  // the bound takes the box's low record integers as its low coordinates:
+  // only for a decode that increases with the record integer
+  if (!(h.sx > 0.f && h.sy > 0.f && h.sz > 0.f))
+    return true;
   float xl = (float)(b.x - h.qx) * h.sx, xh = (float)(b.z - h.qx) * h.sx;
   float yl = (float)(b.y - h.qy) * h.sy, yh = (float)(b.w - h.qy) * h.sy;
   float zd = (float)(h.qz - zmin) * h.sz + h.czp;
@@ -1420,9 +1424,12 @@ __device__ __forceinline__ void classifyGroup(const ClsArgs &a, uint2 grp, int l
  * integers stand for differences of the doubles. */
 static bool decodeIsExact(const WbGeom &g, const double mn[3], const double mx[3])
 {
+  // the decode must increase with the record integer (the FP32 paths take a
+  // box's low record integers as its low coordinates and a column's height
+  // order from its record order), in steps FP64 resolves
   for (int a = 0; a < 3; a++)
   {
-    double step = fabs(g.scale[a] * g.unit);
+    double step = g.scale[a] * g.unit;
     double mag = fmax(fabs(mn[a]), fabs(mx[a])) + fabs(g.off[a] * g.unit) + step;
     if (!(step > 0) || step < 4 * ldexp(mag, -52))
       return false;

@@ -39,7 +39,7 @@ struct TileArgs
   const int32_t *sx, *sy, *sz;
   const double *xyzd;   /* decoded x, y, z planes of nd doubles */
   uint64_t nd;
-  int fast;   /* FP32 filter allowed: decode strictly increasing, 32-bit record differences exact */
+  int fast;   /* FP32 filter allowed: decode steps nonzero (either sign), 32-bit record differences exact */
 };
 
 __device__ __forceinline__ void tileCenter(const TileArgs &a, uint64_t k, double &x, double &y)
@@ -139,8 +139,21 @@ __device__ __forceinline__ bool cylMember(const TileArgs &a, const GridDev &gd, 
 
 __device__ __forceinline__ bool cellMeetsCyl(const TileArgs &a, const int4 &box, double cx, double cy)
 {
+  // a negative scale reverses the decoded box
   double x0 = dec(a, 0, box.x), x1 = dec(a, 0, box.z);
   double y0 = dec(a, 1, box.y), y1 = dec(a, 1, box.w);
+  if (x0 > x1)
+  {
+    const double t = x0;
+    x0 = x1;
+    x1 = t;
+  }
+  if (y0 > y1)
+  {
+    const double t = y0;
+    y0 = y1;
+    y1 = t;
+  }
   double dx = cx < x0 ? x0 - cx : (cx > x1 ? cx - x1 : 0.0);
   double dy = cy < y0 ? y0 - cy : (cy > y1 ? cy - y1 : 0.0);
   double r = a.rad * (1 + 1e-6) + 1e-6;
@@ -157,8 +170,10 @@ __device__ __forceinline__ bool cellMeets(const TileArgs &a, const TileFrame &f,
 {
   if (!a.fast)
     return cellMeetsCyl(a, box, f.cx, f.cy);
-  const float x0 = ((float)(box.x - f.qx0) - f.fx) * f.sx, x1 = ((float)(box.z - f.qx0) - f.fx) * f.sx;
-  const float y0 = ((float)(box.y - f.qy0) - f.fy) * f.sy, y1 = ((float)(box.w - f.qy0) - f.fy) * f.sy;
+  const float ax = ((float)(box.x - f.qx0) - f.fx) * f.sx, bx = ((float)(box.z - f.qx0) - f.fx) * f.sx;
+  const float ay = ((float)(box.y - f.qy0) - f.fy) * f.sy, by = ((float)(box.w - f.qy0) - f.fy) * f.sy;
+  // a negative scale reverses the box's ends
+  const float x0 = fminf(ax, bx), x1 = fmaxf(ax, bx), y0 = fminf(ay, by), y1 = fmaxf(ay, by);
   const float dx = x0 > 0 ? x0 : (x1 < 0 ? -x1 : 0.f);
   const float dy = y0 > 0 ? y0 : (y1 < 0 ? -y1 : 0.f);
   return dx * dx + dy * dy <= f.r2hi * 1.0002f + 1e-8f;
