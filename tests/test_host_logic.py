@@ -122,3 +122,45 @@ def test_bench_oracle_baseline_parity_on_a_small_cloud():
     assert base["value"] > 0 and base["kind"] == "port"
     assert parity["octree_exact"] and parity["sampled_tiles_exact"] == parity["sampled_tiles"]
     assert parity["sampled_labels"] > 0 and parity["agreement"] == 1.0
+
+
+def test_scan_packed_pairwise_tree_groups_as_the_reference():
+    """The exact scan adds the eight quantities of a 32-point chunk's four
+    groups of eight with a lane exchange (pairs, quads, groups; each lane adds
+    the quantities it and its partner split).  Replayed here lane by lane with
+    the kernel's index rules, every group sum equals the fixed tree
+    ((a0+a1)+(a2+a3))+((a4+a5)+(a6+a7)) of pairwisesum bit for bit, and lane l
+    of the first eight holds quantity 4*(l&1) + 2*((l>>1)&1) + ((l>>2)&1)."""
+    rng = np.random.default_rng(11)
+    for _ in range(100):
+        q = rng.standard_normal((32, 8)) * 10.0 ** rng.integers(-8, 9, (32, 8))
+        s1 = np.zeros((32, 4))
+        for r in range(4):
+            give = np.array([q[l][r] if l & 1 else q[l][4 + r] for l in range(32)])
+            for l in range(32):
+                s1[l][r] = (q[l][4 + r] if l & 1 else q[l][r]) + give[l ^ 1]
+        s2 = np.zeros((32, 2))
+        for t in range(2):
+            give = np.array([s1[l][t] if (l >> 1) & 1 else s1[l][2 + t] for l in range(32)])
+            for l in range(32):
+                s2[l][t] = (s1[l][2 + t] if (l >> 1) & 1 else s1[l][t]) + give[l ^ 2]
+        give = np.array([s2[l][0] if (l >> 2) & 1 else s2[l][1] for l in range(32)])
+        for l in range(32):
+            g = (s2[l][1] if (l >> 2) & 1 else s2[l][0]) + give[l ^ 4]
+            u, gq = 4 * (l & 1) + 2 * ((l >> 1) & 1) + ((l >> 2) & 1), l >> 3
+            a = q[8 * gq:8 * gq + 8, u]
+            assert g == ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]))
+
+
+def test_split_word_index_by_multiply_high_is_exact():
+    """The class split finds a word's record as the high half of
+    w * ceil(2^32 / words): exact while w * words < 2^32, which holds for every
+    tile of 2048 records whenever the kernel takes that path."""
+    for words in range(2, 4096):
+        magic = ((1 << 32) + words - 1) // words
+        total = 2048 * words
+        if total * words >= 1 << 32:
+            continue
+        w = np.unique(np.concatenate([np.arange(0, min(total, 3000)), np.arange(max(0, total - 3000), total),
+                                      np.arange(0, total, max(1, total // 5000))])).astype(np.uint64)
+        assert np.array_equal((w * np.uint64(magic)) >> np.uint64(32), w // np.uint64(words)), words
