@@ -304,9 +304,11 @@ __global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const 
   for (int k = 2; k <= P; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1)
     {
+      // comparator t's lower element: (t / j) * 2j + t % j, with shifts (j is a power of two)
+      const int lj = __ffs(j) - 1;
       for (int t = threadIdx.x; t < half; t += kLeafThreads)
       {
-        const int i = (t / j) * 2 * j + (t % j), u = i + j;
+        const int i = ((t >> lj) << (lj + 1)) | (t & (j - 1)), u = i + j;
         const bool up = (i & k) == 0;
         const uint32_t x = v[i], y = v[u];
         if ((x > y) == up)
