@@ -404,6 +404,9 @@ int wb_octree_point_leaf(wb_ctx *c, uint32_t *out)
     return wb_fail(c, WB_ESTATE, "wb_octree_point_leaf: no octree built");
   if (c->n)
   {
+    int rc = wb_point_leaf_map(c);
+    if (rc)
+      return rc;
     WB_CUDA(c, cudaMemcpyAsync(out, c->pointLeaf.p, c->n * 4, cudaMemcpyDefault, c->stream));
     WB_CUDA(c, cudaStreamSynchronize(c->stream));
   }

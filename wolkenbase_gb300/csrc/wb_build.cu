@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const 
                                                                uint32_t *__restrict__ sidx, int32_t *__restrict__ sx,
                                                                int32_t *__restrict__ sy, int32_t *__restrict__ sz,
                                                                int32_t *__restrict__ box, uint32_t *__restrict__ storeOf,
-                                                               uint32_t *__restrict__ pointLeaf, uint64_t L,
+                                                               uint64_t L,
                                                                double *__restrict__ xyzd, uint64_t nd)
 {
   __shared__ uint32_t v[1024];
@@ -340,7 +340,6 @@ __global__ void __launch_bounds__(kLeafThreads) leafSortKernel(KeyArgs a, const 
     for (int ax = 0; ax < 3; ax++)
       xyzd[(uint64_t)ax * nd + f + t] = wb_decode(q[ax], a.off[ax], a.scale[ax], a.unit);
     storeOf[id] = f + t;
-    pointLeaf[id] = (uint32_t)l;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++)
     {
@@ -519,6 +518,22 @@ static void keyFixedPoint(const WbGeom &g, double mn, double mx, int k, KeyArgs 
   a.eps[k] = (long long)ceil(16 * errCells * one) + 16;
 }
 
+/* The point -> leaf map of every record (leaf of its store slot), formed when
+ * a caller asks for it: the pipeline itself reads store slots only. */
+int wb_point_leaf_map(wb_ctx *c)
+{
+  const uint64_t n = c->n;
+  int rc;
+  if (!n)
+    return 0;
+  if ((rc = wb_ensure(c, c->pointLeaf, n * 4 + 64)))
+    return rc;
+  { pointLeafKernel<<<gridFor(c, n), 256, 0, c->stream>>>(n, (const uint32_t *)c->storeOf.p,
+                                                          (const uint32_t *)c->leafId.p, (uint32_t *)c->pointLeaf.p); ++c->launches; }
+  WB_CUDA(c, cudaGetLastError());
+  return 0;
+}
+
 int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
 {
   if (!cl || !cl->records || cl->stride < 12)
@@ -590,7 +605,7 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   if ((rc = wb_ensure(c, c->key0, n * 8)) || (rc = wb_ensure(c, c->key1, n * 8)) ||
       (rc = wb_ensure(c, c->idx0, n * 4)) || (rc = wb_ensure(c, c->idx1, n * 4)) ||
       (rc = wb_ensure(c, c->tmp32, n * 4)) || (rc = wb_ensure(c, c->storeOf, n * 4)) ||
-      (rc = wb_ensure(c, c->pointLeaf, n * 4)) || (rc = wb_ensure(c, c->survivorOf, n * 4)) ||
+      (rc = wb_ensure(c, c->survivorOf, n * 4)) ||
       (rc = wb_ensure(c, c->small, 4096)))
     return rc;
   uint64_t *keys = (uint64_t *)c->key0.p;
@@ -669,15 +684,14 @@ int wb_build_impl(wb_ctx *c, const wb_cloud *cl)
   uint32_t *storeOf = (uint32_t *)c->storeOf.p;
   { leafSortKernel<<<(unsigned)L, kLeafThreads, 0, c->stream>>>(a, first, count, didx, (uint32_t *)c->sidx.p,
                                                                (int32_t *)c->sx.p, (int32_t *)c->sy.p, (int32_t *)c->sz.p,
-                                                               box, storeOf, (uint32_t *)c->pointLeaf.p, L,
+                                                               box, storeOf, L,
                                                                (double *)c->xyzd.p, nd); ++c->launches; }
   WB_CUDA(c, cudaGetLastError());
   wb_mark(c, "leaf_order");
-  // records a later identical point overwrote take their survivor's slot and leaf
+  // records a later identical point overwrote take their survivor's slot
   if (nd != n)
   {
     { dupMapKernel<<<gridFor(c, n), 256, 0, c->stream>>>(a, keys, idx, surv, storeOf); ++c->launches; }
-    { pointLeafKernel<<<gridFor(c, n), 256, 0, c->stream>>>(n, storeOf, leafId, (uint32_t *)c->pointLeaf.p); ++c->launches; }
   }
   { maxLevelKernel<<<gridFor(c, L), 256, 0, c->stream>>>(L, leafLev, dMax); ++c->launches; }
   int maxLev = 0;

@@ -196,6 +196,7 @@ int wb_radix_sort_pairs(wb_ctx *c, uint64_t *&keys, uint32_t *&vals, uint64_t *k
                         uint64_t n, int beginBit, int endBit);
 
 /* stages */
+int wb_point_leaf_map(wb_ctx *c);   /* point -> leaf map into c->pointLeaf */
 int wb_build_impl(wb_ctx *c, const wb_cloud *cloud);
 int wb_grid_impl(wb_ctx *c, double x0, double y0, double x1, double y1);
 int wb_scan_impl(wb_ctx *c, const wb_params *p);
