@@ -24,7 +24,8 @@ machine only; the fixture keeps what the tests need in little room:
 
     python tests/golden/make_c1_golden.py [--raw DIR]
 
---raw keeps the reference's binary output in DIR and reuses it when present.
+--raw keeps the reference's binary output in DIR and reuses it when present (default: a new
+temporary directory).
 """
 from __future__ import annotations
 
@@ -34,6 +35,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -56,7 +58,7 @@ def main():
     if not os.path.exists(O.REF_BIN):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     cloud = synth.plain_small(seed=1)
-    raw = args.raw or os.path.join(ROOT, "_work", "big", "c1_raw")
+    raw = args.raw or tempfile.mkdtemp(prefix="c1_raw_")
     os.makedirs(raw, exist_ok=True)
     inp = os.path.join(raw, "in.wbxyz")
     out = os.path.join(raw, "ref.out")
