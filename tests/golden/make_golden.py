@@ -7,7 +7,9 @@ files.  Needs the reference source tree (the REF environment variable, passed
 on to `make -C oracle ref`) and runs on the development machine only; the
 tests read the committed .npz files.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [NAME ...]
+
+With names, only those fixtures are written (e.g. `negscale8k`).
 """
 from __future__ import annotations
 
@@ -35,9 +37,21 @@ CASES = {
                                           origin=(3.0, 5.0)), dict(), 3),
     "dups5k": (None, dict(), 3),
     "split": (None, dict(), 1),
+    # x and z record integers running against the coordinates (negative scales)
+    "negscale8k": (lambda: negscale_cloud(), dict(), 3),
 }
 
 SPLIT_PRIMES = [(523, 516), (541, 10), (719, 710), (727, 10), (4289, 17), (4297, 15), (5749, 18), (5779, 5762)]
+
+
+def negscale_cloud():
+    """A seeded tile with its x and z record integers and scales negated: the
+    same decoded points, read through negative scales."""
+    c = synth.density_tile(8000, 23)
+    xyz = c.xyz.copy()
+    xyz[:, 0] = -xyz[:, 0]
+    xyz[:, 2] = -xyz[:, 2]
+    return synth.Cloud(xyz, (-c.scale[0], c.scale[1], -c.scale[2]), c.offset, c.unit, c.minc, c.maxc)
 
 
 def dups_cloud():
@@ -142,9 +156,13 @@ def primitives(tmp):
 def main():
     if not os.path.exists(O.REF_BIN):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as tmp:
-        primitives(tmp)
+        if not only:
+            primitives(tmp)
         for name, (builder, params, phases) in CASES.items():
+            if only and name not in only:
+                continue
             if name == "dups5k":
                 cloud = dups_cloud()
             elif name == "split":

@@ -105,9 +105,10 @@ def test_cylinder_known_points(oracle_mod):
         assert bool(L.wbo_cylinder_in(c.ctypes.data, 13.0, np.array(p, float).ctypes.data)) == exp
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("case", GOLDEN_CASES + ["negscale8k"])
 def test_pipeline_matches_reference(oracle_mod, prim, case):
-    """Serial block numbers, storage order, leaf cubes, tiles and classes, exactly."""
+    """Serial block numbers, storage order, leaf cubes, tiles and classes,
+    exactly (negscale8k: x and z read through negative scales)."""
     oracle_mod.set_tables(prim["tan"], prim["sin"], prim["cos"])
     g = load_golden(case)
     cloud = golden_cloud(g)
